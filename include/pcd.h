@@ -1,0 +1,178 @@
+/*
+ * libpcd — GB300-native (sm_103a) Par-CD refine / merge / score path.
+ *
+ * C ABI: plain pointers and sizes; no CUDA or C++ types in the signatures.
+ * Every entry point returns a pcd_status and never exits the process (the
+ * reference's CUDA_CHECK calls exit(); src/cuda-common.cuh:96-106).
+ *
+ * Threading and ordering: one host thread per pcd_ctx.  A context owns one
+ * CUDA stream (or borrows the caller's, pcd_set_stream); every call is ordered
+ * on it.  Calls that return host-visible results (pcd_compress's num_labels,
+ * pcd_score, pcd_labels_get, pcd_stats_get, pcd_triangles, pcd_contract)
+ * synchronise that stream; pcd_refine and pcd_merge are asynchronous and
+ * capturable.
+ *
+ * Labels are int32.  NEW_LABEL (-1, the reference's ~0 in src/common.hpp:20)
+ * marks a vertex that a propagation sweep moved to a fresh singleton
+ * community; pcd_compress renumbers such labels exactly as compress_labels
+ * does (src/framework.cpp:146-170).
+ */
+#ifndef PCD_H
+#define PCD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PCD_NEW_LABEL (-1)
+
+typedef enum pcd_status {
+    PCD_OK = 0,
+    PCD_ERR_INVALID_ARGUMENT = 1, /* null pointer, size out of range, unknown rule */
+    PCD_ERR_CUDA = 2,             /* a CUDA runtime call failed; see pcd_last_error */
+    PCD_ERR_OUT_OF_MEMORY = 3,    /* device allocation failed */
+    PCD_ERR_FORMAT = 4,           /* graph arrays are not a valid "PCD" CSR */
+    PCD_ERR_DEVICE_TIMEOUT = 5,   /* a bounded device-side wait gave up */
+    PCD_ERR_NOT_READY = 6,        /* call order violated (e.g. WCC before labels) */
+    PCD_ERR_UNSUPPORTED = 7
+} pcd_status;
+
+typedef enum pcd_rule_kind {
+    PCD_RULE_MODULARITY = 0, /* ModularityRule  src/rules.cpp:9-56   */
+    PCD_RULE_CPM = 1,        /* CPMRule         src/rules.cpp:121-148 */
+    PCD_RULE_WCC = 2         /* WCCRule         src/rules.cpp:150-436 */
+} pcd_rule_kind;
+
+/* Replaces the reference's Rule / CudaRule objects (src/rules.hpp:9-19,
+ * src/rules-cuda.cuh:23-30): which objective, plus CPM's resolution. */
+typedef struct pcd_rule {
+    int32_t kind;  /* pcd_rule_kind */
+    double lambda; /* CPM resolution; ignored otherwise */
+} pcd_rule;
+
+typedef struct pcd_ctx pcd_ctx;
+typedef struct pcd_graph pcd_graph;
+
+/* Counters of the last pcd_refine / pcd_merge on a graph (host-visible after
+ * the next synchronising call, or pcd_synchronize). */
+typedef struct pcd_sweep_info {
+    int64_t draws;         /* rand_r calls the sweep consumed */
+    int32_t fallback;      /* vertices re-evaluated in FP64 (see DESIGN) */
+    int32_t resolved;      /* vertices / communities whose tie list was replayed */
+    int32_t kernels;       /* kernel launches issued by the call */
+    int32_t merge_pairs;   /* contracted (a, b) pairs (merge only) */
+} pcd_sweep_info;
+
+const char *pcd_status_string(pcd_status s);
+/* Last detailed error message of a context (never NULL). */
+const char *pcd_last_error(const pcd_ctx *ctx);
+
+/* cuda_init (src/framework-cuda.cu:59-73, declared src/framework-cuda.cuh:14).
+ * Selects `device`, creates the context's stream, uploads constant tables. */
+pcd_status pcd_init(pcd_ctx **ctx, int32_t device);
+/* cuda_deinit (src/framework-cuda.cu:75-78).  Frees every graph of the ctx. */
+pcd_status pcd_destroy(pcd_ctx *ctx);
+/* Order all later work on a caller-owned cudaStream_t (passed as void*);
+ * NULL restores the context's own stream. */
+pcd_status pcd_set_stream(pcd_ctx *ctx, void *cuda_stream);
+pcd_status pcd_synchronize(pcd_ctx *ctx);
+
+/* cuda_transfer_graph (src/framework-cuda.cu:89-133) with Graph::read's
+ * semantics (src/graph.cpp:40-105): n vertices, m undirected edges,
+ * indices[n+1], adj[2m] in HOST memory; rows sorted, no loops, symmetric.
+ * The arrays are copied; the caller keeps ownership.  Validates offsets,
+ * ranges, sortedness and loops (PCD_ERR_FORMAT). */
+pcd_status pcd_load_csr(pcd_ctx *ctx, int32_t n, int32_t m, const int32_t *indices,
+                        const int32_t *adj, pcd_graph **out);
+/* Same, from DEVICE pointers already resident on the context's device. */
+pcd_status pcd_load_csr_device(pcd_ctx *ctx, int32_t n, int32_t m, const int32_t *d_indices,
+                               const int32_t *d_adj, pcd_graph **out);
+pcd_status pcd_graph_free(pcd_graph *g);
+
+/* cuda_labels_to_device / cuda_labels_from_device
+ * (src/framework-cuda.cu:135-143).  Host arrays of n labels. */
+pcd_status pcd_labels_set(pcd_graph *g, const int32_t *labels);
+pcd_status pcd_labels_get(pcd_graph *g, int32_t *labels);
+/* Device-pointer variants (n int32 on the context's device). */
+pcd_status pcd_labels_set_device(pcd_graph *g, const int32_t *d_labels);
+pcd_status pcd_labels_get_device(pcd_graph *g, int32_t *d_labels);
+
+/* compress_labels + collect_statistics (src/framework.cpp:146-170, 69-143;
+ * cuda_collect_statistics src/framework-cuda.cu:235-323): renumber labels by
+ * first occurrence and collect per-community size, internal and external
+ * volume.  num_labels may be NULL (then the call does not synchronise). */
+pcd_status pcd_compress(pcd_graph *g, int32_t *num_labels);
+/* Statistics of the current compressed partition (host arrays of capacity
+ * >= num_labels; any may be NULL). */
+pcd_status pcd_stats_get(pcd_graph *g, int32_t *sizes, int32_t *int_volume, int32_t *ext_volume);
+
+/* Graph::count_triangles (src/graph.cpp:107-175): tri[v] (twice the
+ * triangles through v), tri_deg[v] (edges of v in a triangle) and the mean
+ * local clustering coefficient.  Any output may be NULL.  WCC needs this; the
+ * first WCC call computes it if it has not been. */
+pcd_status pcd_triangles(pcd_graph *g, int32_t *tri, int32_t *tri_deg, double *clustering_coef);
+
+/* Rule::calculate (src/rules.cpp:9-22, 121-129, 150-235;
+ * cuda_calculate_metric src/framework-cuda.cu:164-172) of the current
+ * partition, reduced in FP64.  Compresses first if the labels changed. */
+pcd_status pcd_score(pcd_graph *g, const pcd_rule *rule, double *out);
+
+/* One synchronous label-propagation sweep: PropagationRefinement::refine
+ * (src/refinement.cpp:114-182; cuda_propagation_step
+ * src/framework-cuda.cu:465-633).  `seed` is the rand_r state the reference
+ * draws with rand() at the start of the call; ties and the frac test replay
+ * the same rand_r stream, so labels are bit-exact with the reference's -p 1
+ * schedule.  Compresses first if needed.  Writes the new labels (NEW_LABEL
+ * allowed) to the graph; asynchronous. */
+pcd_status pcd_refine(pcd_graph *g, const pcd_rule *rule, double frac, uint32_t seed);
+
+/* Mutual-best community merging: MergingRefinement::refine
+ * (src/refinement.cpp:185-288; cuda_merging_step
+ * src/framework-cuda.cu:744-892), built as a sort by (a, b) community pair
+ * plus segmented reduce (the contracted edge weights), then `rounds` rounds of
+ * best-partner selection and matching.  Asynchronous. */
+pcd_status pcd_merge(pcd_graph *g, const pcd_rule *rule, int32_t rounds, uint32_t seed);
+
+/* Contracted edge weights of the current compressed partition: every ordered
+ * pair (a, b), a != b, of communities joined by w > 0 edges, sorted by
+ * (a, b).  Writes min(cap, pairs) triples and the pair count. */
+pcd_status pcd_contract(pcd_graph *g, int64_t cap, int32_t *a, int32_t *b, int32_t *w,
+                        int64_t *num_pairs);
+
+pcd_status pcd_sweep_info_get(pcd_graph *g, pcd_sweep_info *info);
+
+/* Per-phase device timing (the reference's CudaTimer spans,
+ * src/cuda-common.cuh:253-316): while enabled, pcd_refine / pcd_merge /
+ * pcd_compress record CUDA events between their kernel groups on the
+ * context's stream.  pcd_profile_read synchronises and writes up to `cap`
+ * (phase name, milliseconds) pairs of the most recent call; returns the number
+ * of phases (or -1 on error).  Names are static strings. */
+pcd_status pcd_profile_enable(pcd_ctx *ctx, int32_t on);
+int32_t pcd_profile_read(pcd_ctx *ctx, const char **names, double *ms, int32_t cap);
+
+/* Host-side seed stream: glibc rand() restated (default seed 1 = never
+ * srand'ed), so a driver can hand pcd_refine / pcd_merge the same seed the
+ * reference draws at src/refinement.cpp:123-124 and :217-218.  Replaces the
+ * reference's use of the process-wide libc generator. */
+typedef struct pcd_rand {
+    uint32_t r[34];
+    int32_t pos;
+} pcd_rand;
+void pcd_rand_seed(pcd_rand *s, uint32_t seed);   /* srand(seed) */
+int32_t pcd_rand_next(pcd_rand *s);               /* rand()      */
+void pcd_rand_skip(pcd_rand *s, int64_t count);   /* count x rand() */
+
+/* Initial partitions, computed on the host as the reference does:
+ * create_singleton_partition (src/framework.cpp:14-24) draws n values from s;
+ * create_clustering_partition (src/framework.cpp:27-59) needs tri[] from
+ * pcd_triangles.  Host arrays. */
+pcd_status pcd_singleton_partition(pcd_rand *s, int32_t n, int32_t *labels);
+pcd_status pcd_clustering_partition(int32_t n, const int32_t *indices, const int32_t *adj,
+                                    const int32_t *tri, int32_t *labels);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PCD_H */

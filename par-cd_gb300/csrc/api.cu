@@ -1,0 +1,515 @@
+// The C ABI of libpcd (include/pcd.h): contexts, graphs, and the phase
+// entry points that replace the reference's GPU host API
+// (src/framework-cuda.cuh:14-23) and its CPU phase functions.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "pcd_internal.h"
+
+using namespace pcd;
+
+namespace pcd {
+
+pcd_status set_error(pcd_ctx *ctx, pcd_status s, const std::string &msg) {
+    if (ctx) ctx->last_error = msg;
+    return s;
+}
+
+pcd_status check_cuda(pcd_ctx *ctx, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return PCD_OK;
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    return set_error(ctx, e == cudaErrorMemoryAllocation ? PCD_ERR_OUT_OF_MEMORY : PCD_ERR_CUDA, m);
+}
+
+pcd_status dev_alloc(pcd_graph *g, void **p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return check_cuda(g->ctx, e, "cudaMalloc");
+    }
+    g->allocs.push_back(*p);
+    return PCD_OK;
+}
+
+__global__ void k_degree_max(const int32_t *indices, int32_t n, int32_t *out) {
+    int32_t mx = 0;
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        mx = max(mx, indices[v + 1] - indices[v]);
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    if ((threadIdx.x & 31) == 0) atomicMax(out, mx);
+}
+
+static void prof_record(pcd_ctx *ctx, const char *name, cudaStream_t st) {
+    if (ctx->prof_used == ctx->prof_pool.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return;
+        ctx->prof_pool.push_back(e);
+        ctx->prof_names.push_back(nullptr);
+    }
+    ctx->prof_names[ctx->prof_used] = name;
+    cudaEventRecord(ctx->prof_pool[ctx->prof_used], st);
+    ++ctx->prof_used;
+}
+
+void prof_begin(pcd_ctx *ctx, cudaStream_t st) {
+    if (!ctx->prof_on) return;
+    ctx->prof_used = 0;
+    prof_record(ctx, "begin", st);
+}
+
+void prof_mark(pcd_ctx *ctx, const char *name, cudaStream_t st) {
+    if (!ctx->prof_on || ctx->prof_used == 0) return;
+    prof_record(ctx, name, st);
+}
+
+}  // namespace pcd
+
+#define CK(call, what)                                          \
+    do {                                                        \
+        pcd_status _s = check_cuda(ctx, (call), what);          \
+        if (_s != PCD_OK) return _s;                            \
+    } while (0)
+
+#define TRY(expr)                          \
+    do {                                   \
+        pcd_status _s = (expr);            \
+        if (_s != PCD_OK) return _s;       \
+    } while (0)
+
+static pcd_status scan_guard(pcd_graph *g) {
+    if (!g->scan_overflow) return PCD_OK;
+    g->scan_overflow = 0;
+    return set_error(g->ctx, PCD_ERR_CUDA, "internal: a device scan exceeded its scratch (nothing was launched)");
+}
+
+static pcd_status sync_and_check(pcd_graph *g) {
+    pcd_ctx *ctx = g->ctx;
+    TRY(scan_guard(g));
+    CK(cudaMemcpyAsync(g->h_ctr, g->ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, ctx->stream),
+       "counters");
+    CK(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+    int32_t err = g->h_ctr->error;
+    if (err) {
+        char buf[160];
+        snprintf(buf, sizeof buf, "device error flags 0x%x (1 tie buffer, 2 wait limit, 4 scratch, 8 label range)",
+                 (unsigned)err);
+        cudaMemsetAsync(&g->ctr->error, 0, sizeof(int32_t), ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
+        pcd_status s = (err & ERR_WAIT_TIMEOUT) ? PCD_ERR_DEVICE_TIMEOUT
+                       : (err & ERR_LABEL_RANGE) ? PCD_ERR_INVALID_ARGUMENT
+                                                 : PCD_ERR_CUDA;
+        return set_error(ctx, s, buf);
+    }
+    g->info.draws = g->h_ctr->total_draws;
+    g->info.fallback = g->h_ctr->n_ambiguous;
+    g->info.resolved = g->h_ctr->n_resolve;
+    g->info.merge_pairs = g->h_ctr->n_pairs;
+    return PCD_OK;
+}
+
+extern "C" {
+
+const char *pcd_status_string(pcd_status s) {
+    switch (s) {
+        case PCD_OK: return "ok";
+        case PCD_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case PCD_ERR_CUDA: return "CUDA error";
+        case PCD_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case PCD_ERR_FORMAT: return "invalid graph format";
+        case PCD_ERR_DEVICE_TIMEOUT: return "device wait limit reached";
+        case PCD_ERR_NOT_READY: return "call order violated";
+        case PCD_ERR_UNSUPPORTED: return "unsupported";
+    }
+    return "unknown status";
+}
+
+const char *pcd_last_error(const pcd_ctx *ctx) { return ctx ? ctx->last_error.c_str() : "no context"; }
+
+pcd_status pcd_init(pcd_ctx **out, int32_t device) {
+    if (!out) return PCD_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    pcd_ctx *ctx = new (std::nothrow) pcd_ctx;
+    if (!ctx) return PCD_ERR_OUT_OF_MEMORY;
+    ctx->device = device;
+    pcd_status s = check_cuda(ctx, cudaSetDevice(device), "cudaSetDevice");
+    if (s == PCD_OK) s = check_cuda(ctx, cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking),
+                                    "cudaStreamCreate");
+    if (s == PCD_OK) {
+        ctx->stream = ctx->own_stream;
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        ctx->num_sms = sms > 0 ? sms : 1;
+        int optin = 0;
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+        ctx->smem_optin = (size_t)optin;
+        upload_jump_table(ctx->stream);
+        s = check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "pcd_init");
+    }
+    if (s != PCD_OK) {
+        // keep the context so the caller can read the message, but mark it unusable
+        if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+        ctx->own_stream = ctx->stream = nullptr;
+        *out = ctx;
+        return s;
+    }
+    *out = ctx;
+    return PCD_OK;
+}
+
+pcd_status pcd_graph_free(pcd_graph *g) {
+    if (!g) return PCD_ERR_INVALID_ARGUMENT;
+    pcd_ctx *ctx = g->ctx;
+    if (ctx && ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (void *p : g->allocs) cudaFree(p);
+    if (g->merge_buf) cudaFree(g->merge_buf);
+    if (g->h_ctr) cudaFreeHost(g->h_ctr);
+    if (ctx) ctx->graphs.erase(std::remove(ctx->graphs.begin(), ctx->graphs.end(), g), ctx->graphs.end());
+    delete g;
+    return PCD_OK;
+}
+
+pcd_status pcd_destroy(pcd_ctx *ctx) {
+    if (!ctx) return PCD_ERR_INVALID_ARGUMENT;
+    while (!ctx->graphs.empty()) pcd_graph_free(ctx->graphs.back());
+    for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
+    if (ctx->own_stream) {
+        cudaStreamSynchronize(ctx->own_stream);
+        cudaStreamDestroy(ctx->own_stream);
+    }
+    delete ctx;
+    return PCD_OK;
+}
+
+pcd_status pcd_set_stream(pcd_ctx *ctx, void *stream) {
+    if (!ctx || !ctx->own_stream) return PCD_ERR_INVALID_ARGUMENT;
+    CK(cudaStreamSynchronize(ctx->stream), "pcd_set_stream");
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return PCD_OK;
+}
+
+pcd_status pcd_profile_enable(pcd_ctx *ctx, int32_t on) {
+    if (!ctx) return PCD_ERR_INVALID_ARGUMENT;
+    ctx->prof_on = on != 0;
+    ctx->prof_used = 0;
+    return PCD_OK;
+}
+
+int32_t pcd_profile_read(pcd_ctx *ctx, const char **names, double *ms, int32_t cap) {
+    if (!ctx || !ctx->stream) return -1;
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return -1;
+    const int32_t nph = ctx->prof_used > 0 ? (int32_t)ctx->prof_used - 1 : 0;
+    for (int32_t i = 0; i < nph && i < cap; ++i) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, ctx->prof_pool[i], ctx->prof_pool[i + 1]);
+        if (names) names[i] = ctx->prof_names[i + 1];
+        if (ms) ms[i] = t;
+    }
+    return nph;
+}
+
+pcd_status pcd_synchronize(pcd_ctx *ctx) {
+    if (!ctx || !ctx->stream) return PCD_ERR_INVALID_ARGUMENT;
+    CK(cudaStreamSynchronize(ctx->stream), "pcd_synchronize");
+    return PCD_OK;
+}
+
+static pcd_status graph_setup(pcd_ctx *ctx, pcd_graph *g) {
+    const int64_t n = g->n, nn = std::max<int64_t>(n, 1);
+    cudaStream_t st = ctx->stream;
+    // validation + max degree
+    int32_t *flag = nullptr;
+    TRY(dev_alloc(g, (void **)&flag, 2 * sizeof(int32_t)));
+    CK(cudaMemsetAsync(flag, 0, 2 * sizeof(int32_t), st), "memset");
+    if (n > 0) {
+        launch_validate(g->indices, g->adj, g->n, g->m, flag, st);
+        k_degree_max<<<std::max(1, std::min<int>((int)((n + 255) / 256), ctx->num_sms * 8)), 256, 0, st>>>(
+            g->indices, g->n, flag + 1);
+    }
+    int32_t h[2] = {0, 0};
+    CK(cudaMemcpyAsync(h, flag, sizeof h, cudaMemcpyDeviceToHost, st), "validate");
+    CK(cudaStreamSynchronize(st), "validate");
+    if (h[0]) {
+        char buf[128];
+        snprintf(buf, sizeof buf, "graph arrays are not a valid CSR (flags 0x%x: 1 span, 2 offsets, 4 rows)", h[0]);
+        return set_error(ctx, PCD_ERR_FORMAT, buf);
+    }
+    g->max_deg = h[1];
+    // partition state and sweep scratch
+    TRY(dev_alloc(g, (void **)&g->labels, sizeof(int32_t) * nn));
+    TRY(dev_alloc(g, (void **)&g->labels_alt, sizeof(int32_t) * nn));
+    TRY(dev_alloc(g, (void **)&g->first, sizeof(int32_t) * nn));
+    TRY(dev_alloc(g, (void **)&g->sizes, sizeof(int32_t) * nn));
+    TRY(dev_alloc(g, (void **)&g->intv, sizeof(int32_t) * nn));
+    TRY(dev_alloc(g, (void **)&g->extv, sizeof(int32_t) * nn));
+    TRY(dev_alloc(g, (void **)&g->vol, sizeof(int32_t) * nn));
+    TRY(dev_alloc(g, (void **)&g->ndraw, sizeof(uint32_t) * nn));
+    // scans run over vertices, communities, edges (merge) and radix histograms
+    const int64_t scan_items = std::max<int64_t>({n, g->nnz, 256ll * 2 * ctx->num_sms, 1});
+    const int64_t tile_cap = (scan_items + 2047) / 2048 + 2;
+    TRY(dev_alloc(g, (void **)&g->tile_sums, sizeof(uint32_t) * (size_t)tile_cap));
+    TRY(dev_alloc(g, (void **)&g->scan_total, sizeof(uint32_t) * 4));
+    g->scan = ScanScratch{g->tile_sums, tile_cap, g->scan_total, &g->scan_overflow};
+    g->tiebuf_cap = g->nnz + n + 16;
+    TRY(dev_alloc(g, (void **)&g->tiebuf, sizeof(int32_t) * (size_t)g->tiebuf_cap));
+    TRY(dev_alloc(g, (void **)&g->recs, sizeof(TieRecord) * nn));
+    TRY(dev_alloc(g, (void **)&g->amb, sizeof(int32_t) * nn));
+    TRY(dev_alloc(g, (void **)&g->ctr, sizeof(DevCounters)));
+    TRY(dev_alloc(g, (void **)&g->small, 65536));
+    TRY(dev_alloc(g, (void **)&g->d_score, 64));
+    TRY(dev_alloc(g, (void **)&g->bin_list, sizeof(int32_t) * nn));
+    CK(cudaMallocHost((void **)&g->h_ctr, sizeof(DevCounters)), "cudaMallocHost");
+    CK(cudaMemsetAsync(g->ctr, 0, sizeof(DevCounters), st), "memset");
+    // hub / FP64 re-evaluation tables: one HBM slice per resident block
+    int64_t slots = 64;
+    while (slots < 2 * (int64_t)std::max(g->max_deg, 1)) slots <<= 1;
+    g->hub_slots = slots;
+    const int64_t per_block = 3 * slots + g->max_deg;
+    int64_t blocks = std::min<int64_t>(ctx->num_sms, std::max<int64_t>(8, (int64_t)(2ll << 30) / (4 * per_block)));
+    g->hub_blocks = (int32_t)std::max<int64_t>(1, blocks);
+    TRY(dev_alloc(g, (void **)&g->hub_scratch, sizeof(int32_t) * (size_t)(per_block * g->hub_blocks)));
+    // degree bins
+    g->bins = BinConfig{16, 128, 1024, 4096};
+    if (n > 0) launch_bins(g, st);
+    // initial labels: singletons 0..n-1 (already compressed)
+    g->k = g->n;
+    g->compressed = false;
+    CK(cudaStreamSynchronize(st), "graph setup");
+    return PCD_OK;
+}
+
+__global__ void k_iota(int32_t *p, int32_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = (int32_t)i;
+}
+
+static pcd_status load_common(pcd_ctx *ctx, int32_t n, int32_t m, const int32_t *indices, const int32_t *adj,
+                              cudaMemcpyKind kind, pcd_graph **out) {
+    if (!ctx || !ctx->stream || !out) return PCD_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (n < 0 || m < 0 || (int64_t)2 * m > INT32_MAX) return set_error(ctx, PCD_ERR_INVALID_ARGUMENT, "n or m out of range");
+    if (!indices || (m > 0 && !adj)) return set_error(ctx, PCD_ERR_INVALID_ARGUMENT, "null CSR array");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    pcd_graph *g = new (std::nothrow) pcd_graph;
+    if (!g) return PCD_ERR_OUT_OF_MEMORY;
+    g->ctx = ctx;
+    g->n = n;
+    g->m = m;
+    g->nnz = 2 * (int64_t)m;
+    pcd_status s = dev_alloc(g, (void **)&g->indices, sizeof(int32_t) * ((size_t)n + 1));
+    if (s == PCD_OK) s = dev_alloc(g, (void **)&g->adj, sizeof(int32_t) * (size_t)std::max<int64_t>(g->nnz, 1));
+    if (s == PCD_OK)
+        s = check_cuda(ctx, cudaMemcpyAsync(g->indices, indices, sizeof(int32_t) * ((size_t)n + 1), kind, ctx->stream),
+                       "copy indices");
+    if (s == PCD_OK && g->nnz)
+        s = check_cuda(ctx, cudaMemcpyAsync(g->adj, adj, sizeof(int32_t) * (size_t)g->nnz, kind, ctx->stream),
+                       "copy adj");
+    if (s == PCD_OK) s = graph_setup(ctx, g);
+    if (s == PCD_OK && n > 0) {
+        k_iota<<<std::max(1, std::min<int>((n + 255) / 256, ctx->num_sms * 8)), 256, 0, ctx->stream>>>(g->labels, n);
+        s = check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "init labels");
+    }
+    if (s != PCD_OK) {
+        for (void *p : g->allocs) cudaFree(p);
+        if (g->h_ctr) cudaFreeHost(g->h_ctr);
+        delete g;
+        return s;
+    }
+    ctx->graphs.push_back(g);
+    *out = g;
+    return PCD_OK;
+}
+
+pcd_status pcd_load_csr(pcd_ctx *ctx, int32_t n, int32_t m, const int32_t *indices, const int32_t *adj,
+                        pcd_graph **out) {
+    return load_common(ctx, n, m, indices, adj, cudaMemcpyHostToDevice, out);
+}
+
+pcd_status pcd_load_csr_device(pcd_ctx *ctx, int32_t n, int32_t m, const int32_t *d_indices, const int32_t *d_adj,
+                               pcd_graph **out) {
+    return load_common(ctx, n, m, d_indices, d_adj, cudaMemcpyDeviceToDevice, out);
+}
+
+pcd_status pcd_labels_set(pcd_graph *g, const int32_t *labels) {
+    if (!g || (!labels && g->n)) return PCD_ERR_INVALID_ARGUMENT;
+    pcd_ctx *ctx = g->ctx;
+    for (int32_t v = 0; v < g->n; ++v)
+        if (labels[v] < -1 || labels[v] >= g->n)
+            return set_error(ctx, PCD_ERR_INVALID_ARGUMENT, "label out of range [-1, n)");
+    CK(cudaMemcpyAsync(g->labels, labels, sizeof(int32_t) * (size_t)g->n, cudaMemcpyHostToDevice, ctx->stream),
+       "labels_set");
+    CK(cudaStreamSynchronize(ctx->stream), "labels_set");
+    g->compressed = false;
+    return PCD_OK;
+}
+
+pcd_status pcd_labels_set_device(pcd_graph *g, const int32_t *d_labels) {
+    if (!g || (!d_labels && g->n)) return PCD_ERR_INVALID_ARGUMENT;
+    pcd_ctx *ctx = g->ctx;
+    CK(cudaMemcpyAsync(g->labels, d_labels, sizeof(int32_t) * (size_t)g->n, cudaMemcpyDeviceToDevice, ctx->stream),
+       "labels_set_device");
+    g->compressed = false;  // range checked on the device by the next compress
+    return PCD_OK;
+}
+
+pcd_status pcd_labels_get(pcd_graph *g, int32_t *labels) {
+    if (!g || (!labels && g->n)) return PCD_ERR_INVALID_ARGUMENT;
+    pcd_ctx *ctx = g->ctx;
+    CK(cudaMemcpyAsync(labels, g->labels, sizeof(int32_t) * (size_t)g->n, cudaMemcpyDeviceToHost, ctx->stream),
+       "labels_get");
+    return sync_and_check(g);
+}
+
+pcd_status pcd_labels_get_device(pcd_graph *g, int32_t *d_labels) {
+    if (!g || (!d_labels && g->n)) return PCD_ERR_INVALID_ARGUMENT;
+    pcd_ctx *ctx = g->ctx;
+    CK(cudaMemcpyAsync(d_labels, g->labels, sizeof(int32_t) * (size_t)g->n, cudaMemcpyDeviceToDevice, ctx->stream),
+       "labels_get_device");
+    return PCD_OK;
+}
+
+static pcd_status ensure_compressed(pcd_graph *g, int *launches) {
+    if (g->compressed) return PCD_OK;
+    if (g->n > 0) *launches += launch_compress(g, g->ctx->stream);
+    g->compressed = true;
+    return check_cuda(g->ctx, cudaGetLastError(), "compress launch");
+}
+
+pcd_status pcd_compress(pcd_graph *g, int32_t *num_labels) {
+    if (!g) return PCD_ERR_INVALID_ARGUMENT;
+    int launches = 0;
+    if (!g->compressed) prof_begin(g->ctx, g->ctx->stream);
+    TRY(ensure_compressed(g, &launches));
+    if (launches) prof_mark(g->ctx, "compress+stats", g->ctx->stream);
+    if (num_labels) {
+        TRY(sync_and_check(g));
+        g->k = g->n > 0 ? g->h_ctr->k : 0;
+        *num_labels = g->k;
+    }
+    return PCD_OK;
+}
+
+pcd_status pcd_stats_get(pcd_graph *g, int32_t *sizes, int32_t *int_volume, int32_t *ext_volume) {
+    if (!g) return PCD_ERR_INVALID_ARGUMENT;
+    int32_t k;
+    TRY(pcd_compress(g, &k));
+    pcd_ctx *ctx = g->ctx;
+    size_t b = sizeof(int32_t) * (size_t)k;
+    if (sizes) CK(cudaMemcpyAsync(sizes, g->sizes, b, cudaMemcpyDeviceToHost, ctx->stream), "stats");
+    if (int_volume) CK(cudaMemcpyAsync(int_volume, g->intv, b, cudaMemcpyDeviceToHost, ctx->stream), "stats");
+    if (ext_volume) CK(cudaMemcpyAsync(ext_volume, g->extv, b, cudaMemcpyDeviceToHost, ctx->stream), "stats");
+    CK(cudaStreamSynchronize(ctx->stream), "stats");
+    return PCD_OK;
+}
+
+static pcd_status ensure_triangles(pcd_graph *g) {
+    if (g->have_tri) return PCD_OK;
+    pcd_ctx *ctx = g->ctx;
+    const size_t nn = (size_t)std::max(g->n, 1);
+    if (!g->tri) {
+        TRY(dev_alloc(g, (void **)&g->tri, sizeof(int32_t) * nn));
+        TRY(dev_alloc(g, (void **)&g->tri_deg, sizeof(int32_t) * nn));
+    }
+    double cc = 0.0;
+    if (g->n > 0) {
+        launch_triangles(g, ctx->stream);
+        CK(cudaMemcpyAsync(&cc, g->d_score, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "triangles");
+    }
+    CK(cudaStreamSynchronize(ctx->stream), "triangles");
+    g->cc = cc;
+    g->have_tri = true;
+    return PCD_OK;
+}
+
+pcd_status pcd_triangles(pcd_graph *g, int32_t *tri, int32_t *tri_deg, double *clustering_coef) {
+    if (!g) return PCD_ERR_INVALID_ARGUMENT;
+    TRY(ensure_triangles(g));
+    pcd_ctx *ctx = g->ctx;
+    size_t b = sizeof(int32_t) * (size_t)g->n;
+    if (tri) CK(cudaMemcpyAsync(tri, g->tri, b, cudaMemcpyDeviceToHost, ctx->stream), "tri");
+    if (tri_deg) CK(cudaMemcpyAsync(tri_deg, g->tri_deg, b, cudaMemcpyDeviceToHost, ctx->stream), "tri_deg");
+    CK(cudaStreamSynchronize(ctx->stream), "tri");
+    if (clustering_coef) *clustering_coef = g->cc;
+    return PCD_OK;
+}
+
+static pcd_status check_rule(pcd_graph *g, const pcd_rule *r) {
+    if (!g) return PCD_ERR_INVALID_ARGUMENT;
+    if (!r || r->kind < 0 || r->kind > 2) return set_error(g->ctx, PCD_ERR_INVALID_ARGUMENT, "unknown rule");
+    return PCD_OK;
+}
+
+pcd_status pcd_score(pcd_graph *g, const pcd_rule *rule, double *out) {
+    TRY(check_rule(g, rule));
+    if (!out) return PCD_ERR_INVALID_ARGUMENT;
+    pcd_ctx *ctx = g->ctx;
+    if (rule->kind == PCD_RULE_WCC) TRY(ensure_triangles(g));
+    int launches = 0;
+    TRY(ensure_compressed(g, &launches));
+    if (g->n == 0) {
+        *out = 0.0;
+        return PCD_OK;
+    }
+    if (rule->kind == PCD_RULE_WCC)
+        launch_wcc_score(g, g->d_score, ctx->stream);
+    else
+        launch_score(g, rule->kind, rule->lambda, g->d_score, ctx->stream);
+    CK(cudaMemcpyAsync(out, g->d_score, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "score");
+    return sync_and_check(g);
+}
+
+pcd_status pcd_refine(pcd_graph *g, const pcd_rule *rule, double frac, uint32_t seed) {
+    TRY(check_rule(g, rule));
+    if (!(frac > 0.0 && frac <= 1.0))
+        return set_error(g->ctx, PCD_ERR_INVALID_ARGUMENT, "fraction should be in (0, 1]");
+    if (rule->kind == PCD_RULE_WCC) TRY(ensure_triangles(g));
+    int launches = 0;
+    prof_begin(g->ctx, g->ctx->stream);
+    TRY(ensure_compressed(g, &launches));
+    if (launches) prof_mark(g->ctx, "compress+stats", g->ctx->stream);
+    if (g->n > 0) {
+        launches += launch_refine(g, rule->kind, rule->lambda, frac, seed, g->ctx->stream);
+        std::swap(g->labels, g->labels_alt);
+    }
+    g->compressed = false;
+    g->info.kernels = launches;
+    TRY(scan_guard(g));
+    return check_cuda(g->ctx, cudaGetLastError(), "refine launch");
+}
+
+pcd_status pcd_merge(pcd_graph *g, const pcd_rule *rule, int32_t rounds, uint32_t seed) {
+    TRY(check_rule(g, rule));
+    if (rounds <= 0) return set_error(g->ctx, PCD_ERR_INVALID_ARGUMENT, "number of rounds should be positive");
+    if (rule->kind == PCD_RULE_WCC) TRY(ensure_triangles(g));
+    int launches = 0;
+    prof_begin(g->ctx, g->ctx->stream);
+    TRY(ensure_compressed(g, &launches));
+    if (launches) prof_mark(g->ctx, "compress+stats", g->ctx->stream);
+    if (g->n > 0) {
+        TRY(run_merge(g, rule->kind, rule->lambda, rounds, seed, g->ctx->stream, &launches));
+        std::swap(g->labels, g->labels_alt);
+    }
+    g->compressed = false;
+    g->info.kernels = launches;
+    TRY(scan_guard(g));
+    return check_cuda(g->ctx, cudaGetLastError(), "merge launch");
+}
+
+pcd_status pcd_contract(pcd_graph *g, int64_t cap, int32_t *a, int32_t *b, int32_t *w, int64_t *num_pairs) {
+    if (!g || !num_pairs || cap < 0 || (cap > 0 && (!a || !b || !w))) return PCD_ERR_INVALID_ARGUMENT;
+    int launches = 0;
+    TRY(ensure_compressed(g, &launches));
+    return run_contract(g, cap, a, b, w, num_pairs, g->ctx->stream);
+}
+
+pcd_status pcd_sweep_info_get(pcd_graph *g, pcd_sweep_info *info) {
+    if (!g || !info) return PCD_ERR_INVALID_ARGUMENT;
+    TRY(sync_and_check(g));
+    *info = g->info;
+    return PCD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,341 @@
+// Partition bookkeeping on the device:
+//   * compress  : first-occurrence relabel  (compress_labels, src/framework.cpp:146-170)
+//   * stats     : per-community size / internal / external volume
+//                 (collect_statistics, src/framework.cpp:69-143)
+//   * score     : Rule::calculate for Modularity and CPM (src/rules.cpp:9-22, 121-129)
+//   * validate  : the CSR checks Graph::read leaves implicit
+//   * bins      : vertices grouped by degree class for the sweep kernels
+#include <climits>
+
+#include "pcd_internal.h"
+#include "pcd_scan.cuh"
+
+namespace pcd {
+
+// ---------------------------------------------------------------------------
+// scan of tile sums (declared in pcd_scan.cuh)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_scan_tile_sums(uint32_t *tile_sums, int64_t ntiles, uint32_t *total) {
+    uint32_t carry = 0;
+    for (int64_t base = 0; base < ntiles; base += blockDim.x) {
+        int64_t i = base + threadIdx.x;
+        uint32_t x = i < ntiles ? tile_sums[i] : 0u;
+        uint32_t tot;
+        uint32_t ex = block_excl_sum_u32(x, &tot);
+        if (i < ntiles) tile_sums[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_fill_i32(int32_t *p, int32_t v, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+static inline unsigned grid_for(int64_t n, int threads, int cap = 152 * 32) {
+    int64_t g = (n + threads - 1) / threads;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (unsigned)g;
+}
+
+// ---------------------------------------------------------------------------
+// compress_labels: label L keeps the rank of its first vertex among all
+// "first occurrences" (first vertex of each label, and every NEW_LABEL vertex).
+// ---------------------------------------------------------------------------
+__global__ void k_first_occurrence(const int32_t *__restrict__ labels, int32_t n, int32_t *first,
+                                   DevCounters *ctr) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        int32_t L = labels[v];
+        if (L >= 0 && L < n)
+            atomicMin(first + L, (int32_t)v);
+        else if (L != -1)
+            atomicOr(&ctr->error, ERR_LABEL_RANGE);
+    }
+}
+
+struct FirstFlag {
+    const int32_t *labels;
+    const int32_t *first;
+    int32_t n;
+    __device__ uint32_t operator()(int64_t v) const {
+        int32_t L = labels[v];
+        if (L < 0 || L >= n) return 1u;
+        return first[L] == (int32_t)v ? 1u : 0u;
+    }
+};
+
+struct StoreRank {
+    int32_t *rank;
+    __device__ void operator()(int64_t v, uint32_t x, uint32_t) const { rank[v] = (int32_t)x; }
+};
+
+__global__ void k_relabel(int32_t *labels, const int32_t *__restrict__ rank, const int32_t *__restrict__ first,
+                          int32_t n) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        int32_t L = labels[v];
+        labels[v] = (L < 0 || L >= n) ? rank[v] : rank[first[L]];
+    }
+}
+
+__global__ void k_set_k(DevCounters *ctr, const uint32_t *total) { ctr->k = (int32_t)*total; }
+
+// ---------------------------------------------------------------------------
+// collect_statistics.  sizes[l] += 1, intv[l] += d_int, extv[l] += d_ext,
+// vol[l] += deg.  Integer sums: the result does not depend on order.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void add_stats(int32_t l, int32_t di, int32_t de, int32_t *sizes, int32_t *intv,
+                                          int32_t *extv, int32_t *vol, bool valid) {
+    // lanes of the warp that share a community add once, through their leader
+    const int lane = threadIdx.x & 31;
+    unsigned act = __ballot_sync(FULL, valid);
+    if (!valid) return;
+    unsigned peers = __match_any_sync(act, l);
+    int s = __reduce_add_sync(peers, 1);
+    int a = __reduce_add_sync(peers, di);
+    int b = __reduce_add_sync(peers, de);
+    if (lane == __ffs(peers) - 1) {
+        atomicAdd(sizes + l, s);
+        atomicAdd(intv + l, a);
+        atomicAdd(extv + l, b);
+        atomicAdd(vol + l, a + b);
+    }
+}
+
+__global__ void k_stats_thread(const int32_t *__restrict__ indices, const int32_t *__restrict__ adj,
+                               const int32_t *__restrict__ labels, const int32_t *__restrict__ list,
+                               int64_t count, int32_t *sizes, int32_t *intv, int32_t *extv, int32_t *vol) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t start = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t rounds = (count + stride - 1) / stride;
+    for (int64_t r = 0; r < rounds; ++r) {
+        int64_t idx = start + r * stride;
+        bool valid = idx < count;
+        int32_t l = 0, di = 0, de = 0;
+        if (valid) {
+            int32_t v = list[idx];
+            l = labels[v];
+            int32_t b = indices[v], e = indices[v + 1];
+            for (int32_t j = b; j < e; ++j) di += (labels[adj[j]] == l);
+            de = (e - b) - di;
+        }
+        add_stats(l, di, de, sizes, intv, extv, vol, valid);
+    }
+}
+
+__global__ void k_stats_warp(const int32_t *__restrict__ indices, const int32_t *__restrict__ adj,
+                             const int32_t *__restrict__ labels, const int32_t *__restrict__ list,
+                             int64_t count, int32_t *sizes, int32_t *intv, int32_t *extv, int32_t *vol) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t idx = warp; idx < count; idx += nwarps) {
+        int32_t v = list[idx];
+        int32_t l = labels[v];
+        int32_t b = indices[v], e = indices[v + 1];
+        int32_t di = 0;
+        for (int32_t j = b + lane; j < e; j += 32) di += (labels[adj[j]] == l);
+#pragma unroll
+        for (int d = 16; d; d >>= 1) di += __shfl_xor_sync(FULL, di, d);
+        if (lane == 0) {
+            int32_t de = (e - b) - di;
+            atomicAdd(sizes + l, 1);
+            atomicAdd(intv + l, di);
+            atomicAdd(extv + l, de);
+            atomicAdd(vol + l, e - b);
+        }
+    }
+}
+
+int launch_stats(pcd_graph *g, cudaStream_t st) {
+    int launches = 0;
+    size_t bytes = sizeof(int32_t) * (size_t)(g->n > 0 ? g->n : 1);
+    cudaMemsetAsync(g->sizes, 0, bytes, st);
+    cudaMemsetAsync(g->intv, 0, bytes, st);
+    cudaMemsetAsync(g->extv, 0, bytes, st);
+    cudaMemsetAsync(g->vol, 0, bytes, st);
+    int64_t nt = g->bin_off[BIN_THREAD + 1] - g->bin_off[BIN_THREAD];
+    if (nt > 0) {
+        k_stats_thread<<<grid_for(nt, 256), 256, 0, st>>>(g->indices, g->adj, g->labels,
+                                                           g->bin_list + g->bin_off[BIN_THREAD], nt, g->sizes,
+                                                           g->intv, g->extv, g->vol);
+        ++launches;
+    }
+    int64_t nw = g->bin_off[NBINS] - g->bin_off[BIN_WARP];
+    if (nw > 0) {
+        k_stats_warp<<<grid_for(nw * 32, 256), 256, 0, st>>>(g->indices, g->adj, g->labels,
+                                                             g->bin_list + g->bin_off[BIN_WARP], nw, g->sizes,
+                                                             g->intv, g->extv, g->vol);
+        ++launches;
+    }
+    return launches;
+}
+
+int launch_compress(pcd_graph *g, cudaStream_t st) {
+    int launches = 0;
+    const int32_t n = g->n;
+    k_fill_i32<<<grid_for(n, 256), 256, 0, st>>>(g->first, INT_MAX, n);
+    k_first_occurrence<<<grid_for(n, 256), 256, 0, st>>>(g->labels, n, g->first, g->ctr);
+    launches += 2;
+    launches += scan_exclusive(FirstFlag{g->labels, g->first, n}, StoreRank{g->labels_alt}, n, g->scan, st);
+    k_relabel<<<grid_for(n, 256), 256, 0, st>>>(g->labels, g->labels_alt, g->first, n);
+    k_set_k<<<1, 1, 0, st>>>(g->ctr, g->scan_total);
+    launches += 2;
+    launches += launch_stats(g, st);
+    return launches;
+}
+
+// ---------------------------------------------------------------------------
+// Rule::calculate for Modularity / CPM: per-community FP64 terms in the
+// reference's expression order, summed with a deterministic double-double
+// reduction (fixed grid, fixed tree).
+// ---------------------------------------------------------------------------
+struct DD {
+    double hi, lo;
+};
+
+__device__ __forceinline__ DD dd_add(DD a, double b) {
+    double s = a.hi + b;
+    double bb = s - a.hi;
+    double err = (a.hi - (s - bb)) + (b - bb);
+    double lo = a.lo + err;
+    double hi = s + lo;
+    lo = lo - (hi - s);
+    return {hi, lo};
+}
+
+__device__ __forceinline__ DD dd_add(DD a, DD b) {
+    DD r = dd_add(a, b.hi);
+    return dd_add(r, b.lo);
+}
+
+constexpr int SCORE_BLOCKS = 256;
+constexpr int SCORE_THREADS = 256;
+
+__global__ void __launch_bounds__(SCORE_THREADS) k_score_terms(int32_t kind, double lambda, int32_t m,
+                                                              const int32_t *__restrict__ sizes,
+                                                              const int32_t *__restrict__ intv,
+                                                              const int32_t *__restrict__ vol,
+                                                              const DevCounters *ctr, DD *partial) {
+    const int32_t k = ctr->k;
+    DD acc{0.0, 0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < k; i += (int64_t)gridDim.x * blockDim.x) {
+        double t;
+        if (kind == 0) {
+            double actual = intv[i] / (2.0 * m);
+            double x = vol[i] / (2.0 * m);
+            double expect = x * x;  // pow(x, 2)
+            t = actual - expect;
+        } else {
+            t = intv[i] - lambda * sizes[i] * (sizes[i] - 1);
+        }
+        acc = dd_add(acc, t);
+    }
+    __shared__ DD sh[SCORE_THREADS];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = SCORE_THREADS / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) sh[threadIdx.x] = dd_add(sh[threadIdx.x], sh[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+__global__ void k_score_final(int32_t kind, int32_t m, const DD *partial, int nparts, double *out) {
+    if (threadIdx.x != 0) return;
+    DD acc{0.0, 0.0};
+    for (int i = 0; i < nparts; ++i) acc = dd_add(acc, partial[i]);
+    double s = acc.hi + acc.lo;
+    if (kind == 1) s = s / (double)(2 * m);
+    *out = s;
+}
+
+int launch_score(pcd_graph *g, int32_t kind, double lambda, double *d_out, cudaStream_t st) {
+    DD *partial = reinterpret_cast<DD *>(g->small);
+    k_score_terms<<<SCORE_BLOCKS, SCORE_THREADS, 0, st>>>(kind, lambda, g->m, g->sizes, g->intv, g->vol, g->ctr,
+                                                           partial);
+    k_score_final<<<1, 32, 0, st>>>(kind, g->m, partial, SCORE_BLOCKS, d_out);
+    return 2;
+}
+
+// ---------------------------------------------------------------------------
+// CSR validation: offsets monotone and spanning [0, 2m], neighbours in range,
+// rows strictly increasing (sorted, no duplicates), no loops.
+// ---------------------------------------------------------------------------
+__global__ void k_validate(const int32_t *__restrict__ indices, const int32_t *__restrict__ adj, int32_t n,
+                           int32_t m, int32_t *flag) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    if (warp == 0 && lane == 0) {
+        if (indices[0] != 0 || (int64_t)indices[n] != 2 * (int64_t)m) atomicOr(flag, 1);
+    }
+    for (int64_t v = warp; v < n; v += nwarps) {
+        int32_t b = indices[v], e = indices[v + 1];
+        if (b > e || b < 0 || (int64_t)e > 2 * (int64_t)m) {
+            if (lane == 0) atomicOr(flag, 2);
+            continue;
+        }
+        bool bad = false;
+        for (int32_t j = b + lane; j < e; j += 32) {
+            int32_t u = adj[j];
+            bad |= (u < 0 || u >= n || u == (int32_t)v);
+            if (j > b) bad |= (adj[j - 1] >= u);
+        }
+        if (__any_sync(FULL, bad) && lane == 0) atomicOr(flag, 4);
+    }
+}
+
+int launch_validate(const int32_t *indices, const int32_t *adj, int32_t n, int32_t m, int32_t *d_flag,
+                    cudaStream_t st) {
+    k_validate<<<grid_for((int64_t)n * 32, 256), 256, 0, st>>>(indices, adj, n, m, d_flag);
+    return 1;
+}
+
+// ---------------------------------------------------------------------------
+// degree bins: stable compaction of the vertices of each class
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int32_t bin_of(int32_t d, const BinConfig &b) {
+    if (d <= b.thread_max) return BIN_THREAD;
+    if (d <= b.warp_max) return BIN_WARP;
+    if (d <= b.block_max) return BIN_BLOCK;
+    if (d <= b.block_l_max) return BIN_BLOCK_L;
+    return BIN_HUB;
+}
+
+struct BinFlag {
+    const int32_t *indices;
+    BinConfig cfg;
+    int32_t bin;
+    __device__ uint32_t operator()(int64_t v) const {
+        return bin_of(indices[v + 1] - indices[v], cfg) == bin ? 1u : 0u;
+    }
+};
+
+struct BinStore {
+    const int32_t *indices;
+    BinConfig cfg;
+    int32_t bin;
+    int32_t *out;
+    __device__ void operator()(int64_t v, uint32_t x, uint32_t) const {
+        if (bin_of(indices[v + 1] - indices[v], cfg) == bin) out[x] = (int32_t)v;
+    }
+};
+
+int launch_bins(pcd_graph *g, cudaStream_t st) {
+    int launches = 0;
+    g->bin_off[0] = 0;
+    for (int b = 0; b < NBINS; ++b) {
+        launches += scan_exclusive(BinFlag{g->indices, g->bins, b},
+                                   BinStore{g->indices, g->bins, b, g->bin_list + g->bin_off[b]}, g->n,
+                                   g->scan, st);
+        uint32_t cnt = 0;
+        cudaMemcpyAsync(&cnt, g->scan_total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+        g->bin_off[b + 1] = g->bin_off[b] + cnt;
+    }
+    return launches;
+}
+
+}  // namespace pcd

@@ -1,0 +1,117 @@
+// Host-side state of libpcd and the launchers each translation unit exports.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/pcd.h"
+#include "pcd_types.h"
+
+struct pcd_ctx {
+    int32_t device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;  // own_stream or the caller's
+    int32_t num_sms = 0;
+    size_t smem_optin = 0;
+    std::string last_error;
+    std::vector<pcd_graph *> graphs;
+    // profiling: (phase name, event recorded at the END of that phase)
+    bool prof_on = false;
+    std::vector<cudaEvent_t> prof_pool;
+    std::vector<const char *> prof_names;
+    size_t prof_used = 0;
+};
+
+struct pcd_graph {
+    pcd_ctx *ctx = nullptr;
+    int32_t n = 0, m = 0;
+    int64_t nnz = 0;  // 2m
+    int32_t max_deg = 0;
+
+    // CSR (device)
+    int32_t *indices = nullptr, *adj = nullptr;
+    // partition state (device, capacity n)
+    int32_t *labels = nullptr;      // current labels
+    int32_t *labels_alt = nullptr;  // sweep output / compress scratch
+    int32_t *first = nullptr;       // compress: first vertex of each old label
+    int32_t *sizes = nullptr, *intv = nullptr, *extv = nullptr, *vol = nullptr;
+    // sweep scratch
+    uint32_t *ndraw = nullptr;        // per vertex: rand_r calls; then draw offsets
+    uint32_t *tile_sums = nullptr;    // scan scratch
+    uint32_t *scan_total = nullptr;   // scan result (1 word)
+    pcd::ScanScratch scan{};          // tile_sums + scan_total + overflow flag
+    int32_t scan_overflow = 0;        // host: a scan did not fit its scratch
+    int32_t *tiebuf = nullptr;
+    int64_t tiebuf_cap = 0;
+    pcd::TieRecord *recs = nullptr;   // capacity max(n, k)
+    int32_t *amb = nullptr;           // ambiguous vertex list, capacity n
+    pcd::DevCounters *ctr = nullptr;  // device counters
+    void *small = nullptr;            // 64 KiB of reduction scratch
+    double *d_score = nullptr;        // device result of pcd_score
+    pcd::DevCounters *h_ctr = nullptr;  // pinned mirror
+    // hub scratch: per resident hub block, a table of hub_slots entries
+    int32_t *hub_scratch = nullptr;
+    int64_t hub_slots = 0;   // power of two >= 2 * max_deg (hub bin)
+    int32_t hub_blocks = 0;  // blocks sharing the scratch
+    // degree bins
+    int32_t *bin_list = nullptr;          // vertices grouped by bin
+    int64_t bin_off[pcd::NBINS + 1] = {0};
+    pcd::BinConfig bins{};
+    // triangles (WCC)
+    int32_t *tri = nullptr, *tri_deg = nullptr;
+    double cc = 0.0;
+    bool have_tri = false;
+    // merge scratch (grown on demand)
+    void *merge_buf = nullptr;
+    size_t merge_bytes = 0;
+    // bookkeeping
+    int32_t k = 0;           // communities (valid when compressed)
+    bool compressed = false; // labels renumbered and statistics current
+    pcd_sweep_info info{};
+    std::vector<void *> allocs;
+};
+
+namespace pcd {
+
+// api.cu
+pcd_status set_error(pcd_ctx *ctx, pcd_status s, const std::string &msg);
+pcd_status check_cuda(pcd_ctx *ctx, cudaError_t e, const char *what);
+pcd_status dev_alloc(pcd_graph *g, void **p, size_t bytes);
+
+// partition.cu
+int launch_compress(pcd_graph *g, cudaStream_t st);   // relabel + stats; k to ctr->k
+int launch_stats(pcd_graph *g, cudaStream_t st);
+int launch_score(pcd_graph *g, int32_t kind, double lambda, double *d_out, cudaStream_t st);
+int launch_validate(const int32_t *indices, const int32_t *adj, int32_t n, int32_t m,
+                    int32_t *d_flag, cudaStream_t st);
+int launch_bins(pcd_graph *g, cudaStream_t st);  // fills bin_list / bin_off (syncs)
+
+// propagate.cu
+int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32_t seed,
+                  cudaStream_t st);
+void launch_resolve(const TieRecord *recs, const DevCounters *ctr, const uint32_t *endpos, const uint32_t *base,
+                    const int32_t *tiebuf, int32_t *out, uint32_t seed, int32_t mod_base, int grid,
+                    cudaStream_t st);
+
+// merge.cu
+pcd_status run_merge(pcd_graph *g, int32_t kind, double lambda, int32_t rounds, uint32_t seed,
+                     cudaStream_t st, int *launches);
+pcd_status run_contract(pcd_graph *g, int64_t cap, int32_t *a, int32_t *b, int32_t *w,
+                        int64_t *num_pairs, cudaStream_t st);
+
+// triangles.cu
+int launch_triangles(pcd_graph *g, cudaStream_t st);
+int launch_wcc_score(pcd_graph *g, double *d_out, cudaStream_t st);
+
+// jump table upload (propagate.cu)
+void upload_jump_table(cudaStream_t st);
+
+// profiling marks (api.cu): prof_begin clears the span list and records the
+// start; prof_mark closes the phase `name`.  No-ops unless enabled.
+void prof_begin(pcd_ctx *ctx, cudaStream_t st);
+void prof_mark(pcd_ctx *ctx, const char *name, cudaStream_t st);
+
+}  // namespace pcd

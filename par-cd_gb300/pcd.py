@@ -1,0 +1,388 @@
+"""Python host side of libpcd: the reference's phase and rule interfaces
+(src/framework.hpp:8-11, src/rules.hpp:9-19, src/refinement.hpp:8-42, the GPU
+host API src/framework-cuda.cuh:14-23) over the C ABI in include/pcd.h.
+
+Every call goes through libpcd.so; there is no CPU path.  If the library
+cannot be loaded the import of this module raises.
+
+    ctx = Context(0)
+    g = Graph.from_csr(ctx, indices, adj)
+    rand = GlibcRand()                          # the reference's rand() stream
+    g.labels = create_singleton_partition(g, rand)
+    k = g.compress()                            # compress_labels + collect_statistics
+    score = ModularityRule().calculate(g)
+    PropagationRefinement(1.0).refine(g, ModularityRule(), rand())
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpcd.so")
+
+NEW_LABEL = -1
+
+
+class PcdError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{message} (status {status})")
+        self.status = status
+
+
+class _Rule(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("lam", C.c_double)]
+
+
+class _Info(C.Structure):
+    _fields_ = [("draws", C.c_int64), ("fallback", C.c_int32), ("resolved", C.c_int32),
+                ("kernels", C.c_int32), ("merge_pairs", C.c_int32)]
+
+
+class _Rand(C.Structure):
+    _fields_ = [("r", C.c_uint32 * 34), ("pos", C.c_int32)]
+
+
+def _load() -> C.CDLL:
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"libpcd.so is not built ({LIB_PATH}); run par-cd_gb300/build.py")
+    lib = C.CDLL(LIB_PATH)
+    vp, i32, i64, u32, dbl = C.c_void_p, C.c_int32, C.c_int64, C.c_uint32, C.c_double
+    sig = {
+        "pcd_status_string": ([i32], C.c_char_p),
+        "pcd_last_error": ([vp], C.c_char_p),
+        "pcd_init": ([C.POINTER(vp), i32], i32),
+        "pcd_destroy": ([vp], i32),
+        "pcd_set_stream": ([vp, vp], i32),
+        "pcd_synchronize": ([vp], i32),
+        "pcd_load_csr": ([vp, i32, i32, vp, vp, C.POINTER(vp)], i32),
+        "pcd_load_csr_device": ([vp, i32, i32, vp, vp, C.POINTER(vp)], i32),
+        "pcd_graph_free": ([vp], i32),
+        "pcd_labels_set": ([vp, vp], i32),
+        "pcd_labels_get": ([vp, vp], i32),
+        "pcd_labels_set_device": ([vp, vp], i32),
+        "pcd_labels_get_device": ([vp, vp], i32),
+        "pcd_compress": ([vp, C.POINTER(i32)], i32),
+        "pcd_stats_get": ([vp, vp, vp, vp], i32),
+        "pcd_triangles": ([vp, vp, vp, C.POINTER(dbl)], i32),
+        "pcd_score": ([vp, C.POINTER(_Rule), C.POINTER(dbl)], i32),
+        "pcd_refine": ([vp, C.POINTER(_Rule), dbl, u32], i32),
+        "pcd_merge": ([vp, C.POINTER(_Rule), i32, u32], i32),
+        "pcd_contract": ([vp, i64, vp, vp, vp, C.POINTER(i64)], i32),
+        "pcd_sweep_info_get": ([vp, C.POINTER(_Info)], i32),
+        "pcd_rand_seed": ([C.POINTER(_Rand), u32], None),
+        "pcd_rand_next": ([C.POINTER(_Rand)], i32),
+        "pcd_rand_skip": ([C.POINTER(_Rand), i64], None),
+        "pcd_singleton_partition": ([C.POINTER(_Rand), i32, vp], i32),
+        "pcd_clustering_partition": ([i32, vp, vp, vp, vp], i32),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    return lib
+
+
+LIB = _load()
+
+
+def _ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data) if a is not None and a.size else C.c_void_p(0)
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+# ---------------------------------------------------------------------------
+# rules (src/rules.hpp)
+# ---------------------------------------------------------------------------
+@dataclass(frozen=True)
+class Rule:
+    kind: int
+    lam: float = 0.0
+
+    def _c(self) -> _Rule:
+        return _Rule(self.kind, self.lam)
+
+    def calculate(self, g: "Graph") -> float:
+        """Rule::calculate on the graph's current partition (FP64)."""
+        out = C.c_double()
+        g.ctx._check(LIB.pcd_score(g.h, C.byref(self._c()), C.byref(out)))
+        return out.value
+
+    def get_name(self) -> str:
+        return {0: "modularity", 1: f"CPM (lambda={self.lam:g})", 2: "WCC"}[self.kind]
+
+
+def ModularityRule() -> Rule:
+    return Rule(0)
+
+
+def CPMRule(lam: float) -> Rule:
+    return Rule(1, float(lam))
+
+
+def WCCRule() -> Rule:
+    return Rule(2)
+
+
+def parse_metric(spec: str) -> Rule:
+    """-m mod | wcc | cpm-<gamma> (src/main.cpp:125-141)."""
+    s = spec.lower()
+    if s in ("mod", "modularity"):
+        return ModularityRule()
+    if s == "wcc":
+        return WCCRule()
+    if s.startswith("cpm-") and len(s) > 4:
+        return CPMRule(float(s[4:]))
+    raise ValueError(f"unknown metric: {spec}")
+
+
+# ---------------------------------------------------------------------------
+# context / graph
+# ---------------------------------------------------------------------------
+class Context:
+    """cuda_init / cuda_deinit (src/framework-cuda.cu:59-78)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        st = LIB.pcd_init(C.byref(h), device)
+        self.h = h
+        if st != 0:
+            msg = LIB.pcd_last_error(h).decode() if h else ""
+            if h:
+                LIB.pcd_destroy(h)
+            self.h = None
+            raise PcdError(st, f"pcd_init({device}) failed: {msg}")
+        self.device = device
+
+    def _check(self, st: int):
+        if st != 0:
+            msg = LIB.pcd_last_error(self.h).decode() if self.h else ""
+            raise PcdError(st, f"{LIB.pcd_status_string(st).decode()}: {msg}")
+
+    def set_stream(self, stream_ptr: int | None):
+        self._check(LIB.pcd_set_stream(self.h, C.c_void_p(stream_ptr or 0)))
+
+    def synchronize(self):
+        self._check(LIB.pcd_synchronize(self.h))
+
+    def close(self):
+        if self.h:
+            LIB.pcd_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+@dataclass
+class SweepInfo:
+    draws: int
+    fallback: int
+    resolved: int
+    kernels: int
+    merge_pairs: int
+
+
+class Graph:
+    """A graph resident on the device with its current partition
+    (Graph src/graph.hpp:6-40 + Partition src/common.hpp:26-37)."""
+
+    def __init__(self, ctx: Context, h, n: int, m: int, indices=None, adj=None):
+        self.ctx, self.h, self.n, self.m = ctx, h, n, m
+        self._indices, self._adj = indices, adj
+
+    @classmethod
+    def from_csr(cls, ctx: Context, indices, adj) -> "Graph":
+        """cuda_transfer_graph from host CSR arrays."""
+        ind = _i32(indices)
+        a = _i32(adj)
+        n = ind.shape[0] - 1
+        m = a.shape[0] // 2
+        h = C.c_void_p()
+        ctx._check(LIB.pcd_load_csr(ctx.h, n, m, _ptr(ind), _ptr(a), C.byref(h)))
+        return cls(ctx, h, n, m, ind, a)
+
+    @classmethod
+    def from_device(cls, ctx: Context, n: int, m: int, d_indices: int, d_adj: int) -> "Graph":
+        h = C.c_void_p()
+        ctx._check(LIB.pcd_load_csr_device(ctx.h, n, m, C.c_void_p(d_indices), C.c_void_p(d_adj), C.byref(h)))
+        return cls(ctx, h, n, m)
+
+    def free(self):
+        if self.h:
+            LIB.pcd_graph_free(self.h)
+            self.h = None
+
+    # labels -------------------------------------------------------------
+    @property
+    def labels(self) -> np.ndarray:
+        out = np.empty(self.n, np.int32)
+        self.ctx._check(LIB.pcd_labels_get(self.h, _ptr(out)))
+        return out
+
+    @labels.setter
+    def labels(self, lab):
+        lab = _i32(lab)
+        if lab.shape[0] != self.n:
+            raise ValueError("labels must have n entries")
+        self.ctx._check(LIB.pcd_labels_set(self.h, _ptr(lab)))
+
+    def set_labels_device(self, ptr: int):
+        self.ctx._check(LIB.pcd_labels_set_device(self.h, C.c_void_p(ptr)))
+
+    def get_labels_device(self, ptr: int):
+        self.ctx._check(LIB.pcd_labels_get_device(self.h, C.c_void_p(ptr)))
+
+    # phases -------------------------------------------------------------
+    def compress(self, sync: bool = True) -> int | None:
+        """compress_labels + collect_statistics; returns the community count."""
+        if not sync:
+            self.ctx._check(LIB.pcd_compress(self.h, None))
+            return None
+        k = C.c_int32()
+        self.ctx._check(LIB.pcd_compress(self.h, C.byref(k)))
+        return k.value
+
+    def stats(self):
+        k = self.compress()
+        s = np.zeros(max(k, 1), np.int32)
+        i = np.zeros(max(k, 1), np.int32)
+        e = np.zeros(max(k, 1), np.int32)
+        self.ctx._check(LIB.pcd_stats_get(self.h, _ptr(s), _ptr(i), _ptr(e)))
+        return s[:k], i[:k], e[:k]
+
+    def count_triangles(self):
+        tri = np.zeros(self.n, np.int32)
+        td = np.zeros(self.n, np.int32)
+        cc = C.c_double()
+        self.ctx._check(LIB.pcd_triangles(self.h, _ptr(tri), _ptr(td), C.byref(cc)))
+        return tri, td, cc.value
+
+    def contract(self):
+        """Contracted edge weights (a, b, w), sorted by (a, b)."""
+        npairs = C.c_int64()
+        self.ctx._check(LIB.pcd_contract(self.h, 0, None, None, None, C.byref(npairs)))
+        P = npairs.value
+        a = np.zeros(max(P, 1), np.int32)
+        b = np.zeros(max(P, 1), np.int32)
+        w = np.zeros(max(P, 1), np.int32)
+        self.ctx._check(LIB.pcd_contract(self.h, P, _ptr(a), _ptr(b), _ptr(w), C.byref(npairs)))
+        return a[:P], b[:P], w[:P]
+
+    def info(self) -> SweepInfo:
+        i = _Info()
+        self.ctx._check(LIB.pcd_sweep_info_get(self.h, C.byref(i)))
+        return SweepInfo(i.draws, i.fallback, i.resolved, i.kernels, i.merge_pairs)
+
+
+# ---------------------------------------------------------------------------
+# refinements (src/refinement.hpp)
+# ---------------------------------------------------------------------------
+class PropagationRefinement:
+    def __init__(self, frac: float):
+        self.frac = float(frac)
+
+    def refine(self, g: Graph, rule: Rule, seed: int):
+        g.ctx._check(LIB.pcd_refine(g.h, C.byref(rule._c()), self.frac, C.c_uint32(seed & 0xFFFFFFFF)))
+
+
+class MergingRefinement:
+    def __init__(self, rounds: int = 1):
+        self.rounds = int(rounds)
+
+    def refine(self, g: Graph, rule: Rule, seed: int):
+        g.ctx._check(LIB.pcd_merge(g.h, C.byref(rule._c()), self.rounds, C.c_uint32(seed & 0xFFFFFFFF)))
+
+
+class GlibcRand:
+    """The reference's rand() stream (glibc, default seed 1)."""
+
+    def __init__(self, seed: int = 1):
+        self._s = _Rand()
+        LIB.pcd_rand_seed(C.byref(self._s), seed)
+
+    def __call__(self) -> int:
+        return int(LIB.pcd_rand_next(C.byref(self._s)))
+
+    def skip(self, count: int):
+        LIB.pcd_rand_skip(C.byref(self._s), count)
+
+
+def create_singleton_partition(g: Graph, rand: GlibcRand) -> np.ndarray:
+    lab = np.zeros(g.n, np.int32)
+    g.ctx._check(LIB.pcd_singleton_partition(C.byref(rand._s), g.n, _ptr(lab)))
+    return lab
+
+
+def create_clustering_partition(g: Graph) -> np.ndarray:
+    tri, _, _ = g.count_triangles()
+    if g._indices is None:
+        raise ValueError("clustering partition needs the host CSR")
+    lab = np.zeros(g.n, np.int32)
+    g.ctx._check(LIB.pcd_clustering_partition(g.n, _ptr(g._indices), _ptr(g._adj), _ptr(tri), _ptr(lab)))
+    return lab
+
+
+@dataclass
+class Iteration:
+    it: int
+    kind: str
+    score: float
+    k: int
+    raw: np.ndarray | None = None
+
+
+@dataclass
+class RunResult:
+    labels: np.ndarray
+    score: float
+    iterations: int
+    k: int
+    log: list = field(default_factory=list)
+
+
+def run(g: Graph, rule: Rule, strategy: int = 0, frac: float = 0.5, rounds: int = 1, n_iter: int = -1,
+        threshold: float = 0.0, initial: int = 0, keep_raw: bool = False, callback=None) -> RunResult:
+    """The reference driver loop (src/main.cpp:187-266) on the device."""
+    rand = GlibcRand(1)
+    if initial == 1 or rule.kind == 2:
+        g.count_triangles()
+    if initial == 0:
+        g.labels = create_singleton_partition(g, rand)
+    elif initial == 1:
+        g.labels = create_clustering_partition(g)
+    else:
+        raise ValueError("unknown partitioning strategy")
+    pr = PropagationRefinement(frac)
+    mr = MergingRefinement(rounds)
+    prev = 0.0
+    it = 0
+    log = []
+    while True:
+        k = g.compress()
+        score = rule.calculate(g)
+        done = (it >= n_iter) if n_iter != -1 else (prev > 0 and score > 0 and score / prev - 1 <= threshold)
+        if done:
+            break
+        if strategy == 0 or (strategy == 2 and it % 2 == 0):
+            kind = "prop"
+            pr.refine(g, rule, rand())
+        else:
+            kind = "merge"
+            mr.refine(g, rule, rand())
+        rec = Iteration(it, kind, score, k, g.labels if keep_raw else None)
+        log.append(rec)
+        if callback:
+            callback(rec)
+        it += 1
+        prev = score
+    return RunResult(g.labels, score, it, k, log)

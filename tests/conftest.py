@@ -1,0 +1,66 @@
+"""Shared test setup: import paths, the `gpu` marker, seeded graphs and the
+checkers (oracle/ is test infrastructure; only tests, smoke() and bench.py's
+CPU-baseline leg use it)."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+for p in (os.path.join(ROOT, "par-cd_gb300"), os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA device (run with -m gpu)")
+
+
+def gpu_available() -> bool:
+    try:
+        import torch
+
+        return torch.cuda.is_available()
+    except Exception:  # pragma: no cover
+        return False
+
+
+@pytest.fixture(scope="session")
+def port():
+    import oracle
+
+    return oracle.Port()
+
+
+@pytest.fixture(scope="session")
+def golden():
+    import json
+
+    with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
+        return json.load(f)
+
+
+_GRAPHS = {}
+
+
+def golden_graph(name):
+    """Regenerate a golden graph from its seed (cached)."""
+    if name not in _GRAPHS:
+        sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+        import graphs
+        import make_golden
+
+        _GRAPHS[name] = make_golden.make_graph(name)[1]
+    return _GRAPHS[name]
+
+
+@pytest.fixture(scope="session")
+def ctx():
+    if not gpu_available():
+        pytest.skip("no CUDA device")
+    import pcd
+
+    c = pcd.Context(0)
+    yield c
+    c.close()

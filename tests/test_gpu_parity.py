@@ -1,0 +1,211 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle and with the
+reference's own golden hashes: labels bit-exact after every sweep, integer
+statistics and contracted weights exact, FP64 scores within 1e-12 relative."""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import golden_graph
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-12
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<i4").tobytes()).hexdigest()
+
+
+def close(a, b, rel=REL):
+    return a == b or abs(a - b) <= rel * max(abs(a), abs(b))
+
+
+def gpu_schedule(ctx, indices, adj, metric, strategy, frac, rounds, n_iter, initial):
+    import pcd
+
+    g = pcd.Graph.from_csr(ctx, indices, adj)
+    recs = []
+    res = pcd.run(g, pcd.parse_metric(metric), strategy, frac, rounds, n_iter, 0.0, initial, keep_raw=True,
+                  callback=recs.append)
+    out = (recs, res, g.info())
+    g.free()
+    return out
+
+
+def oracle_schedule(port, indices, adj, metric, strategy, frac, rounds, n_iter, initial):
+    import oracle
+
+    return oracle.run_schedule(port, indices, adj, metric, strategy, frac, rounds, n_iter, 0.0, initial)
+
+
+CASES = [
+    ("sbm10k", "mod", 0, 1.0, 1, 12, 0),
+    ("sbm10k", "mod", 0, 0.5, 1, 8, 0),
+    ("sbm10k", "mod", 1, 1.0, 1, 8, 0),
+    ("sbm10k", "mod", 2, 1.0, 1, 24, 0),
+    ("sbm10k", "cpm-0.01", 0, 1.0, 1, 10, 0),
+    ("sbm10k", "cpm-0.01", 2, 1.0, 1, 16, 0),
+    ("sbm10k", "mod", 2, 1.0, 3, 12, 0),
+    ("rmat12", "mod", 0, 1.0, 1, 10, 0),
+    ("rmat12", "mod", 2, 1.0, 3, 10, 0),
+    ("rmat12", "cpm-0.01", 2, 1.0, 2, 8, 1),
+    ("rmat12", "wcc", 2, 1.0, 1, 6, 1),
+    ("pl20k", "wcc", 0, 1.0, 1, 6, 1),
+    ("pl20k", "cpm-0.01", 2, 1.0, 2, 8, 1),
+    ("pl20k", "mod", 0, 0.7, 1, 6, 0),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: "-".join(map(str, c)))
+def test_schedule_matches_reference_golden(ctx, golden, case):
+    gname, metric, strat, frac, rounds, n_iter, init = case
+    g = golden_graph(gname)
+    ref = next(c for c in golden["cases"]
+               if (c["graph"], c["metric"], c["strategy"], c["frac"], c["rounds"], c["n_iter"], c["initial"]) == case)
+    recs, res, _ = gpu_schedule(ctx, g.indices, g.adj, metric, strat, frac, rounds, n_iter, init)
+    assert len(recs) == len(ref["sweeps"])
+    for mine, theirs in zip(recs, ref["sweeps"]):
+        assert mine.kind == theirs["kind"]
+        assert mine.k == theirs["k"], f"sweep {mine.it}: communities"
+        assert close(mine.score, float(theirs["score"])), f"sweep {mine.it}: score {mine.score} vs {theirs['score']}"
+        assert sha(mine.raw) == theirs["raw_sha256"], f"sweep {mine.it} ({mine.kind}): labels differ"
+    assert sha(res.labels) == ref["final_sha256"]
+    assert close(res.score, float(ref["final_score"]))
+
+
+@pytest.mark.parametrize("case", CASES[:4] + CASES[7:9] + CASES[11:], ids=lambda c: "-".join(map(str, c)))
+def test_schedule_matches_oracle_arrays(ctx, port, case):
+    """Same schedule against the oracle port, comparing whole arrays (a failure
+    shows which vertices differ)."""
+    gname, metric, strat, frac, rounds, n_iter, init = case
+    g = golden_graph(gname)
+    recs, res, _ = gpu_schedule(ctx, g.indices, g.adj, metric, strat, frac, rounds, n_iter, init)
+    _, _, sweeps = oracle_schedule(port, g.indices, g.adj, metric, strat, frac, rounds, n_iter, init)
+    for mine, theirs in zip(recs, sweeps):
+        bad = np.nonzero(mine.raw != theirs.raw)[0]
+        assert bad.size == 0, f"sweep {mine.it} {mine.kind}: {bad.size} vertices differ, first {bad[:8]}"
+
+
+def test_stats_and_triangles_exact(ctx, port, golden):
+    import pcd
+
+    for name in ("sbm10k", "rmat12", "pl20k"):
+        g = golden_graph(name)
+        G = pcd.Graph.from_csr(ctx, g.indices, g.adj)
+        tri, td, cc = G.count_triangles()
+        assert sha(tri) == golden["graphs"][name]["tri_sha256"]
+        assert sha(td) == golden["graphs"][name]["tri_deg_sha256"]
+        assert cc == float(golden["graphs"][name]["cc"])  # bit-exact: summed in vertex order
+        rng = np.random.default_rng(5)
+        lab = rng.integers(0, max(1, g.n // 20), size=g.n).astype(np.int32)
+        lab[rng.random(g.n) < 0.05] = -1
+        G.labels = lab
+        k = G.compress()
+        comp, k2 = port.load(g.indices, g.adj).compress(lab)
+        assert k == k2
+        assert np.array_equal(G.labels, comp)
+        s, i, e = G.stats()
+        st = port.stats(comp)
+        assert np.array_equal(s, st.sizes) and np.array_equal(i, st.int_volume) and np.array_equal(e, st.ext_volume)
+        G.free()
+
+
+def test_contracted_weights_exact(ctx, port, golden):
+    import oracle
+    import pcd
+
+    g = golden_graph("sbm10k")
+    part = {}
+    oracle.run_schedule(port, g.indices, g.adj, "mod", 0, 1.0, 1, 3, callback=lambda sw, lab: part.update(l=lab.copy()))
+    lab = part["l"]
+    assert sha(lab) == golden["contract"]["sbm10k_prop3"]["labels_sha256"]
+    G = pcd.Graph.from_csr(ctx, g.indices, g.adj)
+    G.labels = lab
+    a, b, w = G.contract()
+    pa, pb, pw = port.contract(lab)
+    assert np.array_equal(a, pa) and np.array_equal(b, pb) and np.array_equal(w, pw)
+    key = a.astype(np.int64) * (1 << 32) + b
+    assert a.shape[0] == golden["contract"]["sbm10k_prop3"]["pairs"]
+    assert hashlib.sha256(key.astype("<i8").tobytes()).hexdigest() == golden["contract"]["sbm10k_prop3"]["key_sha256"]
+    assert sha(w) == golden["contract"]["sbm10k_prop3"]["w_sha256"]
+    G.free()
+
+
+def test_hand_graphs(ctx, golden):
+    import pcd
+
+    for name, rec in golden["hand"].items():
+        ind = np.array(rec["indices"], np.int32)
+        adj = np.array(rec["adj"], np.int32)
+        for key, case in rec["cases"].items():
+            metric, s, i = key.split("/")
+            recs, res, _ = gpu_schedule(ctx, ind, adj, metric, int(s[1:]), 1.0, 1, 6, int(i[1:]))
+            for mine, theirs in zip(recs, case["sweeps"]):
+                assert mine.raw.tolist() == theirs["raw"], f"{name} {key} sweep {mine.it}"
+            assert res.labels.tolist() == case["final"], f"{name} {key}"
+            assert close(res.score, float(case["score"])), f"{name} {key}"
+
+
+def test_single_sweeps_many_seeds(ctx, port):
+    """One propagation and one merge sweep from a mid-run partition, many seeds."""
+    import pcd
+
+    g = golden_graph("rmat12")
+    G = pcd.Graph.from_csr(ctx, g.indices, g.adj)
+    port.load(g.indices, g.adj)
+    rng = np.random.default_rng(11)
+    for trial in range(6):
+        lab = rng.integers(0, 60 + 40 * trial, size=g.n).astype(np.int32)
+        comp, _ = port.compress(lab)
+        st = port.stats(comp)
+        for rule_s in ("mod", "cpm-0.05"):
+            rule = pcd.parse_metric(rule_s)
+            import oracle
+
+            rk, lam = oracle.parse_rule(rule_s)
+            seed = int(rng.integers(0, 2**31))
+            G.labels = comp
+            pcd.PropagationRefinement(1.0).refine(G, rule, seed)
+            mine = G.labels
+            theirs = port.refine_prop(rk, lam, comp, 1.0, seed=seed, st=st)
+            assert np.array_equal(mine, theirs), (trial, rule_s, "prop")
+            G.labels = comp
+            pcd.MergingRefinement(1 + trial % 3).refine(G, rule, seed)
+            mine = G.labels
+            theirs = port.refine_merge(rk, lam, comp, 1 + trial % 3, seed=seed, st=st)
+            assert np.array_equal(mine, theirs), (trial, rule_s, "merge")
+    G.free()
+
+
+def test_edge_cases(ctx, port):
+    import pcd
+
+    # empty graph
+    G = pcd.Graph.from_csr(ctx, np.zeros(1, np.int32), np.zeros(0, np.int32))
+    assert G.compress() == 0
+    pcd.PropagationRefinement(1.0).refine(G, pcd.ModularityRule(), 1)
+    G.free()
+    # isolated vertices inside the vertex range, a star, a single edge
+    ind = np.array([0, 3, 3, 4, 5, 6, 6], np.int32)
+    adj = np.array([2, 3, 4, 0, 0, 0], np.int32)
+    for metric in ("mod", "cpm-0.5"):
+        recs, res, _ = gpu_schedule(ctx, ind, adj, metric, 2, 1.0, 1, 6, 0)
+        _, _, sweeps = oracle_schedule(port, ind, adj, metric, 2, 1.0, 1, 6, 0)
+        for a, b in zip(recs, sweeps):
+            assert np.array_equal(a.raw, b.raw)
+    # invalid CSR is rejected
+    with pytest.raises(pcd.PcdError):
+        pcd.Graph.from_csr(ctx, np.array([0, 1, 2], np.int32), np.array([1, 1], np.int32))  # loop 1-1
+    with pytest.raises(pcd.PcdError):
+        pcd.Graph.from_csr(ctx, np.array([0, 2, 2], np.int32), np.array([1, 1], np.int32))  # duplicate
+    with pytest.raises(pcd.PcdError):
+        pcd.Graph.from_csr(ctx, np.array([0, 1, 2], np.int32), np.array([1, 5], np.int32))  # out of range
+    G = pcd.Graph.from_csr(ctx, np.array([0, 1, 2], np.int32), np.array([1, 0], np.int32))
+    with pytest.raises(pcd.PcdError):
+        G.labels = np.array([0, 7], np.int32)
+    with pytest.raises(pcd.PcdError):
+        pcd.PropagationRefinement(0.0).refine(G, pcd.ModularityRule(), 1)
+    with pytest.raises(pcd.PcdError):
+        pcd.MergingRefinement(0).refine(G, pcd.ModularityRule(), 1)
+    G.free()

@@ -1,0 +1,151 @@
+"""CPU: the oracle (our C restatement) pinned against the reference itself.
+
+* always: the golden hashes written by the reference (tests/golden/), the
+  converter's byte output, and libc's own rand()/rand_r();
+* when the reference objects were built here (oracle/_ref): side-by-side runs
+  of the reference and the restatement on seeded graphs.
+"""
+import ctypes
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import golden_graph
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<i4").tobytes()).hexdigest()
+
+
+def test_generators_and_converter_bytes(golden):
+    import graphs
+
+    for name, rec in golden["graphs"].items():
+        g = golden_graph(name)
+        assert (g.n, g.m) == (rec["n"], rec["m"])
+        assert hashlib.sha256(graphs.to_bytes(g)).hexdigest() == rec["pcd_sha256"]
+        back = graphs.from_bytes(graphs.to_bytes(g))
+        assert np.array_equal(back.adj, g.adj) and np.array_equal(back.indices, g.indices)
+
+
+def test_format_reader_rejects_corrupt_files():
+    import graphs
+
+    g = golden_graph("rmat12")
+    data = graphs.to_bytes(g)
+    for bad in (b"XYZ" + data[3:], data[:-1], data + b"\0", data[:40]):
+        with pytest.raises(graphs.FormatError):
+            graphs.from_bytes(bad)
+    # neighbour id out of range
+    arr = bytearray(data)
+    off = 11 + 4 * (g.n + 1)
+    arr[off:off + 4] = (g.n + 5).to_bytes(4, "little")
+    with pytest.raises(graphs.FormatError):
+        graphs.from_bytes(bytes(arr))
+
+
+def test_glibc_streams_match_libc(port):
+    import oracle
+
+    libc = ctypes.CDLL("libc.so.6")
+    libc.rand.restype = ctypes.c_int
+    libc.rand_r.restype = ctypes.c_int
+    for seed in (1, 7, 2**31 + 5):
+        libc.srand(ctypes.c_uint(seed))
+        a = [libc.rand() for _ in range(5000)]
+        r = oracle.GlibcRand(port.lib, seed)
+        assert a == [r() for _ in range(5000)]
+    s1, s2 = ctypes.c_uint(987654321), ctypes.c_uint32(987654321)
+    for _ in range(20000):
+        assert libc.rand_r(ctypes.byref(s1)) == port.lib.pcdo_rand_r(ctypes.byref(s2))
+
+
+@pytest.mark.parametrize("idx", range(14))
+def test_oracle_matches_reference_golden(port, golden, idx):
+    import oracle
+
+    case = golden["cases"][idx]
+    g = golden_graph(case["graph"])
+    seen = []
+    oracle.run_schedule(port, g.indices, g.adj, case["metric"], case["strategy"], case["frac"], case["rounds"],
+                        case["n_iter"], 0.0, case["initial"], callback=lambda sw, lab: seen.append((sw, lab.copy())))
+    assert len(seen) == len(case["sweeps"])
+    for (sw, lab), ref in zip(seen, case["sweeps"]):
+        assert sha(lab) == ref["in_sha256"]
+        assert sha(sw.raw) == ref["raw_sha256"], f"sweep {sw.it} {sw.kind}"
+        assert sw.k == ref["k"]
+        s, r = sw.score, float(ref["score"])
+        if case["metric"] == "wcc":
+            assert abs(s - r) <= 1e-12 * abs(r)  # the reference sums WCC with an OpenMP reduction
+        else:
+            assert s == r
+
+
+def test_oracle_triangles_golden(port, golden):
+    for name, rec in golden["graphs"].items():
+        g = golden_graph(name)
+        tri, td, cc = port.load(g.indices, g.adj).count_triangles()
+        assert sha(tri) == rec["tri_sha256"] and sha(td) == rec["tri_deg_sha256"]
+        assert cc == float(rec["cc"])
+
+
+def test_oracle_hand_graphs(port, golden):
+    import oracle
+
+    for name, rec in golden["hand"].items():
+        ind = np.array(rec["indices"], np.int32)
+        adj = np.array(rec["adj"], np.int32)
+        for key, case in rec["cases"].items():
+            metric, s, i = key.split("/")
+            final, score, sweeps = oracle.run_schedule(port, ind, adj, metric, int(s[1:]), 1.0, 1, 6, 0.0, int(i[1:]))
+            assert [sw.raw.tolist() for sw in sweeps] == [x["raw"] for x in case["sweeps"]], (name, key)
+            assert final.tolist() == case["final"]
+
+
+needs_ref = pytest.mark.skipif("not __import__('oracle').reference_available()",
+                               reason="reference objects not built here (make -C oracle ref)")
+
+
+@needs_ref
+@pytest.mark.parametrize("metric,strategy,frac,rounds,initial", [
+    ("mod", 0, 1.0, 1, 0), ("mod", 0, 0.3, 1, 0), ("mod", 2, 1.0, 2, 0), ("cpm-0.02", 2, 1.0, 1, 0),
+    ("wcc", 2, 1.0, 1, 1), ("cpm-0.2", 1, 1.0, 4, 1)])
+def test_oracle_matches_reference_side_by_side(port, metric, strategy, frac, rounds, initial):
+    import graphs
+    import oracle
+
+    ref = oracle.Reference("strict")
+    e = graphs.rmat(11, 12, 0.55, 0.2, 0.2, seed=17)
+    g = graphs.convert_edges(e)
+    lr, sr, swr = oracle.run_schedule(ref, g.indices, g.adj, metric, strategy, frac, rounds, 8, 0.0, initial)
+    lp, sp, swp = oracle.run_schedule(port, g.indices, g.adj, metric, strategy, frac, rounds, 8, 0.0, initial)
+    assert len(swr) == len(swp)
+    for a, b in zip(swr, swp):
+        assert np.array_equal(a.raw, b.raw), (a.it, a.kind)
+    assert abs(sr - sp) <= 1e-12 * abs(sr)
+
+
+@needs_ref
+def test_oracle_gains_match_reference_including_int_wrap(port):
+    """Single gains, including WCC communities large enough that the
+    reference's int products wrap (sizes > 46341)."""
+    import graphs
+    import oracle
+
+    ref = oracle.Reference("strict")
+    n = 60000
+    edges = np.array([(0, i) for i in range(1, n)] + [(i, i + 1) for i in range(1, n - 1)])
+    g = graphs.convert_edges(edges)
+    ref.load(g.indices, g.adj)
+    port.load(g.indices, g.adj)
+    ref.count_triangles()
+    port.count_triangles()
+    lab = np.zeros(g.n, np.int32)
+    lab[-5:] = 1
+    for rule, lam in ((0, 0.0), (1, 0.01), (2, 0.0)):
+        for (kind, a, b, k) in (("join", g.n - 1, 0, 2), ("leave", 3, 0, 2), ("leave", g.n - 2, 1, 1),
+                                ("merge", 0, 1, 3), ("merge", 1, 0, 3), ("join", 5, 1, 1)):
+            x = ref.gain(kind, rule, lam, lab, a, b, k)
+            y = port.gain(kind, rule, lam, lab, a, b, k)
+            assert (x == y) or (x != x and y != y), (rule, kind, x, y)
