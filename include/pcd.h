@@ -63,6 +63,7 @@ typedef struct pcd_sweep_info {
     int32_t resolved;      /* vertices / communities whose tie list was replayed */
     int32_t kernels;       /* kernel launches issued by the call */
     int32_t merge_pairs;   /* contracted (a, b) pairs (merge only) */
+    int64_t kernels_total; /* kernel launches issued by every call on this graph so far */
 } pcd_sweep_info;
 
 const char *pcd_status_string(pcd_status s);

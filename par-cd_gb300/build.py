@@ -2,7 +2,7 @@
 
 Every translation unit is compiled in parallel with nvcc for
 `-gencode arch=compute_103a,code=sm_103a` and linked into
-par-cd_gb300/libpcd.so.  `-fmad=false` keeps FP64 products and sums from
+par-cd_gb300/libpcd.so; the drop-in driver par-cd_gb300/main-cuda links it.  `-fmad=false` keeps FP64 products and sums from
 being contracted into FMAs, so device gains are the IEEE results of the
 reference's own operation sequence.
 
@@ -20,6 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpcd.so")
+MAIN = os.path.join(HERE, "main-cuda")
 SOURCES = ["api.cu", "partition.cu", "propagate.cu", "merge.cu", "triangles.cu", "hostside.cpp"]
 HEADERS = ["pcd_device.cuh", "pcd_scan.cuh", "pcd_internal.h", "pcd_types.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -75,6 +76,12 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
     objs = [os.path.join(BUILD, os.path.splitext(s)[0] + ".o") for s in SOURCES]
     if force or jobs or _stale(LIB, objs):
         cmd = [nvcc(), "-shared", "-o", LIB] + objs + ARCH + ["-Xcompiler", "-fPIC"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        subprocess.run(cmd, check=True)
+    main_src = os.path.join(CSRC, "main_cuda.cpp")
+    if force or _stale(MAIN, [main_src, LIB]):
+        cmd = ["g++", "-O2", "-std=c++17", "-o", MAIN, main_src, "-L", HERE, "-lpcd", "-Wl,-rpath,$ORIGIN"]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.run(cmd, check=True)

@@ -384,6 +384,7 @@ pcd_status pcd_compress(pcd_graph *g, int32_t *num_labels) {
     if (!g->compressed) prof_begin(g->ctx, g->ctx->stream);
     TRY(ensure_compressed(g, &launches));
     if (launches) prof_mark(g->ctx, "compress+stats", g->ctx->stream);
+    g->info.kernels_total += launches;
     if (num_labels) {
         TRY(sync_and_check(g));
         g->k = g->n > 0 ? g->h_ctr->k : 0;
@@ -476,6 +477,7 @@ pcd_status pcd_refine(pcd_graph *g, const pcd_rule *rule, double frac, uint32_t 
     }
     g->compressed = false;
     g->info.kernels = launches;
+    g->info.kernels_total += launches;
     TRY(scan_guard(g));
     return check_cuda(g->ctx, cudaGetLastError(), "refine launch");
 }
@@ -494,6 +496,7 @@ pcd_status pcd_merge(pcd_graph *g, const pcd_rule *rule, int32_t rounds, uint32_
     }
     g->compressed = false;
     g->info.kernels = launches;
+    g->info.kernels_total += launches;
     TRY(scan_guard(g));
     return check_cuda(g->ctx, cudaGetLastError(), "merge launch");
 }

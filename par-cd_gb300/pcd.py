@@ -39,7 +39,7 @@ class _Rule(C.Structure):
 
 class _Info(C.Structure):
     _fields_ = [("draws", C.c_int64), ("fallback", C.c_int32), ("resolved", C.c_int32),
-                ("kernels", C.c_int32), ("merge_pairs", C.c_int32)]
+                ("kernels", C.c_int32), ("merge_pairs", C.c_int32), ("kernels_total", C.c_int64)]
 
 
 class _Rand(C.Structure):
@@ -73,6 +73,8 @@ def _load() -> C.CDLL:
         "pcd_merge": ([vp, C.POINTER(_Rule), i32, u32], i32),
         "pcd_contract": ([vp, i64, vp, vp, vp, C.POINTER(i64)], i32),
         "pcd_sweep_info_get": ([vp, C.POINTER(_Info)], i32),
+        "pcd_profile_enable": ([vp, i32], i32),
+        "pcd_profile_read": ([vp, C.POINTER(C.c_char_p), C.POINTER(dbl), i32], i32),
         "pcd_rand_seed": ([C.POINTER(_Rand), u32], None),
         "pcd_rand_next": ([C.POINTER(_Rand)], i32),
         "pcd_rand_skip": ([C.POINTER(_Rand), i64], None),
@@ -171,6 +173,17 @@ class Context:
     def synchronize(self):
         self._check(LIB.pcd_synchronize(self.h))
 
+    def profile(self, on: bool = True):
+        self._check(LIB.pcd_profile_enable(self.h, 1 if on else 0))
+
+    def profile_read(self) -> list:
+        names = (C.c_char_p * 64)()
+        ms = (C.c_double * 64)()
+        k = LIB.pcd_profile_read(self.h, names, ms, 64)
+        if k < 0:
+            raise PcdError(2, "pcd_profile_read failed")
+        return [(names[i].decode(), ms[i]) for i in range(min(k, 64))]
+
     def close(self):
         if self.h:
             LIB.pcd_destroy(self.h)
@@ -190,6 +203,7 @@ class SweepInfo:
     resolved: int
     kernels: int
     merge_pairs: int
+    kernels_total: int
 
 
 class Graph:
@@ -210,6 +224,13 @@ class Graph:
         h = C.c_void_p()
         ctx._check(LIB.pcd_load_csr(ctx.h, n, m, _ptr(ind), _ptr(a), C.byref(h)))
         return cls(ctx, h, n, m, ind, a)
+
+    @classmethod
+    def from_host_ptr(cls, ctx: Context, n: int, m: int, indices_ptr: int, adj_ptr: int) -> "Graph":
+        """Load from raw host pointers (e.g. pinned buffers)."""
+        h = C.c_void_p()
+        ctx._check(LIB.pcd_load_csr(ctx.h, n, m, C.c_void_p(indices_ptr), C.c_void_p(adj_ptr), C.byref(h)))
+        return cls(ctx, h, n, m)
 
     @classmethod
     def from_device(cls, ctx: Context, n: int, m: int, d_indices: int, d_adj: int) -> "Graph":
@@ -235,6 +256,12 @@ class Graph:
         if lab.shape[0] != self.n:
             raise ValueError("labels must have n entries")
         self.ctx._check(LIB.pcd_labels_set(self.h, _ptr(lab)))
+
+    def set_labels_ptr(self, host_ptr: int):
+        self.ctx._check(LIB.pcd_labels_set(self.h, C.c_void_p(host_ptr)))
+
+    def get_labels_ptr(self, host_ptr: int):
+        self.ctx._check(LIB.pcd_labels_get(self.h, C.c_void_p(host_ptr)))
 
     def set_labels_device(self, ptr: int):
         self.ctx._check(LIB.pcd_labels_set_device(self.h, C.c_void_p(ptr)))
@@ -281,7 +308,7 @@ class Graph:
     def info(self) -> SweepInfo:
         i = _Info()
         self.ctx._check(LIB.pcd_sweep_info_get(self.h, C.byref(i)))
-        return SweepInfo(i.draws, i.fallback, i.resolved, i.kernels, i.merge_pairs)
+        return SweepInfo(i.draws, i.fallback, i.resolved, i.kernels, i.merge_pairs, i.kernels_total)
 
 
 # ---------------------------------------------------------------------------
