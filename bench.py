@@ -125,8 +125,9 @@ def bins_bytes(ind):
     import numpy as np
 
     deg = np.diff(ind.astype(np.int64))
-    edges = [0, 16, 128, 1024, 4096, 1 << 62]
-    names = ["sweep.thread", "sweep.warp", "sweep.block", "sweep.block_l", "sweep.hub"]
+    edges = [0, 4, 8, 16, 32, 256, 2048, 8192, 1 << 62]
+    names = ["sweep.g4", "sweep.g8", "sweep.g16", "sweep.g32", "sweep.warp", "sweep.block", "sweep.block_l",
+             "sweep.hub"]
     out = {}
     for nm, lo, hi in zip(names, edges[:-1], edges[1:]):
         sel = (deg > lo) & (deg <= hi) if lo else (deg <= hi)
@@ -134,9 +135,12 @@ def bins_bytes(ind):
     return out
 
 
-def cpu_sweep_baseline(ind, adj, seed, threads, budget_s=30.0, max_sweeps=3):
-    """The oracle's propagation sweep (OpenMP, `threads` threads) from the
-    singleton partition; returns (edges/s, sweeps, seconds)."""
+def cpu_sweeps(ind, adj, seeds, threads, steps, budget_s):
+    """The oracle's OpenMP propagation sweeps (Modularity, frac 1.0) on the
+    host cores: the schedule's first len(seeds) sweeps from the singleton
+    partition (each sweep starts from the compressed result of the previous
+    one), cycled for `steps` sweeps or until `budget_s` seconds are spent.
+    Returns (edges/s, sweeps timed, seconds)."""
     import numpy as np
 
     import oracle
@@ -146,15 +150,33 @@ def cpu_sweep_baseline(ind, adj, seed, threads, budget_s=30.0, max_sweeps=3):
     n = ind.shape[0] - 1
     m = adj.shape[0] // 2
     lab = np.arange(n, dtype=np.int32)
-    st = port.stats(lab)
+    starts = []
     times = []
     t_all = time.time()
-    while len(times) < max_sweeps and time.time() - t_all < budget_s:
+    for i in range(steps):
+        j = i % len(seeds)
+        if j < len(starts):
+            lab = starts[j]
+        else:
+            lab, _ = port.compress(lab)
+            starts.append(lab)
+        st = port.stats(lab)
         t0 = time.perf_counter()
-        port.refine_prop(0, 0.0, lab, 1.0, seed=seed, threads=threads, st=st)
+        out = port.refine_prop(0, 0.0, lab, 1.0, seed=seeds[j], threads=threads, st=st)
         times.append(time.perf_counter() - t0)
-    best = statistics.median(times)
-    return m / best, len(times), sum(times)
+        lab = out
+        if time.time() - t_all > budget_s:
+            break
+    sec = sum(times)
+    return m * len(times) / sec, len(times), sec
+
+
+def schedule_seeds(n, count):
+    import pcd
+
+    r = pcd.GlibcRand()
+    r.skip(n)
+    return [r() for _ in range(count)]
 
 
 def run_reference_arm(args, rank, world):
@@ -166,42 +188,20 @@ def run_reference_arm(args, rank, world):
     ind, adj = make_workload(args, dev)
     n = ind.shape[0] - 1
     m = adj.shape[0] // 2
-    import pcd
-
-    r = pcd.GlibcRand()
-    r.skip(n)
-    seed = r()
+    seeds = schedule_seeds(n, args.sweeps)
     threads = os.cpu_count() or 1
-    steps = max(1, args.steps)
-    budget = 180.0
-    import oracle
-    import numpy as np
-
-    port = oracle.Port()
-    port.load(ind, adj)
-    lab = np.arange(n, dtype=np.int32)
-    st = port.stats(lab)
-    for _ in range(min(args.warmup, 1)):
-        port.refine_prop(0, 0.0, lab, 1.0, seed=seed, threads=threads, st=st)
-    times = []
-    t_all = time.time()
-    for _ in range(steps):
-        t0 = time.perf_counter()
-        port.refine_prop(0, 0.0, lab, 1.0, seed=seed, threads=threads, st=st)
-        times.append(time.perf_counter() - t0)
-        if time.time() - t_all > budget:
-            break
-    sec = sum(times)
-    value = m * len(times) / sec
+    if args.warmup:
+        cpu_sweeps(ind, adj, seeds[:1], threads, 1, 60.0)
+    value, k, sec = cpu_sweeps(ind, adj, seeds, threads, max(1, args.steps), 180.0)
     line = {
         "impl": "reference",
         "metric": METRIC,
         "value": value,
         "unit": "edges/s",
         "n_gpus": world,
-        "steps": len(times),
+        "steps": k,
         "warmup": args.warmup,
-        "ms_per_step": 1000.0 * sec / len(times),
+        "ms_per_step": 1000.0 * sec / k,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
@@ -209,9 +209,9 @@ def run_reference_arm(args, rank, world):
         "data": "synthetic",
         "config": workload_config(args, n, m),
         "cpu_baseline": {"value": value, "unit": "edges/s", "cores": threads, "kind": "port",
-                         "sample": f"{len(times)} full propagation sweeps (Modularity, frac 1.0, singleton start) "
-                                   f"of the workload graph by the oracle's OpenMP restatement of "
-                                   f"PropagationRefinement::refine on {threads} host threads"},
+                         "sample": f"{k} propagation sweeps (the schedule's first {args.sweeps}, cycled) of the "
+                                   f"workload graph by the oracle's OpenMP restatement of "
+                                   f"PropagationRefinement::refine on {threads} host threads, {sec:.1f}s"},
         "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -221,7 +221,7 @@ def run_reference_arm(args, rank, world):
 def workload_config(args, n, m):
     return {
         "workload": f"rmat-s{args.scale}-ef{args.edge_factor} (a,b,c,d)=(.57,.19,.19,.05) seed 2, degree-sorted; "
-                    f"Modularity refine sweep 1 (singleton start), frac 1.0",
+                    f"Modularity refine sweeps 1-{args.sweeps} of the -s 0 schedule, cycled, frac 1.0",
         "n": int(n),
         "m": int(m),
         "sweep_bytes": int(16 * m + 12 * n + 4),
@@ -239,6 +239,8 @@ def main():
     ap.add_argument("--scale", type=int, default=24)
     ap.add_argument("--edge-factor", type=int, default=16)
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--sweeps", type=int, default=5, help="cycle through the first S sweeps of the schedule")
+    ap.add_argument("--bins", default="", help="degree classes, 7 comma-separated bounds (default: library's)")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
 
@@ -279,29 +281,42 @@ def main():
     d_adj = torch.from_numpy(adj).to(dev)
     torch.cuda.synchronize()
     G = pcd.Graph.from_device(ctx, n, m, d_ind.data_ptr(), d_adj.data_ptr())
-    start = torch.arange(n, dtype=torch.int32, device=dev)  # singleton partition, compressed
-    r = pcd.GlibcRand()
-    r.skip(n)  # create_singleton_partition's n draws
-    seed = r()
+    if args.bins:
+        G.set_bins([int(x) for x in args.bins.split(",")])
     rule = pcd.ModularityRule()
     sweep = pcd.PropagationRefinement(1.0)
+    # The reference schedule (-s 0, frac 1.0): the start partition and rand_r
+    # seed of each of its first S sweeps, kept on the device.
+    seeds = schedule_seeds(n, args.sweeps)  # after create_singleton_partition's n draws
+    starts = []
+    G.set_labels_device(torch.arange(n, dtype=torch.int32, device=dev).data_ptr())
+    for i in range(args.sweeps):
+        G.compress()
+        lab = torch.empty(n, dtype=torch.int32, device=dev)
+        G.get_labels_device(lab.data_ptr())
+        starts.append(lab)
+        sweep.refine(G, rule, seeds[i])
+    stream.synchronize()
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    results = [None] * args.sweeps
 
-    def step(ev0=None, ev1=None):
+    def step(i, ev0=None, ev1=None):
+        j = i % args.sweeps
         with torch.cuda.stream(stream):
             flush.fill_(1)
-            G.set_labels_device(start.data_ptr())
+            G.set_labels_device(starts[j].data_ptr())
             G.compress(sync=False)
             if ev0 is not None:
                 ev0.record(stream)
-            sweep.refine(G, rule, seed)
+            sweep.refine(G, rule, seeds[j])
             if ev1 is not None:
                 ev1.record(stream)
+        return j
 
-    for _ in range(max(3, args.warmup)):
-        step()
-    stream.synchronize()
-    ref_labels = G.labels  # result of one sweep, for a self-consistency check below
+    for i in range(max(3, args.warmup, args.sweeps)):
+        j = step(i)
+        stream.synchronize()
+        results[j] = G.labels  # each sweep's result, for a self-consistency check below
 
     k_before = G.info().kernels_total
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -311,8 +326,8 @@ def main():
     torch.cuda.synchronize()
     clocks.start()
     t_wall = time.perf_counter()
-    for e0, e1 in evs:
-        step(e0, e1)
+    for i, (e0, e1) in enumerate(evs):
+        last = step(i, e0, e1)
     stream.synchronize()
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall
@@ -328,14 +343,15 @@ def main():
         total_ms = float(t.item())
     ms_per_step = total_ms / args.steps
     value = world * m * args.steps / (total_ms / 1e3)
-    assert np.array_equal(G.labels, ref_labels), "sweep result changed between identical steps"
+    assert np.array_equal(G.labels, results[last]), "sweep result changed between identical steps"
 
     # per-phase profile of one more step (events between kernel groups)
     ctx.profile(True)
-    step()
+    step(0)
     phases = ctx.profile_read()
     ctx.profile(False)
     info = G.info()
+    bins_now = G.get_bins()
     peak, peak_kind = load_peaks()
     bb = bins_bytes(ind)
     sweep_phases = {nm: ms for nm, ms in phases if nm.startswith("sweep.")}
@@ -354,7 +370,7 @@ def main():
     if args.e2e_steps > 0:
         h_ind = torch.from_numpy(ind).pin_memory()
         h_adj = torch.from_numpy(adj).pin_memory()
-        h_lab = torch.arange(n, dtype=torch.int32).pin_memory()
+        h_lab = starts[0].cpu().pin_memory()
         h_out = torch.empty(n, dtype=torch.int32).pin_memory()
         G.free()
         torch.cuda.empty_cache()
@@ -362,12 +378,12 @@ def main():
         def e2e_step():
             g2 = pcd.Graph.from_host_ptr(ctx, n, m, h_ind.data_ptr(), h_adj.data_ptr())
             g2.set_labels_ptr(h_lab.data_ptr())
-            sweep.refine(g2, rule, seed)
+            sweep.refine(g2, rule, seeds[0])
             g2.get_labels_ptr(h_out.data_ptr())
             g2.free()
 
         e2e_step()
-        assert np.array_equal(h_out.numpy(), ref_labels), "end-to-end result differs from the resident run"
+        assert np.array_equal(h_out.numpy(), results[0]), "end-to-end result differs from the resident run"
         if dist:
             dist.barrier()
         t0 = time.perf_counter()
@@ -387,10 +403,11 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, k, sec = cpu_sweep_baseline(ind, adj, seed, threads)
+        v, k, sec = cpu_sweeps(ind, adj, seeds, threads, args.sweeps, 30.0)
         cpu = {"value": v, "unit": "edges/s", "cores": threads, "kind": "port",
-               "sample": f"{k} full propagation sweep(s) of the workload graph (median), oracle OpenMP "
-                         f"restatement of PropagationRefinement::refine, {threads} threads, {sec:.1f}s"}
+               "sample": f"{k} propagation sweep(s) (the schedule's first, in order) of the workload graph, "
+                         f"oracle OpenMP restatement of PropagationRefinement::refine, {threads} threads, "
+                         f"{sec:.1f}s"}
 
     if rank == 0:
         line = {
@@ -417,6 +434,8 @@ def main():
             "gpu_launches": int(launches),
             "clocks": clk,
             "phases_ms": {nm: round(ms, 4) for nm, ms in phases},
+            "per_sweep_ms": [round(statistics.mean(sweep_ms[j::args.sweeps]), 3) for j in range(args.sweeps)],
+            "bins": bins_now,
             "sweep_info": {"draws": info.draws, "fp64_recheck_vertices": info.fallback,
                            "tie_replays": info.resolved},
             "wall_s_timed": wall,

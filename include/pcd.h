@@ -92,6 +92,16 @@ pcd_status pcd_load_csr_device(pcd_ctx *ctx, int32_t n, int32_t m, const int32_t
                                const int32_t *d_adj, pcd_graph **out);
 pcd_status pcd_graph_free(pcd_graph *g);
 
+/* Degree classes of the sweep kernels: vertices of degree <= max_deg[i] (and
+ * above max_deg[i-1]) run in class i: 0..3 groups of 4/8/16/32 lanes per
+ * vertex, 4 a warp per vertex, 5 a 256-thread block, 6 a 1024-thread block
+ * with a shared-memory table, and everything above max_deg[6] a 1024-thread
+ * block with its table in HBM.  Bounds must be non-decreasing and at most
+ * {4, 8, 16, 32, 256, 2048, 8192} (the kernels' capacities).  Results do not
+ * depend on the classes; the autotuner and the tests move them. */
+pcd_status pcd_graph_set_bins(pcd_graph *g, const int32_t max_deg[7]);
+pcd_status pcd_graph_get_bins(pcd_graph *g, int32_t max_deg[7], int64_t counts[8]);
+
 /* cuda_labels_to_device / cuda_labels_from_device
  * (src/framework-cuda.cu:135-143).  Host arrays of n labels. */
 pcd_status pcd_labels_set(pcd_graph *g, const int32_t *labels);

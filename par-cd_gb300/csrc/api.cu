@@ -138,6 +138,9 @@ pcd_status pcd_init(pcd_ctx **out, int32_t device) {
     pcd_status s = check_cuda(ctx, cudaSetDevice(device), "cudaSetDevice");
     if (s == PCD_OK) s = check_cuda(ctx, cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking),
                                     "cudaStreamCreate");
+    if (s == PCD_OK) s = check_cuda(ctx, cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking), "side stream");
+    if (s == PCD_OK) s = check_cuda(ctx, cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming), "event");
+    if (s == PCD_OK) s = check_cuda(ctx, cudaEventCreateWithFlags(&ctx->join, cudaEventDisableTiming), "event");
     if (s == PCD_OK) {
         ctx->stream = ctx->own_stream;
         int sms = 0;
@@ -164,7 +167,8 @@ pcd_status pcd_graph_free(pcd_graph *g) {
     if (!g) return PCD_ERR_INVALID_ARGUMENT;
     pcd_ctx *ctx = g->ctx;
     if (ctx && ctx->stream) cudaStreamSynchronize(ctx->stream);
-    for (void *p : g->allocs) cudaFree(p);
+    for (void *p : g->allocs)
+        if (p) cudaFree(p);
     if (g->merge_buf) cudaFree(g->merge_buf);
     if (g->h_ctr) cudaFreeHost(g->h_ctr);
     if (ctx) ctx->graphs.erase(std::remove(ctx->graphs.begin(), ctx->graphs.end(), g), ctx->graphs.end());
@@ -176,6 +180,12 @@ pcd_status pcd_destroy(pcd_ctx *ctx) {
     if (!ctx) return PCD_ERR_INVALID_ARGUMENT;
     while (!ctx->graphs.empty()) pcd_graph_free(ctx->graphs.back());
     for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
+    if (ctx->fork) cudaEventDestroy(ctx->fork);
+    if (ctx->join) cudaEventDestroy(ctx->join);
+    if (ctx->side) {
+        cudaStreamSynchronize(ctx->side);
+        cudaStreamDestroy(ctx->side);
+    }
     if (ctx->own_stream) {
         cudaStreamSynchronize(ctx->own_stream);
         cudaStreamDestroy(ctx->own_stream);
@@ -263,16 +273,32 @@ static pcd_status graph_setup(pcd_ctx *ctx, pcd_graph *g) {
     TRY(dev_alloc(g, (void **)&g->bin_list, sizeof(int32_t) * nn));
     CK(cudaMallocHost((void **)&g->h_ctr, sizeof(DevCounters)), "cudaMallocHost");
     CK(cudaMemsetAsync(g->ctr, 0, sizeof(DevCounters), st), "memset");
-    // hub / FP64 re-evaluation tables: one HBM slice per resident block
+    // FP64 re-evaluation tables: one HBM slice per block, empty between uses
+    // (keys -1, counts 0, first positions 0xffffffff; position arrays need no init)
     int64_t slots = 64;
     while (slots < 2 * (int64_t)std::max(g->max_deg, 1)) slots <<= 1;
-    g->hub_slots = slots;
-    const int64_t per_block = 3 * slots + g->max_deg;
-    int64_t blocks = std::min<int64_t>(ctx->num_sms, std::max<int64_t>(8, (int64_t)(2ll << 30) / (4 * per_block)));
-    g->hub_blocks = (int32_t)std::max<int64_t>(1, blocks);
-    TRY(dev_alloc(g, (void **)&g->hub_scratch, sizeof(int32_t) * (size_t)(per_block * g->hub_blocks)));
+    g->fb_slots = slots;
+    const int64_t fb_stride = 3 * slots + g->max_deg;
+    g->fb_blocks = (int32_t)std::min<int64_t>(8, std::max<int64_t>(1, (int64_t)(1ll << 29) / (4 * fb_stride)));
+    TRY(dev_alloc(g, (void **)&g->fb_scratch, sizeof(int32_t) * (size_t)(fb_stride * g->fb_blocks)));
+    for (int32_t bk = 0; bk < g->fb_blocks; ++bk) {
+        int32_t *base = g->fb_scratch + (int64_t)bk * fb_stride;
+        CK(cudaMemsetAsync(base, 0xff, sizeof(int32_t) * (size_t)slots, st), "fallback scratch");
+        CK(cudaMemsetAsync(base + slots, 0, sizeof(int32_t) * (size_t)slots, st), "fallback scratch");
+        CK(cudaMemsetAsync(base + 2 * slots, 0xff, sizeof(int32_t) * (size_t)slots, st), "fallback scratch");
+    }
+    // hub slices: the same tables plus labels and counts by position
+    const int64_t hub_stride = 3 * slots + 2ll * g->max_deg;
+    g->hub_blocks = (int32_t)std::min<int64_t>(ctx->num_sms, std::max<int64_t>(8, (int64_t)(4ll << 30) / (4 * hub_stride)));
+    TRY(dev_alloc(g, (void **)&g->hub_scratch, sizeof(int32_t) * (size_t)(hub_stride * g->hub_blocks)));
+    for (int32_t bk = 0; bk < g->hub_blocks; ++bk) {
+        int32_t *base = g->hub_scratch + (int64_t)bk * hub_stride;
+        CK(cudaMemsetAsync(base, 0xff, sizeof(int32_t) * (size_t)slots, st), "hub scratch");
+        CK(cudaMemsetAsync(base + slots, 0, sizeof(int32_t) * (size_t)slots, st), "hub scratch");
+        CK(cudaMemsetAsync(base + 2 * slots, 0xff, sizeof(int32_t) * (size_t)slots, st), "hub scratch");
+    }
     // degree bins
-    g->bins = BinConfig{16, 128, 1024, 4096};
+    g->bins = BinConfig{{4, 8, 16, 32, 256, 2048, 8192}};
     if (n > 0) launch_bins(g, st);
     // initial labels: singletons 0..n-1 (already compressed)
     g->k = g->n;
@@ -313,7 +339,8 @@ static pcd_status load_common(pcd_ctx *ctx, int32_t n, int32_t m, const int32_t 
         s = check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "init labels");
     }
     if (s != PCD_OK) {
-        for (void *p : g->allocs) cudaFree(p);
+        for (void *p : g->allocs)
+            if (p) cudaFree(p);
         if (g->h_ctr) cudaFreeHost(g->h_ctr);
         delete g;
         return s;
@@ -331,6 +358,29 @@ pcd_status pcd_load_csr(pcd_ctx *ctx, int32_t n, int32_t m, const int32_t *indic
 pcd_status pcd_load_csr_device(pcd_ctx *ctx, int32_t n, int32_t m, const int32_t *d_indices, const int32_t *d_adj,
                                pcd_graph **out) {
     return load_common(ctx, n, m, d_indices, d_adj, cudaMemcpyDeviceToDevice, out);
+}
+
+pcd_status pcd_graph_set_bins(pcd_graph *g, const int32_t max_deg[7]) {
+    if (!g || !max_deg) return PCD_ERR_INVALID_ARGUMENT;
+    static const int32_t cap[7] = {4, 8, 16, 32, 256, 2048, 8192};
+    for (int i = 0; i < 7; ++i) {
+        if (max_deg[i] < 0 || max_deg[i] > cap[i] || (i && max_deg[i] < max_deg[i - 1]))
+            return set_error(g->ctx, PCD_ERR_INVALID_ARGUMENT, "degree classes out of range");
+    }
+    pcd_ctx *ctx = g->ctx;
+    CK(cudaStreamSynchronize(ctx->stream), "set_bins");
+    for (int i = 0; i < 7; ++i) g->bins.max_deg[i] = max_deg[i];
+    if (g->n > 0) launch_bins(g, ctx->stream);
+    return check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "set_bins");
+}
+
+pcd_status pcd_graph_get_bins(pcd_graph *g, int32_t max_deg[7], int64_t counts[8]) {
+    if (!g) return PCD_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < 7; ++i)
+        if (max_deg) max_deg[i] = g->bins.max_deg[i];
+    for (int i = 0; i < 8; ++i)
+        if (counts) counts[i] = g->bin_off[i + 1] - g->bin_off[i];
+    return PCD_OK;
 }
 
 pcd_status pcd_labels_set(pcd_graph *g, const int32_t *labels) {

@@ -236,15 +236,11 @@ struct MergeArgs {
 
 template <class R>
 __global__ void __launch_bounds__(256) k_merge_analyze(MergeArgs a, R rule) {
-    using E = Elem<KeyD>;
-    struct RD {  // KeyD view of the rule for the scan helpers
-        using Key = KeyD;
-        __device__ static bool gt(Key x, Key y) { return x.s > y.s; }
-    };
+    using E = Elem<double>;
     const int lane = threadIdx.x & 31;
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const KeyD ident{-__longlong_as_double(0x7ff0000000000000LL)};
+    const double ident = R::identity();
     for (int64_t li = gw; li < a.k; li += nw) {
         const int32_t l = (int32_t)li;
         const int32_t bp = a.best[l];
@@ -255,7 +251,8 @@ __global__ void __launch_bounds__(256) k_merge_analyze(MergeArgs a, R rule) {
         }
         const int32_t s0 = a.seg_start[l], s1 = a.seg_end[l];
         int32_t *ties = a.tiebuf + s0 + l + 1;
-        E carry{KeyD{0.0}, -1, -1};
+        E carry{0.0, -1};
+        int32_t holder = -1;
         uint32_t t = 0;
         int32_t r = 0;
         for (int32_t base = s0; base < s1; base += 32) {
@@ -263,29 +260,30 @@ __global__ void __launch_bounds__(256) k_merge_analyze(MergeArgs a, R rule) {
             const bool valid = i < s1;
             int32_t c = -1, w = 0;
             bool sc = false;
-            KeyD key = ident;
+            double key = ident;
             if (valid) {
                 c = a.cb[i];
                 w = a.cw[i];
                 sc = !a.found[c];
                 if (sc) {
-                    key.s = rule.merge(l, c, w, a.cm);
-                    if (key.s != key.s) {  // NaN: neither ties nor wins
+                    key = rule.merge(l, c, w, a.cm);
+                    if (key != key) {  // NaN: neither ties nor wins
                         sc = false;
                         key = ident;
                     }
                 }
             }
-            E x{key, sc ? i : -2, c};
-            E inc = warp_scan_max<RD>(x, lane);
+            const E inc = warp_scan_max<R>(E{key, sc ? i : -2}, lane);
             E ex = shfl_up_any(inc, 1);
-            if (lane == 0) ex = E{ident, -2, -1};
-            E pre = combine<RD>(carry, ex);
-            const bool tie = sc && key.s == pre.key.s;
+            if (lane == 0) ex = E{ident, -2};
+            const E pre = combine<R>(carry, ex);
+            const bool tie = sc && key == pre.key;
             t += __popc(__ballot_sync(FULL, tie));
-            E tot = shfl_any(inc, 31);
-            E nxt = combine<RD>(carry, tot);
-            if (nxt.ord != carry.ord) r = 0;
+            const E nxt = combine<R>(carry, shfl_any(inc, 31));
+            if (nxt.ord != carry.ord) {
+                r = 0;
+                holder = __shfl_sync(FULL, c, nxt.ord - base);
+            }
             const bool inrun = tie && pre.ord == nxt.ord;
             const unsigned run = __ballot_sync(FULL, inrun);
             if (inrun) ties[r + __popc(run & lanemask_lt())] = c;
@@ -294,9 +292,9 @@ __global__ void __launch_bounds__(256) k_merge_analyze(MergeArgs a, R rule) {
         }
         if (lane == 0) {
             a.ndraw[l] = t;
-            a.best[l] = carry.label;  // -1 when no candidate beat 0.0
+            a.best[l] = holder;  // -1 when no candidate beat 0.0
             if (r > 0) {
-                a.tiebuf[s0 + l] = carry.label;
+                a.tiebuf[s0 + l] = holder;
                 const int32_t ri = atomicAdd(&a.ctr->n_resolve, 1);
                 a.recs[ri] = TieRecord{l, r, (long long)(s0 + l)};
             }

@@ -5,7 +5,9 @@
 //   * score     : Rule::calculate for Modularity and CPM (src/rules.cpp:9-22, 121-129)
 //   * validate  : the CSR checks Graph::read leaves implicit
 //   * bins      : vertices grouped by degree class for the sweep kernels
+#include <algorithm>
 #include <climits>
+#include <vector>
 
 #include "pcd_internal.h"
 #include "pcd_scan.cuh"
@@ -155,10 +157,10 @@ int launch_stats(pcd_graph *g, cudaStream_t st) {
     cudaMemsetAsync(g->intv, 0, bytes, st);
     cudaMemsetAsync(g->extv, 0, bytes, st);
     cudaMemsetAsync(g->vol, 0, bytes, st);
-    int64_t nt = g->bin_off[BIN_THREAD + 1] - g->bin_off[BIN_THREAD];
+    int64_t nt = g->bin_off[BIN_WARP] - g->bin_off[0];
     if (nt > 0) {
         k_stats_thread<<<grid_for(nt, 256), 256, 0, st>>>(g->indices, g->adj, g->labels,
-                                                           g->bin_list + g->bin_off[BIN_THREAD], nt, g->sizes,
+                                                           g->bin_list + g->bin_off[0], nt, g->sizes,
                                                            g->intv, g->extv, g->vol);
         ++launches;
     }
@@ -297,11 +299,9 @@ int launch_validate(const int32_t *indices, const int32_t *adj, int32_t n, int32
 // degree bins: stable compaction of the vertices of each class
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int32_t bin_of(int32_t d, const BinConfig &b) {
-    if (d <= b.thread_max) return BIN_THREAD;
-    if (d <= b.warp_max) return BIN_WARP;
-    if (d <= b.block_max) return BIN_BLOCK;
-    if (d <= b.block_l_max) return BIN_BLOCK_L;
-    return BIN_HUB;
+    for (int i = 0; i < NBINS - 1; ++i)
+        if (d <= b.max_deg[i]) return i;
+    return NBINS - 1;
 }
 
 struct BinFlag {

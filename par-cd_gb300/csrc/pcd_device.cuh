@@ -134,36 +134,38 @@ static __device__ __noinline__ double wcc_improvement(int32_t n_x, int32_t n_y, 
 }
 
 // ---------------------------------------------------------------------------
-// Rules.  Each rule defines a Key, its ordering, the join gain of a
-// candidate (vertex of degree d, community c, k neighbours in c) and the
-// final move decision.  Decision codes:
+// Rules.  Each rule defines a scan Key and its order, the join gain of a
+// candidate (vertex v of degree d, community c, k neighbours in c) and the
+// final move decision.  A Tag carries what the exact-integer Modularity key
+// needs to tell equal keys apart (k and the community volume V).
+// ---------------------------------------------------------------------------
 enum : int32_t { DEC_STAY = 0, DEC_MOVE = 1, DEC_NEW = 2, DEC_AMBIGUOUS = 3 };
 
-// FP64 key (CPM, WCC, and Modularity when re-evaluated exactly).
-struct KeyD {
-    double s;
+struct Tag {
+    int32_t k;
+    int32_t V;
 };
 
-// The generic FP64 parts.
+// The FP64 rules: CPM, WCC, and Modularity when re-evaluated exactly.
 template <class Derived>
 struct RuleF64Base {
-    using Key = KeyD;
+    using Key = double;
     static constexpr bool kExactInt = false;
-    __device__ static Key identity() { return {-__longlong_as_double(0x7ff0000000000000LL)}; }
-    __device__ static Key initial() { return {0.0}; }
-    __device__ static bool gt(Key a, Key b) { return a.s > b.s; }
-    __device__ static bool eq(Key a, Key b) { return a.s == b.s; }
+    __device__ static Key identity() { return -__longlong_as_double(0x7ff0000000000000LL); }
+    __device__ static Key initial() { return 0.0; }
+    __device__ static bool gt(Key a, Key b) { return a > b; }
+    __device__ static bool eq(Key a, Key b) { return a == b; }
     // NaN gains compare false against everything in the reference loop:
     // they never win and never tie, exactly like an absent candidate.
-    __device__ static bool usable(Key a) { return a.s == a.s; }
-    __device__ static bool ambiguous_tie(Key, Key, bool) { return false; }
+    __device__ static bool usable(Key a) { return a == a; }
+    __device__ static bool ambiguous_tie(const Tag &, const Tag &, bool) { return false; }
     __device__ bool vertex_ambiguous(int32_t) const { return false; }
     // src/refinement.cpp:169-179
     __device__ int32_t decide(Key best, bool has_best, int32_t v, int32_t d, int32_t curr,
                               int32_t curr_freq, const CommView &cm) const {
         (void)has_best;
         double leave = static_cast<const Derived *>(this)->leave(v, d, curr, curr_freq, cm);
-        double best_score = best.s;
+        double best_score = best;
         best_score += leave;
         if (best_score > 0 && best_score > leave) return DEC_MOVE;
         if (leave > 0) return DEC_NEW;
@@ -174,11 +176,11 @@ struct RuleF64Base {
 // ModularityRule, src/rules.cpp:24-56.
 struct RuleModF64 : RuleF64Base<RuleModF64> {
     int32_t m;
-    __device__ Key join(int32_t, int32_t d, int32_t c, int32_t k, const CommView &cm) const {
+    __device__ Key join(int32_t, int32_t d, int32_t c, int32_t k, const CommView &cm, Tag &) const {
         double e_ij = k / (double)m;
         double a_i = cm.vol[c] / (2.0 * m);
         double a_j = d / (2.0 * m);
-        return {e_ij - 2 * a_i * a_j};
+        return e_ij - 2 * a_i * a_j;
     }
     __device__ double leave(int32_t, int32_t d, int32_t c, int32_t k, const CommView &cm) const {
         double e_ij = k / (double)m;
@@ -197,8 +199,8 @@ struct RuleModF64 : RuleF64Base<RuleModF64> {
 // CPMRule, src/rules.cpp:131-144.
 struct RuleCPM : RuleF64Base<RuleCPM> {
     double lambda;
-    __device__ Key join(int32_t, int32_t, int32_t c, int32_t k, const CommView &cm) const {
-        return {k - lambda * cm.size[c]};
+    __device__ Key join(int32_t, int32_t, int32_t c, int32_t k, const CommView &cm, Tag &) const {
+        return k - lambda * cm.size[c];
     }
     __device__ double leave(int32_t, int32_t, int32_t c, int32_t k, const CommView &cm) const {
         return -(k - lambda * (cm.size[c] - 1));
@@ -211,8 +213,8 @@ struct RuleCPM : RuleF64Base<RuleCPM> {
 // WCCRule, src/rules.cpp:391-436.
 struct RuleWCC : RuleF64Base<RuleWCC> {
     double cc;
-    __device__ Key join(int32_t, int32_t d, int32_t c, int32_t k, const CommView &cm) const {
-        return {wcc_improvement(1, cm.size[c], 1, k, 0, cm.intv[c] / 2, k, d, cm.extv[c], cc)};
+    __device__ Key join(int32_t, int32_t d, int32_t c, int32_t k, const CommView &cm, Tag &) const {
+        return wcc_improvement(1, cm.size[c], 1, k, 0, cm.intv[c] / 2, k, d, cm.extv[c], cc);
     }
     __device__ double leave(int32_t, int32_t d, int32_t c, int32_t k, const CommView &cm) const {
         return -wcc_improvement(1, cm.size[c] - 1, 1, k, 0, cm.intv[c] / 2 - k, k, d,
@@ -238,38 +240,34 @@ struct RuleWCC : RuleF64Base<RuleWCC> {
 // different (k, V), N == 0 against the initial 0.0, N_best == J, J == 0, or
 // m d > 2^47 -- is flagged and the vertex is re-evaluated in FP64
 // (RuleModF64), so the labels are always those of the FP64 computation.
-struct KeyI {
-    long long N;
-    int32_t k;  // -1 marks the initial 0.0
-    int32_t V;
-};
-
 struct RuleModInt {
-    using Key = KeyI;
+    using Key = long long;
     static constexpr bool kExactInt = true;
     int32_t m;
     long long two_m;
-    __device__ static Key identity() { return {LLONG_MIN, 0, 0}; }
-    __device__ static Key initial() { return {0, -1, -1}; }
-    __device__ static bool gt(Key a, Key b) { return a.N > b.N; }
-    __device__ static bool eq(Key a, Key b) { return a.N == b.N; }
+    __device__ static Key identity() { return LLONG_MIN; }
+    __device__ static Key initial() { return 0; }
+    __device__ static bool gt(Key a, Key b) { return a > b; }
+    __device__ static bool eq(Key a, Key b) { return a == b; }
     __device__ static bool usable(Key) { return true; }
-    __device__ static bool ambiguous_tie(Key cand, Key holder, bool) {
-        return holder.k < 0 || cand.k != holder.k || cand.V != holder.V;
+    __device__ static bool ambiguous_tie(const Tag &cand, const Tag &holder, bool holder_real) {
+        return !holder_real || cand.k != holder.k || cand.V != holder.V;
     }
     __device__ bool vertex_ambiguous(int32_t d) const {
         return (long long)m * (long long)d > (1LL << 47);
     }
-    __device__ Key join(int32_t, int32_t d, int32_t c, int32_t k, const CommView &cm) const {
-        int32_t V = cm.vol[c];
-        return {two_m * k - (long long)V * d, k, V};
+    __device__ Key join(int32_t, int32_t d, int32_t c, int32_t k, const CommView &cm, Tag &tag) const {
+        const int32_t V = cm.vol[c];
+        tag.k = k;
+        tag.V = V;
+        return two_m * k - (long long)V * d;
     }
-    __device__ int32_t decide(Key best, bool has_best, int32_t, int32_t d, int32_t curr,
-                              int32_t curr_freq, const CommView &cm) const {
+    __device__ int32_t decide(Key best, bool has_best, int32_t, int32_t d, int32_t curr, int32_t curr_freq,
+                              const CommView &cm) const {
         long long J = two_m * curr_freq - (long long)(cm.vol[curr] - d) * d;
         if (has_best) {
-            if (best.N > J) return DEC_MOVE;
-            if (best.N == J) return DEC_AMBIGUOUS;
+            if (best > J) return DEC_MOVE;
+            if (best == J) return DEC_AMBIGUOUS;
             return DEC_STAY;
         }
         if (J < 0) return DEC_NEW;
@@ -279,15 +277,15 @@ struct RuleModInt {
 };
 
 // ---------------------------------------------------------------------------
-// Ordered running-maximum scan.  An element is (key, ord, label); combining
-// keeps the LEFT element unless the right key is strictly greater -- the
-// reference's `if (score > best_score)` with the first holder of a level kept.
+// Ordered running-maximum scan.  An element is (key, ord); combining keeps the
+// LEFT element unless the right key is strictly greater -- the reference's
+// `if (score > best_score)` with the first holder of a level kept.
+// ord: candidate position, -1 for the initial 0.0, -2 for the identity.
 // ---------------------------------------------------------------------------
 template <class Key>
 struct Elem {
     Key key;
-    int32_t ord;    // candidate position; -1 for the initial 0.0, -2 identity
-    int32_t label;
+    int32_t ord;
 };
 
 template <class R>
@@ -297,34 +295,34 @@ __device__ __forceinline__ Elem<typename R::Key> combine(const Elem<typename R::
 }
 
 template <class T>
-__device__ __forceinline__ T shfl_up_any(const T &v, int delta) {
+__device__ __forceinline__ T shfl_up_any(const T &v, int delta, int width = 32) {
     static_assert(sizeof(T) % 4 == 0, "word-sized");
     T out;
     const int *s = reinterpret_cast<const int *>(&v);
     int *d = reinterpret_cast<int *>(&out);
 #pragma unroll
-    for (int i = 0; i < (int)(sizeof(T) / 4); ++i) d[i] = __shfl_up_sync(FULL, s[i], delta);
+    for (int i = 0; i < (int)(sizeof(T) / 4); ++i) d[i] = __shfl_up_sync(FULL, s[i], delta, width);
     return out;
 }
 
 template <class T>
-__device__ __forceinline__ T shfl_any(const T &v, int src) {
+__device__ __forceinline__ T shfl_any(const T &v, int src, int width = 32) {
     static_assert(sizeof(T) % 4 == 0, "word-sized");
     T out;
     const int *s = reinterpret_cast<const int *>(&v);
     int *d = reinterpret_cast<int *>(&out);
 #pragma unroll
-    for (int i = 0; i < (int)(sizeof(T) / 4); ++i) d[i] = __shfl_sync(FULL, s[i], src);
+    for (int i = 0; i < (int)(sizeof(T) / 4); ++i) d[i] = __shfl_sync(FULL, s[i], src, width);
     return out;
 }
 
-// Inclusive warp scan; every lane must call it.
-template <class R>
-__device__ __forceinline__ Elem<typename R::Key> warp_scan_max(Elem<typename R::Key> x, int lane) {
+// Inclusive scan within aligned groups of `width` lanes; every lane calls it.
+template <class R, int WIDTH = 32>
+__device__ __forceinline__ Elem<typename R::Key> warp_scan_max(Elem<typename R::Key> x, int lane_in_group) {
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        Elem<typename R::Key> o = shfl_up_any(x, d);
-        if (lane >= d) x = combine<R>(o, x);
+    for (int d = 1; d < WIDTH; d <<= 1) {
+        Elem<typename R::Key> o = shfl_up_any(x, d, WIDTH);
+        if (lane_in_group >= d) x = combine<R>(o, x);
     }
     return x;
 }

@@ -14,6 +14,8 @@ struct pcd_ctx {
     int32_t device = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;  // own_stream or the caller's
+    cudaStream_t side = nullptr;    // hubs run here, concurrently with the other degree classes
+    cudaEvent_t fork = nullptr, join = nullptr;
     int32_t num_sms = 0;
     size_t smem_optin = 0;
     std::string last_error;
@@ -52,10 +54,14 @@ struct pcd_graph {
     void *small = nullptr;            // 64 KiB of reduction scratch
     double *d_score = nullptr;        // device result of pcd_score
     pcd::DevCounters *h_ctr = nullptr;  // pinned mirror
-    // hub scratch: per resident hub block, a table of hub_slots entries
+    // FP64 re-evaluation: per block an HBM table of fb_slots entries (kept
+    // empty between vertices) and a position array of max_deg entries
+    int32_t *fb_scratch = nullptr;
+    int64_t fb_slots = 0;    // power of two >= 2 * max_deg
+    int32_t fb_blocks = 0;
+    // hub tables: the same layout, one slice per hub block
     int32_t *hub_scratch = nullptr;
-    int64_t hub_slots = 0;   // power of two >= 2 * max_deg (hub bin)
-    int32_t hub_blocks = 0;  // blocks sharing the scratch
+    int32_t hub_blocks = 0;
     // degree bins
     int32_t *bin_list = nullptr;          // vertices grouped by bin
     int64_t bin_off[pcd::NBINS + 1] = {0};

@@ -43,14 +43,20 @@ struct ScanScratch {
 };
 
 // Degree bins (vertex counts are per graph, fixed at load).
-enum Bin : int32_t { BIN_THREAD = 0, BIN_WARP = 1, BIN_BLOCK = 2, BIN_BLOCK_L = 3, BIN_HUB = 4, NBINS = 5 };
+enum Bin : int32_t {
+    BIN_G4 = 0,    // deg <= 4     : 4 lanes per vertex, 8 vertices per warp
+    BIN_G8 = 1,    // deg <= 8
+    BIN_G16 = 2,   // deg <= 16
+    BIN_G32 = 3,   // deg <= 32    : one warp, row in registers
+    BIN_WARP = 4,  // deg <= 256   : one warp, hash in shared memory
+    BIN_BLOCK = 5, // deg <= 2048  : 256-thread block, table in shared memory
+    BIN_BLOCK_L = 6,  // deg <= 8192 : 1024-thread block, 224 KiB shared table
+    BIN_HUB = 7,   // larger       : 1024-thread block, table in HBM
+    NBINS = 8
+};
 
 struct BinConfig {
-    int32_t thread_max;   // deg <= thread_max       -> one thread per vertex
-    int32_t warp_max;     // deg <= warp_max         -> one warp per vertex
-    int32_t block_max;    // deg <= block_max        -> one 256-thread block, table in smem
-    int32_t block_l_max;  // deg <= block_l_max      -> one 1024-thread block, large smem table
-                          // else                    -> hub: block with its table in HBM
+    int32_t max_deg[NBINS - 1];  // upper degree of each bin but the last
 };
 
 }  // namespace pcd

@@ -98,78 +98,118 @@ __device__ __forceinline__ void write_decision(const SweepArgs &a, int32_t v, in
     a.new_labels[v] = dec == DEC_MOVE ? holder : (dec == DEC_NEW ? -1 : curr);
 }
 
+// Warp-aggregated allocation of tie records: every lane that passes
+// want = r + 1 > 0 gets its own offset in the tie buffer and a record slot.
+// Returns the offset (or -1).  All lanes of the warp must call it.
+__device__ __forceinline__ long long alloc_ties_warp(const SweepArgs &a, int32_t v, int32_t r, int32_t holder,
+                                                    bool want) {
+    const int lane = threadIdx.x & 31;
+    const unsigned wm = __ballot_sync(FULL, want);
+    if (!wm) return -1;
+    int tot;
+    const int words = want ? r + 1 : 0;
+    const int ex = warp_excl_sum(words, lane, &tot);
+    const int leader = __ffs(wm) - 1;
+    unsigned long long base = 0;
+    int32_t rbase = 0;
+    if (lane == leader) {
+        base = atomicAdd(&a.ctr->tie_used, (unsigned long long)tot);
+        rbase = atomicAdd(&a.ctr->n_resolve, __popc(wm));
+    }
+    base = __shfl_sync(FULL, base, leader);
+    rbase = __shfl_sync(FULL, rbase, leader);
+    if (!want) return -1;
+    const long long off = (long long)(base + ex);
+    if (off + r + 1 > a.tiebuf_cap) {
+        atomicOr(&a.ctr->error, ERR_TIEBUF_OVERFLOW);
+        return -1;
+    }
+    a.tiebuf[off] = holder;
+    a.recs[rbase + __popc(wm & lanemask_lt())] = TieRecord{v, r, off};
+    return off;
+}
+
 // ---------------------------------------------------------------------------
-// thread per vertex (deg <= CAP): the reference loop, one vertex per thread,
-// candidates in a per-thread slice of shared memory (stride blockDim).
+// G lanes per vertex (deg <= G, G in {4, 8, 16, 32}): the whole row sits in
+// registers, one neighbour per lane in row order.  Lanes holding the same
+// label are merged with match_any; the lowest lane of each set is the label's
+// first occurrence and carries its count.  The ordered running maximum is a
+// segmented warp scan over the group.
 // ---------------------------------------------------------------------------
-template <class R, int CAP>
-__global__ void __launch_bounds__(128) k_prop_thread(SweepArgs a, R rule, const int32_t *__restrict__ list,
-                                                     int64_t count) {
-    extern __shared__ int32_t smem[];
-    const int T = blockDim.x;
-    int32_t *cl = smem + threadIdx.x;
-    int32_t *cc = smem + T * CAP + threadIdx.x;
+template <class R, int G>
+__global__ void __launch_bounds__(256) k_prop_group(SweepArgs a, R rule, const int32_t *__restrict__ list,
+                                                    int64_t count) {
     using Key = typename R::Key;
-    for (int64_t idx = blockIdx.x * (int64_t)T + threadIdx.x; idx < count; idx += (int64_t)gridDim.x * T) {
-        const int32_t v = list[idx];
-        const int32_t b = a.g.indices[v], e = a.g.indices[v + 1], d = e - b;
-        const int32_t curr = a.labels[v];
-        if (rule.vertex_ambiguous(d)) {
-            push_ambiguous(a, v);
-            continue;
+    using E = Elem<Key>;
+    constexpr int VPW = 32 / G;
+    const int lane = threadIdx.x & 31, gl = lane & (G - 1), gid = lane / G;
+    const unsigned gmask = G == 32 ? FULL : (((1u << G) - 1u) << (gid * G));
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp * VPW; base < count; base += nwarps * VPW) {
+        const int64_t idx = base + gid;
+        const bool has_v = idx < count;
+        const int32_t v = has_v ? list[idx] : 0;
+        const int32_t b = has_v ? a.g.indices[v] : 0;
+        const int32_t d = has_v ? a.g.indices[v + 1] - b : 0;
+        const int32_t curr = has_v ? a.labels[v] : -1;
+        const bool valid = gl < d;
+        const int32_t lab = valid ? a.labels[a.g.adj[b + gl]] : -1;
+        const unsigned long long mk =
+            valid ? (((unsigned long long)(unsigned)gid << 32) | (unsigned)lab) : (~0ull << 32) | (unsigned)lane;
+        const unsigned peers = __match_any_sync(FULL, mk);
+        const bool first = valid && lane == __ffs(peers) - 1;
+        const int32_t k = __popc(peers);
+        const bool is_curr = first && lab == curr;
+        bool sc = first && !is_curr;
+        Tag tag{0, 0};
+        Key key = R::identity();
+        if (sc) {
+            key = rule.join(v, d, lab, k, a.cm, tag);
+            if (!R::usable(key)) {
+                sc = false;
+                key = R::identity();
+            }
         }
-        int32_t nc = 0;
-        for (int32_t j = b; j < e; ++j) {
-            int32_t l = a.labels[a.g.adj[j]];
-            int32_t i = 0;
-            while (i < nc && cl[i * T] != l) ++i;
-            if (i < nc) {
-                cc[i * T] += 1;
+        const E x{key, sc ? gl : -2};
+        const E inc = warp_scan_max<R, G>(x, gl);
+        E ex = shfl_up_any(inc, 1, G);
+        if (gl == 0) ex = E{R::identity(), -2};
+        const E init{R::initial(), -1};
+        const E pre = combine<R>(init, ex);
+        const E fin = combine<R>(init, shfl_any(inc, G - 1, G));
+        const bool tie = sc && R::eq(key, pre.key);
+        // tag of the holder each tie compared against (a lane of this group)
+        const Tag htag{__shfl_sync(FULL, tag.k, pre.ord >= 0 ? pre.ord : gl, G),
+                       __shfl_sync(FULL, tag.V, pre.ord >= 0 ? pre.ord : gl, G)};
+        const bool amb_tie = tie && R::ambiguous_tie(tag, htag, pre.ord >= 0);
+        const bool inrun = tie && pre.ord == fin.ord;
+        const unsigned tm = __ballot_sync(FULL, tie) & gmask;
+        const unsigned rm = __ballot_sync(FULL, inrun) & gmask;
+        const unsigned cm = __ballot_sync(FULL, is_curr) & gmask;
+        bool amb = (__ballot_sync(FULL, amb_tie) & gmask) != 0;
+        const int32_t ck = __shfl_sync(FULL, k, cm ? __ffs(cm) - 1 : lane);
+        const int32_t curr_freq = cm ? ck : 0;
+        const int32_t holder = __shfl_sync(FULL, lab, fin.ord >= 0 ? fin.ord : gl, G);
+        const int32_t r = __popc(rm);
+        int32_t dec = DEC_STAY;
+        if (has_v) {
+            amb |= rule.vertex_ambiguous(d);
+            if (!amb) dec = rule.decide(fin.key, fin.ord >= 0, v, d, curr, curr_freq, a.cm);
+            if (dec == DEC_AMBIGUOUS) amb = true;
+        }
+        const bool leader = has_v && gl == 0;
+        const bool want = leader && !amb && dec == DEC_MOVE && r > 0;
+        long long off = alloc_ties_warp(a, v, r, holder, want);
+        off = __shfl_sync(FULL, off, gid * G);
+        if (off >= 0 && inrun) a.tiebuf[off + 1 + __popc(rm & lanemask_lt())] = lab;
+        if (leader) {
+            if (amb) {
+                push_ambiguous(a, v);
             } else {
-                cl[nc * T] = l;
-                cc[nc * T] = 1;
-                ++nc;
+                a.ndraw[v] = (uint32_t)__popc(tm);
+                write_decision(a, v, dec, holder, curr);
             }
-        }
-        Key M = R::initial();
-        bool has = false, amb = false;
-        int32_t hl = -1, r = 0, curr_freq = 0;
-        uint32_t t = 0;
-        for (int32_t i = 0; i < nc; ++i) {
-            int32_t l = cl[i * T], k = cc[i * T];
-            if (l == curr) {
-                curr_freq = k;
-                continue;
-            }
-            Key s = rule.join(v, d, l, k, a.cm);
-            if (!R::usable(s)) continue;
-            if (R::gt(s, M)) {
-                M = s;
-                hl = l;
-                has = true;
-                r = 0;
-            } else if (R::eq(s, M)) {
-                ++t;
-                amb |= R::ambiguous_tie(s, M, has);
-                cl[r * T] = l;  // r <= i: candidate r was already read
-                ++r;
-            }
-        }
-        if (amb) {
-            push_ambiguous(a, v);
-            continue;
-        }
-        int32_t dec = rule.decide(M, has, v, d, curr, curr_freq, a.cm);
-        if (dec == DEC_AMBIGUOUS) {
-            push_ambiguous(a, v);
-            continue;
-        }
-        a.ndraw[v] = t;
-        write_decision(a, v, dec, hl, curr);
-        if (dec == DEC_MOVE && r > 0) {
-            long long off = alloc_ties(a, v, r, hl);
-            if (off >= 0)
-                for (int32_t j = 0; j < r; ++j) a.tiebuf[off + 1 + j] = cl[j * T];
         }
     }
 }
@@ -177,23 +217,26 @@ __global__ void __launch_bounds__(128) k_prop_thread(SweepArgs a, R rule, const 
 // ---------------------------------------------------------------------------
 // warp per vertex (deg <= WCAP): adjacency in chunks of 32 in order; lanes
 // holding the same label are merged with match_any and the lowest lane (the
-// first occurrence) inserts; new labels get consecutive ordinals in lane
-// order, so ordinals are first-occurrence order.  Then an ordered warp scan
-// of the gains with the running maximum carried across chunks.
+// first occurrence) inserts into the warp's shared hash; new labels get
+// consecutive ordinals in lane order, so ordinals are first-occurrence order.
+// Then an ordered warp scan of the gains with the running maximum carried
+// across chunks.
 // ---------------------------------------------------------------------------
 template <class R, int WCAP>
 __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const int32_t *__restrict__ list,
                                                    int64_t count) {
     constexpr int TS = 2 * WCAP;
+    constexpr int PER_WARP = 2 * TS + 4 * WCAP;
     extern __shared__ int32_t smem[];
     using Key = typename R::Key;
     using E = Elem<Key>;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int32_t *keys = smem + wid * (2 * TS + 3 * WCAP);
+    int32_t *keys = smem + wid * PER_WARP;
     int32_t *ords = keys + TS;
     int32_t *clab = ords + TS;
     int32_t *ccnt = clab + WCAP;
-    int32_t *ties = ccnt + WCAP;
+    int32_t *cvol = ccnt + WCAP;
+    int32_t *ties = cvol + WCAP;
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t idx = gw; idx < count; idx += nw) {
@@ -204,7 +247,9 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
             if (lane == 0) push_ambiguous(a, v);
             continue;
         }
-        for (int i = lane; i < TS; i += 32) keys[i] = -1;
+        int32_t ts = 64;
+        while (ts < 2 * d) ts <<= 1;
+        for (int i = lane; i < ts; i += 32) keys[i] = -1;
         __syncwarp();
         int32_t nc = 0;
         for (int32_t base = b; base < e; base += 32) {
@@ -216,7 +261,7 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
             bool isnew = false;
             uint32_t h = 0;
             if (leader) {
-                h = hash_label(l) & (TS - 1);
+                h = hash_label(l) & (uint32_t)(ts - 1);
                 for (;;) {
                     int32_t kk = keys[h];
                     if (kk == l) break;
@@ -228,7 +273,7 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
                         }
                         if (old == l) break;
                     }
-                    h = (h + 1) & (TS - 1);
+                    h = (h + 1) & (uint32_t)(ts - 1);
                 }
             }
             const unsigned newmask = __ballot_sync(FULL, isnew);
@@ -244,7 +289,8 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
             __syncwarp();
         }
         // ordered scoring
-        E carry{R::initial(), -1, -1};
+        E carry{R::initial(), -1};
+        Tag ctag{0, 0};
         uint32_t t = 0;
         int32_t r = 0, my_curr = 0;
         bool amb = false;
@@ -256,25 +302,34 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
             const bool is_curr = valid && l == curr;
             if (is_curr) my_curr = k;
             bool sc = valid && !is_curr;
+            Tag tag{0, 0};
             Key key = R::identity();
             if (sc) {
-                key = rule.join(v, d, l, k, a.cm);
+                key = rule.join(v, d, l, k, a.cm, tag);
                 if (!R::usable(key)) {
                     sc = false;
                     key = R::identity();
                 }
             }
-            E x{key, sc ? i : -2, l};
-            E inc = warp_scan_max<R>(x, lane);
+            if (!__any_sync(FULL, sc && !R::gt(carry.key, key))) continue;  // nothing reaches the maximum
+            const E inc = warp_scan_max<R>(E{key, sc ? i : -2}, lane);
             E ex = shfl_up_any(inc, 1);
-            if (lane == 0) ex = E{R::identity(), -2, -1};
-            E pre = combine<R>(carry, ex);
+            if (lane == 0) ex = E{R::identity(), -2};
+            const E pre = combine<R>(carry, ex);
             const bool tie = sc && R::eq(key, pre.key);
-            if (tie && R::ambiguous_tie(key, pre.key, pre.ord >= 0)) amb = true;
+            // the holder a tie met: the carried holder or a lane of this chunk
+            const bool in_chunk = pre.ord >= base;
+            const int src = in_chunk ? pre.ord - base : lane;
+            const Tag lt{__shfl_sync(FULL, tag.k, src), __shfl_sync(FULL, tag.V, src)};
+            const Tag htag = in_chunk ? lt : ctag;
+            if (tie && R::ambiguous_tie(tag, htag, pre.ord >= 0)) amb = true;
             t += __popc(__ballot_sync(FULL, tie));
-            E tot = shfl_any(inc, 31);
-            E nxt = combine<R>(carry, tot);
-            if (nxt.ord != carry.ord) r = 0;
+            const E nxt = combine<R>(carry, shfl_any(inc, 31));
+            if (nxt.ord != carry.ord) {
+                r = 0;
+                const int hs = nxt.ord - base;  // a new holder is always in this chunk
+                ctag = Tag{__shfl_sync(FULL, tag.k, hs), __shfl_sync(FULL, tag.V, hs)};
+            }
             const bool inrun = tie && pre.ord == nxt.ord;
             const unsigned run = __ballot_sync(FULL, inrun);
             if (inrun) ties[r + __popc(run & lanemask_lt())] = l;
@@ -284,23 +339,19 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
         __syncwarp();
         amb = __any_sync(FULL, amb);
         const int32_t curr_freq = __reduce_add_sync(FULL, my_curr);
-        if (amb) {
-            if (lane == 0) push_ambiguous(a, v);
-            continue;
-        }
         const bool has = carry.ord >= 0;
-        const int32_t dec = rule.decide(carry.key, has, v, d, curr, curr_freq, a.cm);
+        const int32_t holder = has ? clab[carry.ord] : -1;
+        int32_t dec = amb ? DEC_AMBIGUOUS : rule.decide(carry.key, has, v, d, curr, curr_freq, a.cm);
         if (dec == DEC_AMBIGUOUS) {
             if (lane == 0) push_ambiguous(a, v);
             continue;
         }
-        long long off = -1;
+        long long off = alloc_ties_warp(a, v, r, holder, lane == 0 && dec == DEC_MOVE && r > 0);
+        off = __shfl_sync(FULL, off, 0);
         if (lane == 0) {
             a.ndraw[v] = t;
-            write_decision(a, v, dec, carry.label, curr);
-            if (dec == DEC_MOVE && r > 0) off = alloc_ties(a, v, r, carry.label);
+            write_decision(a, v, dec, holder, curr);
         }
-        off = __shfl_sync(FULL, off, 0);
         if (off >= 0)
             for (int32_t j = lane; j < r; j += 32) a.tiebuf[off + 1 + j] = ties[j];
         __syncwarp();
@@ -308,82 +359,71 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
 }
 
 // ---------------------------------------------------------------------------
-// block per vertex.  Table (key, count, first position) with atomicMin on the
-// first position; then position -> slot, and an ordered block scan over
-// positions (empty positions are identity) reproduces insertion order.
+// block per vertex.  Histogram into a table (label, count, first position)
+// with atomicMin on the first position; position -> slot; then an ordered
+// reduce-then-scan over positions: every warp owns a contiguous range, pass A
+// takes each range's running maximum, one warp combines them into each
+// range's carry-in (starting from the initial 0.0), pass B finds the ties.
 // The table lives in shared memory (block bins) or in a per-block HBM slice
 // (hubs, FP64 re-evaluation).
 // ---------------------------------------------------------------------------
 template <class R>
 struct BlockScratch {
     Elem<typename R::Key> warp_tot[32];
-    Elem<typename R::Key> blk_total;
-    Elem<typename R::Key> run_carry;
-    int32_t warp_cnt[32];
-    int32_t r;
+    Elem<typename R::Key> carry_in[32];
+    Tag carry_tag[32];
+    int32_t warp_label[32];
+    Elem<typename R::Key> fin;
+    int32_t fin_label;
+    int32_t warp_ties[32];
+    int32_t tie_off[32];
     uint32_t t;
     int32_t amb;
     int32_t curr_freq;
+    int32_t holder;
+    int32_t r;
     long long off;
 };
 
-// Block-wide running-max scan (keep-left).  Returns this thread's exclusive
-// prefix; *total receives the block aggregate.  Contains __syncthreads.
+// Warp-wide maximum of a key (all lanes get it).
 template <class R>
-__device__ __forceinline__ Elem<typename R::Key> block_scan_max(Elem<typename R::Key> x, BlockScratch<R> &s,
-                                                                Elem<typename R::Key> *total) {
-    using E = Elem<typename R::Key>;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    E inc = warp_scan_max<R>(x, lane);
-    E ex = shfl_up_any(inc, 1);
-    if (lane == 0) ex = E{R::identity(), -2, -1};
-    if (lane == 31) s.warp_tot[wid] = inc;
-    __syncthreads();
-    if (wid == 0) {
-        E wt = lane < nw ? s.warp_tot[lane] : E{R::identity(), -2, -1};
-        E wi = warp_scan_max<R>(wt, lane);
-        E we = shfl_up_any(wi, 1);
-        if (lane == 0) we = E{R::identity(), -2, -1};
-        if (lane < nw) s.warp_tot[lane] = we;
-        if (lane == 31) s.blk_total = wi;
+__device__ __forceinline__ typename R::Key warp_max_key(typename R::Key k) {
+#pragma unroll
+    for (int d = 16; d; d >>= 1) {
+        typename R::Key o = shfl_any(k, (threadIdx.x & 31) ^ d);
+        if (R::gt(o, k)) k = o;
     }
-    __syncthreads();
-    E res = combine<R>(s.warp_tot[wid], ex);
-    *total = s.blk_total;
-    __syncthreads();
-    return res;
+    return k;
 }
 
-// Exclusive count of `f` over the block in thread order.  Contains __syncthreads.
-__device__ __forceinline__ int block_excl_count(bool f, int32_t *warp_cnt, int *total) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    unsigned m = __ballot_sync(FULL, f);
-    if (lane == 0) warp_cnt[wid] = __popc(m);
-    __syncthreads();
-    int before = 0, tot = 0;
-    for (int w = 0; w < nw; ++w) {
-        int c = warp_cnt[w];
-        before += w < wid ? c : 0;
-        tot += c;
-    }
-    __syncthreads();
-    *total = tot;
-    return before + __popc(m & lanemask_lt());
-}
-
-template <class R, bool GLOBAL>
-__global__ void k_prop_block(SweepArgs a, R rule, const int32_t *__restrict__ list, int64_t count,
-                             const int32_t *count_dev, int32_t table_cap, int32_t *gscratch, int64_t gstride) {
+// The table of a block: keys (-1 = empty), counts, first positions (unsigned,
+// 0xffffffff = none), then the position -> slot array.  Between vertices the
+// table is left empty: pass B clears every slot it reads, and every slot is
+// read exactly once (at its label's first position).  Tables live in shared
+// memory (one per block), in per-block HBM slices (stride gstride), or in a
+// per-vertex HBM region (region_off[list index], hubs: all of them at once).
+// Every loop over positions handles U chunks of 32 per warp step so that U
+// independent gathers are in flight.
+template <class R, bool GLOBAL, int BT, int U>
+__global__ void __launch_bounds__(BT) k_prop_block(SweepArgs a, R rule, const int32_t *__restrict__ list,
+                                                   int64_t count, const int32_t *count_dev, int32_t table_cap,
+                                                   int32_t *gscratch, int64_t gstride,
+                                                   const long long *__restrict__ region_off) {
     using Key = typename R::Key;
     using E = Elem<Key>;
+    constexpr int NW = BT / 32;
     extern __shared__ int32_t smem[];
     __shared__ BlockScratch<R> s;
-    int32_t *keys = GLOBAL ? gscratch + (int64_t)blockIdx.x * gstride : smem;
-    int32_t *cnts = keys + table_cap;
-    int32_t *fpos = cnts + table_cap;
-    int32_t *posarr = fpos + table_cap;  // position -> slot; reused for the tie list
     if (count_dev) count = *count_dev;
-    const int tid = threadIdx.x, BT = blockDim.x, lane = threadIdx.x & 31;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (!GLOBAL) {  // shared tables start empty once per block
+        uint32_t *f = reinterpret_cast<uint32_t *>(smem + 2 * table_cap);
+        for (int32_t i = tid; i < table_cap; i += BT) {
+            smem[i] = -1;
+            smem[table_cap + i] = 0;
+            f[i] = 0xffffffffu;
+        }
+    }
     for (int64_t vi = blockIdx.x; vi < count; vi += gridDim.x) {
         const int32_t v = list[vi];
         const int32_t b = a.g.indices[v], e = a.g.indices[v + 1], d = e - b;
@@ -394,107 +434,508 @@ __global__ void k_prop_block(SweepArgs a, R rule, const int32_t *__restrict__ li
         }
         int32_t ts = 64;
         while (ts < 2 * d) ts <<= 1;
-        if (ts > table_cap) {  // a vertex binned past its table: never expected
+        int32_t cap = table_cap;
+        int32_t *keys = smem;
+        if (GLOBAL) {
+            if (region_off) {
+                keys = gscratch + region_off[vi];
+                cap = ts;
+            } else {
+                keys = gscratch + (int64_t)blockIdx.x * gstride;
+            }
+        }
+        if (ts > cap) {  // a vertex binned past its table: never expected
             if (tid == 0) atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);
             continue;
         }
-        for (int32_t i = tid; i < ts; i += BT) {
-            keys[i] = -1;
-            cnts[i] = 0;
-            fpos[i] = INT_MAX;
-        }
+        int32_t *cnts = keys + cap;
+        uint32_t *fpos = reinterpret_cast<uint32_t *>(cnts + cap);
+        int32_t *posarr = cnts + 2 * cap;  // position -> slot; then each warp's final-level ties
         for (int32_t p = tid; p < d; p += BT) posarr[p] = -1;
         if (tid == 0) {
-            s.run_carry = E{R::initial(), -1, -1};
-            s.r = 0;
             s.t = 0;
             s.amb = 0;
             s.curr_freq = 0;
         }
         __syncthreads();
         // histogram with first positions
-        for (int32_t p0 = 0; p0 < d; p0 += BT) {
-            const int32_t p = p0 + tid;
-            const bool valid = p < d;
-            const int32_t l = valid ? a.labels[a.g.adj[b + p]] : -2;
-            const unsigned peers = __match_any_sync(FULL, l);
-            if (valid && lane == __ffs(peers) - 1) {
-                uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
-                for (;;) {
-                    int32_t kk = keys[h];
-                    if (kk == l) break;
-                    if (kk == -1) {
-                        int32_t old = atomicCAS(&keys[h], -1, l);
-                        if (old == -1 || old == l) break;
+        for (int32_t p0 = 0; p0 < d; p0 += BT * U) {
+            int32_t lab[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int32_t p = p0 + u * BT + tid;
+                lab[u] = p < d ? a.g.adj[b + p] : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) lab[u] = lab[u] >= 0 ? a.labels[lab[u]] : -2;
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int32_t p = p0 + u * BT + tid;
+                const int32_t l = lab[u];
+                const unsigned peers = __match_any_sync(FULL, l);
+                if (p < d && lane == __ffs(peers) - 1) {
+                    uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
+                    for (;;) {
+                        int32_t kk = keys[h];
+                        if (kk == l) break;
+                        if (kk == -1) {
+                            int32_t old = atomicCAS(&keys[h], -1, l);
+                            if (old == -1 || old == l) break;
+                        }
+                        h = (h + 1) & (uint32_t)(ts - 1);
                     }
-                    h = (h + 1) & (uint32_t)(ts - 1);
+                    atomicAdd(&cnts[h], __popc(peers));
+                    atomicMin(&fpos[h], (uint32_t)p);  // leader = lowest lane = first position of the group
                 }
-                atomicAdd(&cnts[h], __popc(peers));
-                atomicMin(&fpos[h], p);  // leader = lowest lane = first position of the group
             }
         }
         __syncthreads();
         for (int32_t i = tid; i < ts; i += BT)
             if (keys[i] != -1) posarr[fpos[i]] = i;
         __syncthreads();
-        // ordered scoring over positions
-        for (int32_t p0 = 0; p0 < d; p0 += BT) {
-            const int32_t p = p0 + tid;
-            const int32_t slot = p < d ? posarr[p] : -1;
-            const bool valid = slot >= 0;
-            const int32_t l = valid ? keys[slot] : -1;
-            const int32_t k = valid ? cnts[slot] : 0;
-            const bool is_curr = valid && l == curr;
-            if (is_curr) s.curr_freq = k;
-            bool sc = valid && !is_curr;
-            Key key = R::identity();
-            if (sc) {
-                key = rule.join(v, d, l, k, a.cm);
-                if (!R::usable(key)) {
-                    sc = false;
-                    key = R::identity();
+        // each warp owns positions [lo, hi)
+        const int32_t span = ((d + NW - 1) / NW + 32 * U - 1) / (32 * U) * (32 * U);
+        const int32_t lo = min(d, wid * span), hi = min(d, lo + span);
+        // pass A: each range's maximum (first position holding it)
+        {
+            E carry{R::identity(), -2};
+            Tag ctag{0, 0};
+            int32_t clabel = -1;
+            for (int32_t base0 = lo; base0 < hi; base0 += 32 * U) {
+                int32_t slot[U], l[U];
+                Key key[U];
+                Tag tag[U];
+                bool sc[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int32_t p = base0 + 32 * u + lane;
+                    slot[u] = p < hi ? posarr[p] : -1;
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    l[u] = slot[u] >= 0 ? keys[slot[u]] : -1;
+                    const int32_t k = slot[u] >= 0 ? cnts[slot[u]] : 0;
+                    if (slot[u] >= 0 && l[u] == curr) s.curr_freq = k;
+                    sc[u] = slot[u] >= 0 && l[u] != curr;
+                    tag[u] = Tag{0, 0};
+                    key[u] = R::identity();
+                    if (sc[u]) {
+                        key[u] = rule.join(v, d, l[u], k, a.cm, tag[u]);
+                        if (!R::usable(key[u])) {
+                            sc[u] = false;
+                            key[u] = R::identity();
+                        }
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (!__any_sync(FULL, sc[u] && R::gt(key[u], carry.key))) continue;
+                    const Key wm = warp_max_key<R>(key[u]);
+                    const int fl = __ffs(__ballot_sync(FULL, sc[u] && R::eq(key[u], wm))) - 1;
+                    carry = E{wm, base0 + 32 * u + fl};
+                    ctag = Tag{__shfl_sync(FULL, tag[u].k, fl), __shfl_sync(FULL, tag[u].V, fl)};
+                    clabel = __shfl_sync(FULL, l[u], fl);
                 }
             }
-            E tot;
-            const E ex = block_scan_max<R>(E{key, sc ? p : -2, l}, s, &tot);  // all posarr reads are done
-            const E carry = s.run_carry;
-            const E pre = combine<R>(carry, ex);
-            const bool tie = sc && R::eq(key, pre.key);
-            if (tie && R::ambiguous_tie(key, pre.key, pre.ord >= 0)) s.amb = 1;
-            const unsigned tm = __ballot_sync(FULL, tie);
-            if (lane == 0 && tm) atomicAdd(&s.t, (uint32_t)__popc(tm));
-            const E nxt = combine<R>(carry, tot);
-            const bool inrun = tie && pre.ord == nxt.ord;
-            int run_total;
-            const int rank = block_excl_count(inrun, s.warp_cnt, &run_total);
-            const int32_t r0 = nxt.ord != carry.ord ? 0 : s.r;
-            // r0 + rank < candidates seen so far <= p0 + BT: only positions already read are overwritten
-            if (inrun) posarr[r0 + rank] = l;
-            __syncthreads();
-            if (tid == 0) {
-                s.r = r0 + run_total;
-                s.run_carry = nxt;
+            if (lane == 0) {
+                s.warp_tot[wid] = carry;
+                s.carry_tag[wid] = ctag;  // tag and label of this range's maximum
+                s.warp_label[wid] = clabel;
             }
-            __syncthreads();
         }
+        __syncthreads();
+        if (wid == 0) {
+            const E wt = lane < NW ? s.warp_tot[lane] : E{R::identity(), -2};
+            const Tag wtag = lane < NW ? s.carry_tag[lane] : Tag{0, 0};
+            const E wi = warp_scan_max<R>(wt, lane);
+            E we = shfl_up_any(wi, 1);
+            if (lane == 0) we = E{R::identity(), -2};
+            const E init{R::initial(), -1};
+            const E cin = combine<R>(init, we);
+            const E fin = combine<R>(init, shfl_any(wi, 31));
+            int src = lane, fsrc = 0;
+            for (int w2 = 0; w2 < NW; ++w2) {
+                const int32_t o = __shfl_sync(FULL, wt.ord, w2);
+                if (cin.ord >= 0 && o == cin.ord) src = w2;
+                if (fin.ord >= 0 && o == fin.ord) fsrc = w2;
+            }
+            const Tag ct{__shfl_sync(FULL, wtag.k, src), __shfl_sync(FULL, wtag.V, src)};
+            const int32_t wl = lane < NW ? s.warp_label[lane] : -1;
+            const int32_t fl = __shfl_sync(FULL, wl, fsrc);
+            __syncwarp();
+            if (lane < NW) {
+                s.carry_in[lane] = cin;
+                s.carry_tag[lane] = ct;
+            }
+            if (lane == 0) {
+                s.fin = fin;
+                s.fin_label = fin.ord >= 0 ? fl : -1;
+            }
+        }
+        __syncthreads();
+        // pass B: ties against the true running maximum; clears the table
+        {
+            E carry = s.carry_in[wid];
+            Tag ctag = s.carry_tag[wid];
+            const E fin = s.fin;
+            uint32_t t = 0;
+            int32_t nt = 0;  // this warp's final-level ties so far
+            bool amb = false;
+            for (int32_t base0 = lo; base0 < hi; base0 += 32 * U) {
+                int32_t slot[U], l[U];
+                Key key[U];
+                Tag tag[U];
+                bool sc[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int32_t p = base0 + 32 * u + lane;
+                    slot[u] = p < hi ? posarr[p] : -1;
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    l[u] = -1;
+                    int32_t k = 0;
+                    if (slot[u] >= 0) {
+                        l[u] = keys[slot[u]];
+                        k = cnts[slot[u]];
+                        keys[slot[u]] = -1;
+                        cnts[slot[u]] = 0;
+                        fpos[slot[u]] = 0xffffffffu;
+                    }
+                    sc[u] = slot[u] >= 0 && l[u] != curr;
+                    tag[u] = Tag{0, 0};
+                    key[u] = R::identity();
+                    if (sc[u]) {
+                        key[u] = rule.join(v, d, l[u], k, a.cm, tag[u]);
+                        if (!R::usable(key[u])) {
+                            sc[u] = false;
+                            key[u] = R::identity();
+                        }
+                    }
+                }
+                __syncwarp();  // all lanes have read posarr[base0, base0 + 32 U)
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (!__any_sync(FULL, sc[u] && !R::gt(carry.key, key[u]))) continue;  // below the maximum
+                    const int32_t base = base0 + 32 * u;
+                    const E inc = warp_scan_max<R>(E{key[u], sc[u] ? base + lane : -2}, lane);
+                    E ex = shfl_up_any(inc, 1);
+                    if (lane == 0) ex = E{R::identity(), -2};
+                    const E pre = combine<R>(carry, ex);
+                    const bool tie = sc[u] && R::eq(key[u], pre.key);
+                    const bool in_chunk = pre.ord >= base;
+                    const int src = in_chunk ? pre.ord - base : lane;
+                    const Tag lt{__shfl_sync(FULL, tag[u].k, src), __shfl_sync(FULL, tag[u].V, src)};
+                    const Tag htag = in_chunk ? lt : ctag;
+                    if (tie && R::ambiguous_tie(tag[u], htag, pre.ord >= 0)) amb = true;
+                    t += __popc(__ballot_sync(FULL, tie));
+                    const E nxt = combine<R>(carry, shfl_any(inc, 31));
+                    if (nxt.ord != carry.ord) {
+                        const int hs = nxt.ord - base;
+                        ctag = Tag{__shfl_sync(FULL, tag[u].k, hs), __shfl_sync(FULL, tag[u].V, hs)};
+                    }
+                    const bool inrun = tie && pre.ord == fin.ord;
+                    const unsigned run = __ballot_sync(FULL, inrun);
+                    // nt + rank < positions of this range already read: overwrites only consumed slots
+                    if (inrun) posarr[lo + nt + __popc(run & lanemask_lt())] = l[u];
+                    nt += __popc(run);
+                    carry = nxt;
+                }
+            }
+            amb = __any_sync(FULL, amb);
+            if (lane == 0) {
+                s.warp_ties[wid] = nt;
+                if (t) atomicAdd(&s.t, t);
+                if (amb) s.amb = 1;
+            }
+        }
+        __syncthreads();
         if (tid == 0) {
+            const E c = s.fin;
+            int32_t r = 0;
+            for (int w = 0; w < NW; ++w) {
+                s.tie_off[w] = r;
+                r += s.warp_ties[w];
+            }
+            s.r = r;
             s.off = -1;
-            const E c = s.run_carry;
-            int32_t dec = DEC_AMBIGUOUS;
-            if (!s.amb) dec = rule.decide(c.key, c.ord >= 0, v, d, curr, s.curr_freq, a.cm);
+            const int32_t dec = s.amb ? DEC_AMBIGUOUS : rule.decide(c.key, c.ord >= 0, v, d, curr, s.curr_freq, a.cm);
             if (dec == DEC_AMBIGUOUS) {
                 push_ambiguous(a, v);
             } else {
                 a.ndraw[v] = s.t;
-                write_decision(a, v, dec, c.label, curr);
-                if (dec == DEC_MOVE && s.r > 0) s.off = alloc_ties(a, v, s.r, c.label);
+                write_decision(a, v, dec, s.fin_label, curr);
+                if (dec == DEC_MOVE && r > 0) s.off = alloc_ties(a, v, r, s.fin_label);
             }
         }
         __syncthreads();
-        const long long off = s.off;
-        const int32_t r = s.r;
-        if (off >= 0)
-            for (int32_t j = tid; j < r; j += BT) a.tiebuf[off + 1 + j] = posarr[j];
+        {
+            const long long off = s.off;
+            if (off >= 0) {
+                const int32_t nt = s.warp_ties[wid], o = s.tie_off[wid];
+                for (int32_t j = lane; j < nt; j += 32) a.tiebuf[off + 1 + o + j] = posarr[lo + j];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// hubs: one 512-thread block per vertex with the table in a per-block HBM
+// slice.  Random HBM traffic is what costs here, so after the histogram the
+// table is walked once in slot order: each candidate is written to
+// position-indexed arrays (label, count) at its first position and its slot
+// is cleared in the same coalesced sweep.  The ordered passes then read the
+// position arrays sequentially.  Slice layout: keys, counts, first positions
+// (fb_slots each), labels and counts by position (max degree each).
+// ---------------------------------------------------------------------------
+template <class R, int U>
+__global__ void __launch_bounds__(512) k_prop_hub(SweepArgs a, R rule, const int32_t *__restrict__ list,
+                                                  int64_t count, int32_t slots, int32_t *gscratch, int64_t gstride) {
+    using Key = typename R::Key;
+    using E = Elem<Key>;
+    constexpr int BT = 512, NW = BT / 32;
+    __shared__ BlockScratch<R> s;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    int32_t *keys = gscratch + (int64_t)blockIdx.x * gstride;
+    int32_t *cnts = keys + slots;
+    uint32_t *fpos = reinterpret_cast<uint32_t *>(cnts + slots);
+    int32_t *posL = cnts + 2 * slots;
+    for (int64_t vi = blockIdx.x; vi < count; vi += gridDim.x) {
+        const int32_t v = list[vi];
+        const int32_t b = a.g.indices[v], e = a.g.indices[v + 1], d = e - b;
+        const int32_t curr = a.labels[v];
+        if (rule.vertex_ambiguous(d)) {
+            if (tid == 0) push_ambiguous(a, v);
+            continue;
+        }
+        int32_t ts = 64;
+        while (ts < 2 * d) ts <<= 1;
+        if (ts > slots) {
+            if (tid == 0) atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);
+            continue;
+        }
+        int32_t *posC = posL + d;
+        for (int32_t p = tid; p < d; p += BT) posL[p] = -1;
+        if (tid == 0) {
+            s.t = 0;
+            s.amb = 0;
+            s.curr_freq = 0;
+        }
+        __syncthreads();
+        for (int32_t p0 = 0; p0 < d; p0 += BT * U) {
+            int32_t lab[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int32_t p = p0 + u * BT + tid;
+                lab[u] = p < d ? a.g.adj[b + p] : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) lab[u] = lab[u] >= 0 ? a.labels[lab[u]] : -2;
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int32_t p = p0 + u * BT + tid;
+                const int32_t l = lab[u];
+                const unsigned peers = __match_any_sync(FULL, l);
+                if (p < d && lane == __ffs(peers) - 1) {
+                    uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
+                    for (;;) {
+                        int32_t kk = keys[h];
+                        if (kk == l) break;
+                        if (kk == -1) {
+                            int32_t old = atomicCAS(&keys[h], -1, l);
+                            if (old == -1 || old == l) break;
+                        }
+                        h = (h + 1) & (uint32_t)(ts - 1);
+                    }
+                    atomicAdd(&cnts[h], __popc(peers));
+                    atomicMin(&fpos[h], (uint32_t)p);
+                }
+            }
+        }
+        __syncthreads();
+        for (int32_t i = tid; i < ts; i += BT) {
+            const int32_t kk = keys[i];
+            if (kk != -1) {
+                const uint32_t fp = fpos[i];
+                posL[fp] = kk;
+                posC[fp] = cnts[i];
+                keys[i] = -1;
+                cnts[i] = 0;
+                fpos[i] = 0xffffffffu;
+            }
+        }
+        __syncthreads();
+        const int32_t span = ((d + NW - 1) / NW + 32 * U - 1) / (32 * U) * (32 * U);
+        const int32_t lo = min(d, wid * span), hi = min(d, lo + span);
+        {  // pass A
+            E carry{R::identity(), -2};
+            Tag ctag{0, 0};
+            int32_t clabel = -1;
+            for (int32_t base0 = lo; base0 < hi; base0 += 32 * U) {
+                int32_t l[U], k[U];
+                Key key[U];
+                Tag tag[U];
+                bool sc[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int32_t p = base0 + 32 * u + lane;
+                    l[u] = p < hi ? posL[p] : -1;
+                    k[u] = p < hi ? posC[p] : 0;
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (l[u] >= 0 && l[u] == curr) s.curr_freq = k[u];
+                    sc[u] = l[u] >= 0 && l[u] != curr;
+                    tag[u] = Tag{0, 0};
+                    key[u] = R::identity();
+                    if (sc[u]) {
+                        key[u] = rule.join(v, d, l[u], k[u], a.cm, tag[u]);
+                        if (!R::usable(key[u])) {
+                            sc[u] = false;
+                            key[u] = R::identity();
+                        }
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (!__any_sync(FULL, sc[u] && R::gt(key[u], carry.key))) continue;
+                    const Key wm = warp_max_key<R>(key[u]);
+                    const int fl = __ffs(__ballot_sync(FULL, sc[u] && R::eq(key[u], wm))) - 1;
+                    carry = E{wm, base0 + 32 * u + fl};
+                    ctag = Tag{__shfl_sync(FULL, tag[u].k, fl), __shfl_sync(FULL, tag[u].V, fl)};
+                    clabel = __shfl_sync(FULL, l[u], fl);
+                }
+            }
+            if (lane == 0) {
+                s.warp_tot[wid] = carry;
+                s.carry_tag[wid] = ctag;
+                s.warp_label[wid] = clabel;
+            }
+        }
+        __syncthreads();
+        if (wid == 0) {
+            const E wt = lane < NW ? s.warp_tot[lane] : E{R::identity(), -2};
+            const Tag wtag = lane < NW ? s.carry_tag[lane] : Tag{0, 0};
+            const E wi = warp_scan_max<R>(wt, lane);
+            E we = shfl_up_any(wi, 1);
+            if (lane == 0) we = E{R::identity(), -2};
+            const E init{R::initial(), -1};
+            const E cin = combine<R>(init, we);
+            const E fin = combine<R>(init, shfl_any(wi, 31));
+            int src = lane, fsrc = 0;
+            for (int w2 = 0; w2 < NW; ++w2) {
+                const int32_t o = __shfl_sync(FULL, wt.ord, w2);
+                if (cin.ord >= 0 && o == cin.ord) src = w2;
+                if (fin.ord >= 0 && o == fin.ord) fsrc = w2;
+            }
+            const Tag ct{__shfl_sync(FULL, wtag.k, src), __shfl_sync(FULL, wtag.V, src)};
+            const int32_t wl = lane < NW ? s.warp_label[lane] : -1;
+            const int32_t fl = __shfl_sync(FULL, wl, fsrc);
+            __syncwarp();
+            if (lane < NW) {
+                s.carry_in[lane] = cin;
+                s.carry_tag[lane] = ct;
+            }
+            if (lane == 0) {
+                s.fin = fin;
+                s.fin_label = fin.ord >= 0 ? fl : -1;
+            }
+        }
+        __syncthreads();
+        {  // pass B
+            E carry = s.carry_in[wid];
+            Tag ctag = s.carry_tag[wid];
+            const E fin = s.fin;
+            uint32_t t = 0;
+            int32_t nt = 0;
+            bool amb = false;
+            for (int32_t base0 = lo; base0 < hi; base0 += 32 * U) {
+                int32_t l[U], k[U];
+                Key key[U];
+                Tag tag[U];
+                bool sc[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int32_t p = base0 + 32 * u + lane;
+                    l[u] = p < hi ? posL[p] : -1;
+                    k[u] = p < hi ? posC[p] : 0;
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    sc[u] = l[u] >= 0 && l[u] != curr;
+                    tag[u] = Tag{0, 0};
+                    key[u] = R::identity();
+                    if (sc[u]) {
+                        key[u] = rule.join(v, d, l[u], k[u], a.cm, tag[u]);
+                        if (!R::usable(key[u])) {
+                            sc[u] = false;
+                            key[u] = R::identity();
+                        }
+                    }
+                }
+                __syncwarp();
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (!__any_sync(FULL, sc[u] && !R::gt(carry.key, key[u]))) continue;
+                    const int32_t base = base0 + 32 * u;
+                    const E inc = warp_scan_max<R>(E{key[u], sc[u] ? base + lane : -2}, lane);
+                    E ex = shfl_up_any(inc, 1);
+                    if (lane == 0) ex = E{R::identity(), -2};
+                    const E pre = combine<R>(carry, ex);
+                    const bool tie = sc[u] && R::eq(key[u], pre.key);
+                    const bool in_chunk = pre.ord >= base;
+                    const int src = in_chunk ? pre.ord - base : lane;
+                    const Tag lt{__shfl_sync(FULL, tag[u].k, src), __shfl_sync(FULL, tag[u].V, src)};
+                    const Tag htag = in_chunk ? lt : ctag;
+                    if (tie && R::ambiguous_tie(tag[u], htag, pre.ord >= 0)) amb = true;
+                    t += __popc(__ballot_sync(FULL, tie));
+                    const E nxt = combine<R>(carry, shfl_any(inc, 31));
+                    if (nxt.ord != carry.ord) {
+                        const int hs = nxt.ord - base;
+                        ctag = Tag{__shfl_sync(FULL, tag[u].k, hs), __shfl_sync(FULL, tag[u].V, hs)};
+                    }
+                    const bool inrun = tie && pre.ord == fin.ord;
+                    const unsigned run = __ballot_sync(FULL, inrun);
+                    if (inrun) posL[lo + nt + __popc(run & lanemask_lt())] = l[u];
+                    nt += __popc(run);
+                    carry = nxt;
+                }
+            }
+            amb = __any_sync(FULL, amb);
+            if (lane == 0) {
+                s.warp_ties[wid] = nt;
+                if (t) atomicAdd(&s.t, t);
+                if (amb) s.amb = 1;
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            const E c = s.fin;
+            int32_t r = 0;
+            for (int w = 0; w < NW; ++w) {
+                s.tie_off[w] = r;
+                r += s.warp_ties[w];
+            }
+            s.r = r;
+            s.off = -1;
+            const int32_t dec = s.amb ? DEC_AMBIGUOUS : rule.decide(c.key, c.ord >= 0, v, d, curr, s.curr_freq, a.cm);
+            if (dec == DEC_AMBIGUOUS) {
+                push_ambiguous(a, v);
+            } else {
+                a.ndraw[v] = s.t;
+                write_decision(a, v, dec, s.fin_label, curr);
+                if (dec == DEC_MOVE && r > 0) s.off = alloc_ties(a, v, r, s.fin_label);
+            }
+        }
+        __syncthreads();
+        {
+            const long long off = s.off;
+            if (off >= 0) {
+                const int32_t nt = s.warp_ties[wid], o = s.tie_off[wid];
+                for (int32_t j = lane; j < nt; j += 32) a.tiebuf[off + 1 + o + j] = posL[lo + j];
+            }
+        }
         __syncthreads();
     }
 }
@@ -575,14 +1016,25 @@ __global__ void k_reset_sweep(DevCounters *ctr) {
 // ---------------------------------------------------------------------------
 // host launcher
 // ---------------------------------------------------------------------------
-constexpr int THREAD_CAP = 16;
-constexpr int WARP_CAP = 128;
-constexpr int BLOCK_CAP = 1024;    // table 2048
-constexpr int BLOCK_L_CAP = 4096;  // table 8192
+constexpr int WARP_CAP = 256;
+constexpr int BLOCK_CAP = 2048;    // table 4096, 256 threads
+constexpr int BLOCK_L_CAP = 8192;  // table 16384, 1024 threads
 
 static inline unsigned cap_grid(int64_t want, int64_t cap) {
     if (want < 1) want = 1;
     return (unsigned)(want < cap ? want : cap);
+}
+
+template <class R, int G>
+static void launch_group(pcd_graph *g, const SweepArgs &a, const R &rule, int bin, const char *name,
+                         cudaStream_t st, int *launches) {
+    const int64_t c = g->bin_off[bin + 1] - g->bin_off[bin];
+    if (c <= 0) return;
+    const int64_t warps = (c + (32 / G) - 1) / (32 / G);
+    k_prop_group<R, G><<<cap_grid((warps + 7) / 8, (int64_t)g->ctx->num_sms * 16), 256, 0, st>>>(
+        a, rule, g->bin_list + g->bin_off[bin], c);
+    ++*launches;
+    prof_mark(g->ctx, name, st);
 }
 
 template <class R>
@@ -591,39 +1043,41 @@ static int launch_bins_rule(pcd_graph *g, const SweepArgs &a, const R &rule, cud
     int launches = 0;
     const int32_t *L = g->bin_list;
     int64_t c;
-    if ((c = g->bin_off[BIN_THREAD + 1] - g->bin_off[BIN_THREAD]) > 0) {
-        size_t smem = 2ull * 128 * THREAD_CAP * sizeof(int32_t);
-        k_prop_thread<R, THREAD_CAP><<<cap_grid((c + 127) / 128, sms * 16), 128, smem, st>>>(
-            a, rule, L + g->bin_off[BIN_THREAD], c);
-        ++launches;
-        prof_mark(g->ctx, "sweep.thread", st);
-    }
+    launch_group<R, 4>(g, a, rule, BIN_G4, "sweep.g4", st, &launches);
+    launch_group<R, 8>(g, a, rule, BIN_G8, "sweep.g8", st, &launches);
+    launch_group<R, 16>(g, a, rule, BIN_G16, "sweep.g16", st, &launches);
+    launch_group<R, 32>(g, a, rule, BIN_G32, "sweep.g32", st, &launches);
     if ((c = g->bin_off[BIN_WARP + 1] - g->bin_off[BIN_WARP]) > 0) {
-        size_t smem = 8ull * (2 * 2 * WARP_CAP + 3 * WARP_CAP) * sizeof(int32_t);
+        const size_t smem = 8ull * (2 * 2 * WARP_CAP + 4 * WARP_CAP) * sizeof(int32_t);
+        cudaFuncSetAttribute(k_prop_warp<R, WARP_CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_prop_warp<R, WARP_CAP><<<cap_grid((c + 7) / 8, sms * 8), 256, smem, st>>>(a, rule,
                                                                                 L + g->bin_off[BIN_WARP], c);
         ++launches;
         prof_mark(g->ctx, "sweep.warp", st);
     }
     if ((c = g->bin_off[BIN_BLOCK + 1] - g->bin_off[BIN_BLOCK]) > 0) {
-        size_t smem = (3ull * 2 * BLOCK_CAP + BLOCK_CAP) * sizeof(int32_t);
-        k_prop_block<R, false><<<cap_grid(c, sms * 6), 256, smem, st>>>(
-            a, rule, L + g->bin_off[BIN_BLOCK], c, nullptr, 2 * BLOCK_CAP, nullptr, 0);
+        const size_t smem = (3ull * 2 * BLOCK_CAP + BLOCK_CAP) * sizeof(int32_t);
+        cudaFuncSetAttribute(k_prop_block<R, false, 256, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        k_prop_block<R, false, 256, 4><<<cap_grid(c, sms * 4), 256, smem, st>>>(
+            a, rule, L + g->bin_off[BIN_BLOCK], c, nullptr, 2 * BLOCK_CAP, nullptr, 0, nullptr);
         ++launches;
         prof_mark(g->ctx, "sweep.block", st);
     }
     if ((c = g->bin_off[BIN_BLOCK_L + 1] - g->bin_off[BIN_BLOCK_L]) > 0) {
-        size_t smem = (3ull * 2 * BLOCK_L_CAP + BLOCK_L_CAP) * sizeof(int32_t);
-        cudaFuncSetAttribute(k_prop_block<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_prop_block<R, false><<<cap_grid(c, sms * 2), 512, smem, st>>>(
-            a, rule, L + g->bin_off[BIN_BLOCK_L], c, nullptr, 2 * BLOCK_L_CAP, nullptr, 0);
+        const size_t smem = (3ull * 2 * BLOCK_L_CAP + BLOCK_L_CAP) * sizeof(int32_t);
+        cudaFuncSetAttribute(k_prop_block<R, false, 512, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        k_prop_block<R, false, 512, 4><<<cap_grid(c, sms), 512, smem, st>>>(
+            a, rule, L + g->bin_off[BIN_BLOCK_L], c, nullptr, 2 * BLOCK_L_CAP, nullptr, 0, nullptr);
         ++launches;
         prof_mark(g->ctx, "sweep.block_l", st);
     }
     if ((c = g->bin_off[BIN_HUB + 1] - g->bin_off[BIN_HUB]) > 0) {
-        k_prop_block<R, true><<<cap_grid(c, g->hub_blocks), 512, 0, st>>>(
-            a, rule, L + g->bin_off[BIN_HUB], c, nullptr, (int32_t)g->hub_slots, g->hub_scratch,
-            3 * g->hub_slots + g->max_deg);
+        // hubs: 512-thread blocks, tables in per-block HBM slices kept empty between vertices
+        k_prop_hub<R, 4><<<cap_grid(c, g->hub_blocks), 512, 0, st>>>(
+            a, rule, L + g->bin_off[BIN_HUB], c, (int32_t)g->fb_slots, g->hub_scratch,
+            3 * g->fb_slots + 2ll * g->max_deg);
         ++launches;
         prof_mark(g->ctx, "sweep.hub", st);
     }
@@ -655,9 +1109,9 @@ int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32
         launches += launch_bins_rule(g, a, r, st);
         RuleModF64 rf;
         rf.m = g->m;
-        k_prop_block<RuleModF64, true><<<g->hub_blocks, 512, 0, st>>>(
-            a, rf, g->amb, 0, &g->ctr->n_ambiguous, (int32_t)g->hub_slots, g->hub_scratch,
-            3 * g->hub_slots + g->max_deg);
+        k_prop_block<RuleModF64, true, 512, 2><<<g->fb_blocks, 512, 0, st>>>(
+            a, rf, g->amb, 0, &g->ctr->n_ambiguous, (int32_t)g->fb_slots, g->fb_scratch,
+            3 * g->fb_slots + g->max_deg, nullptr);
         ++launches;
         prof_mark(g->ctx, "sweep.fp64_recheck", st);
     } else if (kind == PCD_RULE_CPM) {

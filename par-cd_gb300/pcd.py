@@ -74,6 +74,8 @@ def _load() -> C.CDLL:
         "pcd_contract": ([vp, i64, vp, vp, vp, C.POINTER(i64)], i32),
         "pcd_sweep_info_get": ([vp, C.POINTER(_Info)], i32),
         "pcd_profile_enable": ([vp, i32], i32),
+        "pcd_graph_set_bins": ([vp, C.POINTER(i32)], i32),
+        "pcd_graph_get_bins": ([vp, C.POINTER(i32), C.POINTER(i64)], i32),
         "pcd_profile_read": ([vp, C.POINTER(C.c_char_p), C.POINTER(dbl), i32], i32),
         "pcd_rand_seed": ([C.POINTER(_Rand), u32], None),
         "pcd_rand_next": ([C.POINTER(_Rand)], i32),
@@ -304,6 +306,16 @@ class Graph:
         w = np.zeros(max(P, 1), np.int32)
         self.ctx._check(LIB.pcd_contract(self.h, P, _ptr(a), _ptr(b), _ptr(w), C.byref(npairs)))
         return a[:P], b[:P], w[:P]
+
+    def set_bins(self, max_deg):
+        arr = (C.c_int32 * 7)(*[int(x) for x in max_deg])
+        self.ctx._check(LIB.pcd_graph_set_bins(self.h, arr))
+
+    def get_bins(self):
+        md = (C.c_int32 * 7)()
+        cnt = (C.c_int64 * 8)()
+        self.ctx._check(LIB.pcd_graph_get_bins(self.h, md, cnt))
+        return list(md), list(cnt)
 
     def info(self) -> SweepInfo:
         i = _Info()

@@ -209,3 +209,53 @@ def test_edge_cases(ctx, port):
     with pytest.raises(pcd.PcdError):
         pcd.MergingRefinement(0).refine(G, pcd.ModularityRule(), 1)
     G.free()
+
+
+BIN_LAYOUTS = [
+    [4, 8, 16, 32, 256, 2048, 8192],   # default
+    [0, 0, 0, 0, 0, 0, 0],             # everything in HBM-table blocks
+    [0, 0, 0, 0, 0, 0, 8192],          # everything in 1024-thread shared-table blocks
+    [0, 0, 0, 0, 0, 2048, 2048],       # 256-thread blocks (+ HBM beyond)
+    [0, 0, 0, 0, 256, 256, 256],       # warps (+ HBM beyond)
+    [4, 4, 4, 4, 4, 4, 4],             # 4-lane groups, the rest in HBM
+    [2, 5, 9, 20, 60, 200, 700],       # a bit of everything
+]
+
+
+@pytest.mark.parametrize("bins", BIN_LAYOUTS, ids=lambda b: "-".join(map(str, b)))
+@pytest.mark.parametrize("gname,metric", [("rmat12", "mod"), ("pl20k", "cpm-0.01"), ("rmat12", "wcc")])
+def test_every_kernel_class_matches_oracle(ctx, port, bins, gname, metric):
+    """The same sweeps with vertices forced into each kernel class."""
+    import oracle
+    import pcd
+
+    g = golden_graph(gname)
+    init = 1 if metric == "wcc" else 0
+    G = pcd.Graph.from_csr(ctx, g.indices, g.adj)
+    G.set_bins(bins)
+    got = []
+    pcd.run(G, pcd.parse_metric(metric), 0, 1.0, 1, 4, 0.0, init, keep_raw=True, callback=got.append)
+    G.free()
+    _, _, want = oracle.run_schedule(port, g.indices, g.adj, metric, 0, 1.0, 1, 4, 0.0, init)
+    for a, b in zip(got, want):
+        bad = np.nonzero(a.raw != b.raw)[0]
+        assert bad.size == 0, f"sweep {a.it}: {bad.size} vertices differ, first {bad[:6]}"
+
+
+def test_larger_rmat_sweeps_match_oracle(ctx, port):
+    """R-MAT scale 16 (hubs above 8192 neighbours only appear at larger
+    scales; the layouts above cover that class on small graphs)."""
+    import graphs
+    import oracle
+    import pcd
+
+    g = graphs.convert_edges(graphs.rmat(16, 16, 0.57, 0.19, 0.19, seed=9))
+    for metric, strat in (("mod", 0), ("mod", 2), ("cpm-0.02", 2)):
+        G = pcd.Graph.from_csr(ctx, g.indices, g.adj)
+        got = []
+        pcd.run(G, pcd.parse_metric(metric), strat, 1.0, 1, 4, keep_raw=True, callback=got.append)
+        G.free()
+        _, _, want = oracle.run_schedule(port, g.indices, g.adj, metric, strat, 1.0, 1, 4)
+        for a, b in zip(got, want):
+            bad = np.nonzero(a.raw != b.raw)[0]
+            assert bad.size == 0, f"{metric} s{strat} sweep {a.it}: {bad.size} differ"
