@@ -149,3 +149,22 @@ def test_oracle_gains_match_reference_including_int_wrap(port):
             x = ref.gain(kind, rule, lam, lab, a, b, k)
             y = port.gain(kind, rule, lam, lab, a, b, k)
             assert (x == y) or (x != x and y != y), (rule, kind, x, y)
+
+
+@needs_ref
+def test_reference_shipped_flags_match_strict_except_cpm(golden):
+    """The reference compiled with its Makefile flags (-ffast-math
+    -march=native) against the strict-IEEE golden hashes: identical for
+    Modularity and WCC; CPM differs (FMA contraction of k - lambda * size)."""
+    import oracle
+
+    ref = oracle.Reference("shipped")
+    for case in golden["cases"]:
+        g = golden_graph(case["graph"])
+        seen = []
+        oracle.run_schedule(ref, g.indices, g.adj, case["metric"], case["strategy"], case["frac"], case["rounds"],
+                            case["n_iter"], 0.0, case["initial"], callback=lambda sw, lab: seen.append(sha(sw.raw)))
+        same = seen == [s["raw_sha256"] for s in case["sweeps"]]
+        if case["metric"].startswith("cpm"):
+            continue  # contraction-dependent: fast-math may fuse k - lambda * size
+        assert same, (case["graph"], case["metric"], case["strategy"])
