@@ -163,6 +163,23 @@ pcd_status pcd_sweep_info_get(pcd_graph *g, pcd_sweep_info *info);
 pcd_status pcd_profile_enable(pcd_ctx *ctx, int32_t on);
 int32_t pcd_profile_read(pcd_ctx *ctx, const char **names, double *ms, int32_t cap);
 
+/* compress_labels on caller-owned device buffers, with no device allocation.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc where they relabel (inside another framework's memory arena,
+ * allocation-free serving loops, hosts that reserve all device memory up
+ * front).  d_labels_in / d_labels_out: n int32 on the current device, distinct
+ * buffers; labels in [-1, n), -1 = NEW_LABEL (out-of-range values get a fresh
+ * id like NEW_LABEL); *d_num_labels (device) receives the community count.
+ * Scratch is a fixed file-scope device array sized for PCD_NOALLOC_MAX_LABELS
+ * labels (about 8 MiB per GPU, held until the process exits); larger n is
+ * rejected with PCD_ERR_INVALID_ARGUMENT.  The first call on a device, with
+ * that device current, looks up the array's address; make that first call
+ * before any stream capture.  Calls share the array: calls that overlap on the
+ * GPU race.  Asynchronous on `cuda_stream` (NULL = legacy default stream). */
+#define PCD_NOALLOC_MAX_LABELS (1 << 20)
+pcd_status pcd_compress_labels_noalloc(const int32_t *d_labels_in, int32_t n, int32_t *d_labels_out,
+                                       int32_t *d_num_labels, void *cuda_stream);
+
 /* Host-side seed stream: glibc rand() restated (default seed 1 = never
  * srand'ed), so a driver can hand pcd_refine / pcd_merge the same seed the
  * reference draws at src/refinement.cpp:123-124 and :217-218.  Replaces the
