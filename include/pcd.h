@@ -163,6 +163,43 @@ pcd_status pcd_sweep_info_get(pcd_graph *g, pcd_sweep_info *info);
 pcd_status pcd_profile_enable(pcd_ctx *ctx, int32_t on);
 int32_t pcd_profile_read(pcd_ctx *ctx, const char **names, double *ms, int32_t cap);
 
+/* ------------------------------------------------------------------------
+ * Batched path (no counterpart in the reference, which handles one graph per
+ * process).  A batch is many graphs loaded as one packed CSR: graph g owns
+ * vertices [vertex_offsets[g], vertex_offsets[g+1]) (every graph at least one
+ * vertex); indices[N+1] are row offsets into the packed adjacency
+ * (N = vertex_offsets[G]); adj holds each graph's LOCAL neighbour ids.  The
+ * returned handle is a pcd_graph; per-graph results use local labels.  Every
+ * graph gets exactly the labels and scores it gets alone through the
+ * single-graph calls with the same seeds.
+ * ------------------------------------------------------------------------ */
+pcd_status pcd_batch_load(pcd_ctx *ctx, int32_t num_graphs, const int32_t *vertex_offsets,
+                          const int32_t *indices, const int32_t *adj, pcd_graph **out);
+/* Same with indices / adj in device memory (vertex_offsets on the host). */
+pcd_status pcd_batch_load_device(pcd_ctx *ctx, int32_t num_graphs, const int32_t *vertex_offsets,
+                                 const int32_t *d_indices, const int32_t *d_adj, pcd_graph **out);
+pcd_status pcd_batch_num_graphs(pcd_graph *batch, int32_t *num_graphs);
+/* Host arrays of N labels, each graph's labels local to it ([-1, n_g)). */
+pcd_status pcd_batch_labels_set(pcd_graph *batch, const int32_t *labels);
+pcd_status pcd_batch_labels_get(pcd_graph *batch, int32_t *labels);
+/* Per-graph community counts / scores (host arrays of num_graphs). */
+pcd_status pcd_batch_compress(pcd_graph *batch, int32_t *per_graph_k);
+pcd_status pcd_batch_score(pcd_graph *batch, const pcd_rule *rule, double *per_graph);
+/* One sweep / one merge of every graph, with per-graph rand_r seeds. */
+pcd_status pcd_batch_refine(pcd_graph *batch, const pcd_rule *rule, double frac, const uint32_t *seeds);
+pcd_status pcd_batch_merge(pcd_graph *batch, const pcd_rule *rule, int32_t rounds, const uint32_t *seeds);
+/* The reference driver loop (src/main.cpp:199-266, singleton start, -s
+ * strategy, -f frac, -r rounds, -n n_iter or -t threshold when n_iter == -1)
+ * for every graph at once, each graph with its own glibc seed stream and stop
+ * test.  With use_cuda_graph, each propagation iteration of the whole batch is
+ * one captured CUDA graph replay.  Threshold mode stops a graph after 1000
+ * iterations at the latest (the reference's loop never ends for a graph whose
+ * score stays <= 0).  Writes each graph's final score and iteration count
+ * (host arrays, may be NULL). */
+pcd_status pcd_batch_run(pcd_graph *batch, const pcd_rule *rule, int32_t strategy, double frac,
+                         int32_t rounds, int32_t n_iter, double threshold, int32_t use_cuda_graph,
+                         double *scores, int32_t *iterations);
+
 /* compress_labels on caller-owned device buffers, with no device allocation.
  * No counterpart in the reference: it exists for callers that cannot call
  * cudaMalloc where they relabel (inside another framework's memory arena,

@@ -21,7 +21,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpcd.so")
 MAIN = os.path.join(HERE, "main-cuda")
-SOURCES = ["api.cu", "partition.cu", "propagate.cu", "merge.cu", "triangles.cu", "noalloc.cu", "hostside.cpp"]
+SOURCES = ["api.cu", "partition.cu", "propagate.cu", "merge.cu", "triangles.cu", "batch.cu", "noalloc.cu", "hostside.cpp"]
 HEADERS = ["pcd_device.cuh", "pcd_scan.cuh", "pcd_internal.h", "pcd_types.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -80,13 +80,13 @@ void prof_mark(pcd_ctx *ctx, const char *name, cudaStream_t st) {
         if (_s != PCD_OK) return _s;       \
     } while (0)
 
-static pcd_status scan_guard(pcd_graph *g) {
+pcd_status scan_guard(pcd_graph *g) {
     if (!g->scan_overflow) return PCD_OK;
     g->scan_overflow = 0;
     return set_error(g->ctx, PCD_ERR_CUDA, "internal: a device scan exceeded its scratch (nothing was launched)");
 }
 
-static pcd_status sync_and_check(pcd_graph *g) {
+pcd_status sync_and_check(pcd_graph *g) {
     pcd_ctx *ctx = g->ctx;
     TRY(scan_guard(g));
     CK(cudaMemcpyAsync(g->h_ctr, g->ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, ctx->stream),
@@ -108,6 +108,39 @@ static pcd_status sync_and_check(pcd_graph *g) {
     g->info.fallback = g->h_ctr->n_ambiguous;
     g->info.resolved = g->h_ctr->n_resolve;
     g->info.merge_pairs = g->h_ctr->n_pairs;
+    return PCD_OK;
+}
+
+pcd_status ensure_compressed(pcd_graph *g, int *launches) {
+    if (g->compressed) return PCD_OK;
+    if (g->n > 0) *launches += launch_compress(g, g->ctx->stream);
+    g->compressed = true;
+    return check_cuda(g->ctx, cudaGetLastError(), "compress launch");
+}
+
+pcd_status ensure_triangles(pcd_graph *g) {
+    if (g->have_tri) return PCD_OK;
+    pcd_ctx *ctx = g->ctx;
+    const size_t nn = (size_t)std::max(g->n, 1);
+    if (!g->tri) {
+        TRY(dev_alloc(g, (void **)&g->tri, sizeof(int32_t) * nn));
+        TRY(dev_alloc(g, (void **)&g->tri_deg, sizeof(int32_t) * nn));
+    }
+    double cc = 0.0;
+    if (g->n > 0) {
+        launch_triangles(g, ctx->stream);
+        if (!g->batch)
+            CK(cudaMemcpyAsync(&cc, g->d_score, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "triangles");
+    }
+    CK(cudaStreamSynchronize(ctx->stream), "triangles");
+    g->cc = cc;
+    g->have_tri = true;
+    return PCD_OK;
+}
+
+pcd_status check_rule(pcd_graph *g, const pcd_rule *r) {
+    if (!g) return PCD_ERR_INVALID_ARGUMENT;
+    if (!r || r->kind < 0 || r->kind > 2) return set_error(g->ctx, PCD_ERR_INVALID_ARGUMENT, "unknown rule");
     return PCD_OK;
 }
 
@@ -171,6 +204,7 @@ pcd_status pcd_graph_free(pcd_graph *g) {
         if (p) cudaFree(p);
     if (g->merge_buf) cudaFree(g->merge_buf);
     if (g->h_ctr) cudaFreeHost(g->h_ctr);
+    delete g->batch;
     if (ctx) ctx->graphs.erase(std::remove(ctx->graphs.begin(), ctx->graphs.end(), g), ctx->graphs.end());
     delete g;
     return PCD_OK;
@@ -421,12 +455,6 @@ pcd_status pcd_labels_get_device(pcd_graph *g, int32_t *d_labels) {
     return PCD_OK;
 }
 
-static pcd_status ensure_compressed(pcd_graph *g, int *launches) {
-    if (g->compressed) return PCD_OK;
-    if (g->n > 0) *launches += launch_compress(g, g->ctx->stream);
-    g->compressed = true;
-    return check_cuda(g->ctx, cudaGetLastError(), "compress launch");
-}
 
 pcd_status pcd_compress(pcd_graph *g, int32_t *num_labels) {
     if (!g) return PCD_ERR_INVALID_ARGUMENT;
@@ -456,24 +484,6 @@ pcd_status pcd_stats_get(pcd_graph *g, int32_t *sizes, int32_t *int_volume, int3
     return PCD_OK;
 }
 
-static pcd_status ensure_triangles(pcd_graph *g) {
-    if (g->have_tri) return PCD_OK;
-    pcd_ctx *ctx = g->ctx;
-    const size_t nn = (size_t)std::max(g->n, 1);
-    if (!g->tri) {
-        TRY(dev_alloc(g, (void **)&g->tri, sizeof(int32_t) * nn));
-        TRY(dev_alloc(g, (void **)&g->tri_deg, sizeof(int32_t) * nn));
-    }
-    double cc = 0.0;
-    if (g->n > 0) {
-        launch_triangles(g, ctx->stream);
-        CK(cudaMemcpyAsync(&cc, g->d_score, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "triangles");
-    }
-    CK(cudaStreamSynchronize(ctx->stream), "triangles");
-    g->cc = cc;
-    g->have_tri = true;
-    return PCD_OK;
-}
 
 pcd_status pcd_triangles(pcd_graph *g, int32_t *tri, int32_t *tri_deg, double *clustering_coef) {
     if (!g) return PCD_ERR_INVALID_ARGUMENT;
@@ -487,11 +497,6 @@ pcd_status pcd_triangles(pcd_graph *g, int32_t *tri, int32_t *tri_deg, double *c
     return PCD_OK;
 }
 
-static pcd_status check_rule(pcd_graph *g, const pcd_rule *r) {
-    if (!g) return PCD_ERR_INVALID_ARGUMENT;
-    if (!r || r->kind < 0 || r->kind > 2) return set_error(g->ctx, PCD_ERR_INVALID_ARGUMENT, "unknown rule");
-    return PCD_OK;
-}
 
 pcd_status pcd_score(pcd_graph *g, const pcd_rule *rule, double *out) {
     TRY(check_rule(g, rule));

@@ -232,6 +232,8 @@ struct MergeArgs {
     TieRecord *recs;
     DevCounters *ctr;
     int32_t k;
+    const int32_t *cgid;   // batch: graph of each community (else null)
+    const int32_t *gdone;  // batch: graphs whose schedule has ended
 };
 
 template <class R>
@@ -244,7 +246,8 @@ __global__ void __launch_bounds__(256) k_merge_analyze(MergeArgs a, R rule) {
     for (int64_t li = gw; li < a.k; li += nw) {
         const int32_t l = (int32_t)li;
         const int32_t bp = a.best[l];
-        const bool active = !a.found[l] && (bp == -1 || a.found[bp]);
+        const bool active = !a.found[l] && (bp == -1 || a.found[bp]) && !(a.gdone && a.gdone[a.cgid[l]]);
+        const R vr = rule.at_comm(l);
         if (!active) {
             if (lane == 0) a.ndraw[l] = 0;
             continue;
@@ -266,7 +269,7 @@ __global__ void __launch_bounds__(256) k_merge_analyze(MergeArgs a, R rule) {
                 w = a.cw[i];
                 sc = !a.found[c];
                 if (sc) {
-                    key = rule.merge(l, c, w, a.cm);
+                    key = vr.merge(l, c, w, a.cm);
                     if (key != key) {  // NaN: neither ties nor wins
                         sc = false;
                         key = ident;
@@ -315,6 +318,13 @@ struct CommDrawStore {
 };
 
 __global__ void k_round_advance(DevCounters *ctr, const uint32_t *total) { ctr->total_draws += *total; }
+
+// Batch: each graph's draws this round (its communities' span of the scan).
+__global__ void k_round_advance_graphs(const int32_t *gK, int32_t G, const uint32_t *endpos, const uint32_t *gbase,
+                                       uint32_t *gtotal) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < G; g += (int64_t)gridDim.x * blockDim.x)
+        if (gK[g + 1] > gK[g]) gtotal[g] += endpos[gK[g + 1] - 1] - gbase[g];
+}
 
 __global__ void k_found(const int32_t *__restrict__ best, int32_t *found, int32_t k) {
     for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < k; l += (int64_t)gridDim.x * blockDim.x) {
@@ -492,7 +502,17 @@ static void merge_rounds(pcd_graph *g, const MergeArgs &ma, const R &rule, int32
         k_merge_analyze<R><<<wgrid, 256, 0, st>>>(ma, rule);
         *launches += 2;
         *launches += scan_exclusive(CommDrawLoad{ma.ndraw}, CommDrawStore{ma.ndraw}, k, g->scan, st);
-        launch_resolve(ma.recs, g->ctr, ma.ndraw, &g->ctr->total_draws, ma.tiebuf, ma.best, seed, 1, sms * 4, st);
+        BatchState *B = g->batch;
+        if (B) {
+            launch_graph_base(B->gK, B->G, ma.ndraw, B->gbase, st);
+            launch_resolve(ma.recs, g->ctr, ma.ndraw, nullptr, ma.tiebuf, ma.best, seed, 1, sms * 4, st, B->cgid,
+                           B->gseed, B->gbase, B->gtotal);
+            k_round_advance_graphs<<<(B->G + 255) / 256, 256, 0, st>>>(B->gK, B->G, ma.ndraw, B->gbase, B->gtotal);
+            *launches += 3;
+        } else {
+            launch_resolve(ma.recs, g->ctr, ma.ndraw, &g->ctr->total_draws, ma.tiebuf, ma.best, seed, 1, sms * 4,
+                           st);
+        }
         k_round_advance<<<1, 1, 0, st>>>(g->ctr, g->scan_total);
         k_found<<<grid_n(k, sms), 256, 0, st>>>(ma.best, ma.found, (int32_t)k);
         *launches += 3;
@@ -537,17 +557,25 @@ pcd_status run_merge(pcd_graph *g, int32_t kind, double lambda, int32_t rounds, 
     ma.recs = g->recs;
     ma.ctr = g->ctr;
     ma.k = k;
+    BatchState *B = g->batch;
+    ma.cgid = B ? B->cgid : nullptr;
+    ma.gdone = B ? B->gdone : nullptr;
+    const BatchView bv = B ? BatchView{B->vgid, B->cgid, B->gm, B->gcc} : BatchView{};
+    if (B) cudaMemsetAsync(B->gtotal, 0, sizeof(uint32_t) * B->G, st);
     if (kind == PCD_RULE_MODULARITY) {
         RuleModF64 r;
         r.m = g->m;
+        r.bv = bv;
         merge_rounds(g, ma, r, rounds, seed, st, launches);
     } else if (kind == PCD_RULE_CPM) {
         RuleCPM r;
         r.lambda = lambda;
+        r.bv = bv;
         merge_rounds(g, ma, r, rounds, seed, st, launches);
     } else {
         RuleWCC r;
         r.cc = g->cc;
+        r.bv = bv;
         merge_rounds(g, ma, r, rounds, seed, st, launches);
     }
     k_merge_relabel<<<grid_n(g->n, sms), 256, 0, st>>>(g->labels, mb.best, mb.found, g->n, g->labels_alt);

@@ -174,6 +174,17 @@ int launch_stats(pcd_graph *g, cudaStream_t st) {
     return launches;
 }
 
+// Batch: community -> graph, and the first community of each graph (the label
+// of its first vertex: compress numbers communities by first occurrence).
+__global__ void k_batch_comm(const int32_t *__restrict__ labels, const int32_t *__restrict__ vgid,
+                             const int32_t *__restrict__ voff, int32_t G, int32_t n, int32_t *cgid, int32_t *gK,
+                             const DevCounters *ctr) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        cgid[labels[v]] = vgid[v];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i <= G; i += (int64_t)gridDim.x * blockDim.x)
+        gK[i] = i < G ? labels[voff[i]] : ctr->k;
+}
+
 int launch_compress(pcd_graph *g, cudaStream_t st) {
     int launches = 0;
     const int32_t n = g->n;
@@ -184,6 +195,11 @@ int launch_compress(pcd_graph *g, cudaStream_t st) {
     k_relabel<<<grid_for(n, 256), 256, 0, st>>>(g->labels, g->labels_alt, g->first, n);
     k_set_k<<<1, 1, 0, st>>>(g->ctr, g->scan_total);
     launches += 2;
+    if (g->batch) {
+        k_batch_comm<<<grid_for(n, 256), 256, 0, st>>>(g->labels, g->batch->vgid, g->batch->voff, g->batch->G, n,
+                                                        g->batch->cgid, g->batch->gK, g->ctr);
+        ++launches;
+    }
     launches += launch_stats(g, st);
     return launches;
 }
@@ -212,17 +228,24 @@ __device__ __forceinline__ DD dd_add(DD a, DD b) {
     return dd_add(r, b.lo);
 }
 
-constexpr int SCORE_BLOCKS = 256;
-constexpr int SCORE_THREADS = 256;
+// One block per graph: thread j adds terms j, j + 1024, ... in order in
+// double-double, then a fixed tree.  The same kernel scores a single graph
+// (G = 1) and every graph of a batch, so a graph gets the same score either way.
+// Community range of graph g: [gK[g], gK[g + 1]) (a single graph: [0, k)).
+constexpr int SCORE_THREADS = 1024;
 
-__global__ void __launch_bounds__(SCORE_THREADS) k_score_terms(int32_t kind, double lambda, int32_t m,
+__global__ void __launch_bounds__(SCORE_THREADS) k_score_graph(int32_t kind, double lambda, int32_t m_single,
+                                                              const int32_t *__restrict__ gm,
+                                                              const int32_t *__restrict__ gK,
                                                               const int32_t *__restrict__ sizes,
                                                               const int32_t *__restrict__ intv,
                                                               const int32_t *__restrict__ vol,
-                                                              const DevCounters *ctr, DD *partial) {
-    const int32_t k = ctr->k;
+                                                              const DevCounters *ctr, double *out) {
+    const int g = blockIdx.x;
+    const int32_t c0 = gK ? gK[g] : 0, c1 = gK ? gK[g + 1] : ctr->k;
+    const int32_t m = gm ? gm[g] : m_single;
     DD acc{0.0, 0.0};
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < k; i += (int64_t)gridDim.x * blockDim.x) {
+    for (int32_t i = c0 + threadIdx.x; i < c1; i += SCORE_THREADS) {
         double t;
         if (kind == 0) {
             double actual = intv[i] / (2.0 * m);
@@ -241,24 +264,19 @@ __global__ void __launch_bounds__(SCORE_THREADS) k_score_terms(int32_t kind, dou
         if ((int)threadIdx.x < s) sh[threadIdx.x] = dd_add(sh[threadIdx.x], sh[threadIdx.x + s]);
         __syncthreads();
     }
-    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
-}
-
-__global__ void k_score_final(int32_t kind, int32_t m, const DD *partial, int nparts, double *out) {
-    if (threadIdx.x != 0) return;
-    DD acc{0.0, 0.0};
-    for (int i = 0; i < nparts; ++i) acc = dd_add(acc, partial[i]);
-    double s = acc.hi + acc.lo;
-    if (kind == 1) s = s / (double)(2 * m);
-    *out = s;
+    if (threadIdx.x == 0) {
+        double s = sh[0].hi + sh[0].lo;
+        if (kind == 1) s = s / (double)(2 * m);
+        out[g] = s;
+    }
 }
 
 int launch_score(pcd_graph *g, int32_t kind, double lambda, double *d_out, cudaStream_t st) {
-    DD *partial = reinterpret_cast<DD *>(g->small);
-    k_score_terms<<<SCORE_BLOCKS, SCORE_THREADS, 0, st>>>(kind, lambda, g->m, g->sizes, g->intv, g->vol, g->ctr,
-                                                           partial);
-    k_score_final<<<1, 32, 0, st>>>(kind, g->m, partial, SCORE_BLOCKS, d_out);
-    return 2;
+    BatchState *B = g->batch;
+    k_score_graph<<<B ? B->G : 1, SCORE_THREADS, 0, st>>>(kind, lambda, g->m, B ? B->gm : nullptr,
+                                                         B ? B->gK : nullptr, g->sizes, g->intv, g->vol, g->ctr,
+                                                         B ? B->gscore : d_out);
+    return 1;
 }
 
 // ---------------------------------------------------------------------------

@@ -133,6 +133,15 @@ static __device__ __noinline__ double wcc_improvement(int32_t n_x, int32_t n_y, 
     return score;
 }
 
+// Per-graph parameters when many graphs are refined as one disjoint union
+// (the batched path).  All pointers are null for a single graph.
+struct BatchView {
+    const int32_t *__restrict__ vgid;  // graph of each vertex
+    const int32_t *__restrict__ cgid;  // graph of each community
+    const int32_t *__restrict__ gm;    // edges of each graph
+    const double *__restrict__ gcc;    // clustering coefficient of each graph (WCC)
+};
+
 // ---------------------------------------------------------------------------
 // Rules.  Each rule defines a scan Key and its order, the join gain of a
 // candidate (vertex v of degree d, community c, k neighbours in c) and the
@@ -151,6 +160,19 @@ template <class Derived>
 struct RuleF64Base {
     using Key = double;
     static constexpr bool kExactInt = false;
+    BatchView bv{};
+    // the rule as seen by vertex v / community c (batched: that graph's parameters)
+    __device__ Derived at(int32_t v) const {
+        Derived r = *static_cast<const Derived *>(this);
+        if (bv.vgid) r.set_graph(bv.vgid[v]);
+        return r;
+    }
+    __device__ Derived at_comm(int32_t c) const {
+        Derived r = *static_cast<const Derived *>(this);
+        if (bv.cgid) r.set_graph(bv.cgid[c]);
+        return r;
+    }
+    __device__ void set_graph(int32_t) {}
     __device__ static Key identity() { return -__longlong_as_double(0x7ff0000000000000LL); }
     __device__ static Key initial() { return 0.0; }
     __device__ static bool gt(Key a, Key b) { return a > b; }
@@ -176,6 +198,7 @@ struct RuleF64Base {
 // ModularityRule, src/rules.cpp:24-56.
 struct RuleModF64 : RuleF64Base<RuleModF64> {
     int32_t m;
+    __device__ void set_graph(int32_t g) { m = bv.gm[g]; }
     __device__ Key join(int32_t, int32_t d, int32_t c, int32_t k, const CommView &cm, Tag &) const {
         double e_ij = k / (double)m;
         double a_i = cm.vol[c] / (2.0 * m);
@@ -213,6 +236,7 @@ struct RuleCPM : RuleF64Base<RuleCPM> {
 // WCCRule, src/rules.cpp:391-436.
 struct RuleWCC : RuleF64Base<RuleWCC> {
     double cc;
+    __device__ void set_graph(int32_t g) { cc = bv.gcc[g]; }
     __device__ Key join(int32_t, int32_t d, int32_t c, int32_t k, const CommView &cm, Tag &) const {
         return wcc_improvement(1, cm.size[c], 1, k, 0, cm.intv[c] / 2, k, d, cm.extv[c], cc);
     }
@@ -245,6 +269,15 @@ struct RuleModInt {
     static constexpr bool kExactInt = true;
     int32_t m;
     long long two_m;
+    BatchView bv{};
+    __device__ RuleModInt at(int32_t v) const {
+        RuleModInt r = *this;
+        if (bv.vgid) {
+            r.m = bv.gm[bv.vgid[v]];
+            r.two_m = 2LL * r.m;
+        }
+        return r;
+    }
     __device__ static Key identity() { return LLONG_MIN; }
     __device__ static Key initial() { return 0; }
     __device__ static bool gt(Key a, Key b) { return a > b; }

@@ -27,8 +27,34 @@ struct pcd_ctx {
     size_t prof_used = 0;
 };
 
+// Per-graph state of a batch: many graphs refined as one disjoint union whose
+// vertices (and, after compress, communities) are grouped graph by graph.
+struct BatchState {
+    int32_t G = 0;
+    std::vector<int32_t> h_voff;   // vertex offsets (G + 1)
+    std::vector<int32_t> h_m;      // edges per graph
+    int32_t *voff = nullptr;       // device copy of h_voff
+    int32_t *vgid = nullptr;       // graph of each vertex
+    int32_t *cgid = nullptr;       // graph of each community (after compress)
+    int32_t *gK = nullptr;         // first community of each graph, gK[G] = k (after compress)
+    int32_t *gm = nullptr;         // edges per graph
+    double *gcc = nullptr;         // clustering coefficient per graph (WCC)
+    uint32_t *gseed = nullptr;     // rand_r seed of each graph for the current call
+    uint32_t *gbase = nullptr;     // each graph's offset in the scanned draw stream
+    uint32_t *gtotal = nullptr;    // merge: draws of earlier rounds, per graph
+    int32_t *gdone = nullptr;      // graph finished its schedule (labels frozen)
+    double *gscore = nullptr, *gprev = nullptr;
+    double *tile_part = nullptr;   // per-tile partial sums of the score (2 doubles each)
+    int64_t tile_cap = 0;
+    int32_t *gtile = nullptr;      // first score tile of each graph (G + 1)
+    int32_t *iter = nullptr;       // device iteration counter (captured runs)
+    uint32_t *seed_table = nullptr;  // [iters][G] seeds for captured runs
+    int32_t seed_iters = 0;
+};
+
 struct pcd_graph {
     pcd_ctx *ctx = nullptr;
+    BatchState *batch = nullptr;   // non-null for a batch (see pcd_batch_* in pcd.h)
     int32_t n = 0, m = 0;
     int64_t nnz = 0;  // 2m
     int32_t max_deg = 0;
@@ -76,6 +102,7 @@ struct pcd_graph {
     // bookkeeping
     int32_t k = 0;           // communities (valid when compressed)
     bool compressed = false; // labels renumbered and statistics current
+    bool labels_vertex_space = false;  // batch: labels still hold vertex ids (set, not compressed)
     pcd_sweep_info info{};
     std::vector<void *> allocs;
 };
@@ -100,7 +127,10 @@ int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32
                   cudaStream_t st);
 void launch_resolve(const TieRecord *recs, const DevCounters *ctr, const uint32_t *endpos, const uint32_t *base,
                     const int32_t *tiebuf, int32_t *out, uint32_t seed, int32_t mod_base, int grid,
-                    cudaStream_t st);
+                    cudaStream_t st, const int32_t *ugid = nullptr, const uint32_t *gseed = nullptr,
+                    const uint32_t *gbase = nullptr, const uint32_t *gextra = nullptr);
+void launch_graph_base(const int32_t *first_unit, int32_t G, const uint32_t *endpos, uint32_t *gbase,
+                       cudaStream_t st);
 
 // merge.cu
 pcd_status run_merge(pcd_graph *g, int32_t kind, double lambda, int32_t rounds, uint32_t seed,
@@ -111,6 +141,17 @@ pcd_status run_contract(pcd_graph *g, int64_t cap, int32_t *a, int32_t *b, int32
 // triangles.cu
 int launch_triangles(pcd_graph *g, cudaStream_t st);
 int launch_wcc_score(pcd_graph *g, double *d_out, cudaStream_t st);
+
+}  // namespace pcd
+
+// api.cu helpers shared with batch.cu
+pcd_status scan_guard(pcd_graph *g);
+pcd_status sync_and_check(pcd_graph *g);
+pcd_status ensure_compressed(pcd_graph *g, int *launches);
+pcd_status ensure_triangles(pcd_graph *g);
+pcd_status check_rule(pcd_graph *g, const pcd_rule *r);
+
+namespace pcd {
 
 // jump table upload (propagate.cu)
 void upload_jump_table(cudaStream_t st);

@@ -153,6 +153,7 @@ __global__ void __launch_bounds__(256) k_prop_group(SweepArgs a, R rule, const i
         const int32_t b = has_v ? a.g.indices[v] : 0;
         const int32_t d = has_v ? a.g.indices[v + 1] - b : 0;
         const int32_t curr = has_v ? a.labels[v] : -1;
+        const R vr = has_v ? rule.at(v) : rule;
         const bool valid = gl < d;
         const int32_t lab = valid ? a.labels[a.g.adj[b + gl]] : -1;
         const unsigned long long mk =
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(256) k_prop_group(SweepArgs a, R rule, const i
         Tag tag{0, 0};
         Key key = R::identity();
         if (sc) {
-            key = rule.join(v, d, lab, k, a.cm, tag);
+            key = vr.join(v, d, lab, k, a.cm, tag);
             if (!R::usable(key)) {
                 sc = false;
                 key = R::identity();
@@ -194,8 +195,8 @@ __global__ void __launch_bounds__(256) k_prop_group(SweepArgs a, R rule, const i
         const int32_t r = __popc(rm);
         int32_t dec = DEC_STAY;
         if (has_v) {
-            amb |= rule.vertex_ambiguous(d);
-            if (!amb) dec = rule.decide(fin.key, fin.ord >= 0, v, d, curr, curr_freq, a.cm);
+            amb |= vr.vertex_ambiguous(d);
+            if (!amb) dec = vr.decide(fin.key, fin.ord >= 0, v, d, curr, curr_freq, a.cm);
             if (dec == DEC_AMBIGUOUS) amb = true;
         }
         const bool leader = has_v && gl == 0;
@@ -243,7 +244,8 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
         const int32_t v = list[idx];
         const int32_t b = a.g.indices[v], e = a.g.indices[v + 1], d = e - b;
         const int32_t curr = a.labels[v];
-        if (rule.vertex_ambiguous(d)) {
+        const R vr = rule.at(v);
+        if (vr.vertex_ambiguous(d)) {
             if (lane == 0) push_ambiguous(a, v);
             continue;
         }
@@ -305,7 +307,7 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
             Tag tag{0, 0};
             Key key = R::identity();
             if (sc) {
-                key = rule.join(v, d, l, k, a.cm, tag);
+                key = vr.join(v, d, l, k, a.cm, tag);
                 if (!R::usable(key)) {
                     sc = false;
                     key = R::identity();
@@ -341,7 +343,7 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
         const int32_t curr_freq = __reduce_add_sync(FULL, my_curr);
         const bool has = carry.ord >= 0;
         const int32_t holder = has ? clab[carry.ord] : -1;
-        int32_t dec = amb ? DEC_AMBIGUOUS : rule.decide(carry.key, has, v, d, curr, curr_freq, a.cm);
+        int32_t dec = amb ? DEC_AMBIGUOUS : vr.decide(carry.key, has, v, d, curr, curr_freq, a.cm);
         if (dec == DEC_AMBIGUOUS) {
             if (lane == 0) push_ambiguous(a, v);
             continue;
@@ -428,7 +430,8 @@ __global__ void __launch_bounds__(BT) k_prop_block(SweepArgs a, R rule, const in
         const int32_t v = list[vi];
         const int32_t b = a.g.indices[v], e = a.g.indices[v + 1], d = e - b;
         const int32_t curr = a.labels[v];
-        if (rule.vertex_ambiguous(d)) {
+        const R vr = rule.at(v);
+        if (vr.vertex_ambiguous(d)) {
             if (tid == 0) push_ambiguous(a, v);
             continue;
         }
@@ -520,7 +523,7 @@ __global__ void __launch_bounds__(BT) k_prop_block(SweepArgs a, R rule, const in
                     tag[u] = Tag{0, 0};
                     key[u] = R::identity();
                     if (sc[u]) {
-                        key[u] = rule.join(v, d, l[u], k, a.cm, tag[u]);
+                        key[u] = vr.join(v, d, l[u], k, a.cm, tag[u]);
                         if (!R::usable(key[u])) {
                             sc[u] = false;
                             key[u] = R::identity();
@@ -606,7 +609,7 @@ __global__ void __launch_bounds__(BT) k_prop_block(SweepArgs a, R rule, const in
                     tag[u] = Tag{0, 0};
                     key[u] = R::identity();
                     if (sc[u]) {
-                        key[u] = rule.join(v, d, l[u], k, a.cm, tag[u]);
+                        key[u] = vr.join(v, d, l[u], k, a.cm, tag[u]);
                         if (!R::usable(key[u])) {
                             sc[u] = false;
                             key[u] = R::identity();
@@ -659,7 +662,7 @@ __global__ void __launch_bounds__(BT) k_prop_block(SweepArgs a, R rule, const in
             }
             s.r = r;
             s.off = -1;
-            const int32_t dec = s.amb ? DEC_AMBIGUOUS : rule.decide(c.key, c.ord >= 0, v, d, curr, s.curr_freq, a.cm);
+            const int32_t dec = s.amb ? DEC_AMBIGUOUS : vr.decide(c.key, c.ord >= 0, v, d, curr, s.curr_freq, a.cm);
             if (dec == DEC_AMBIGUOUS) {
                 push_ambiguous(a, v);
             } else {
@@ -705,7 +708,8 @@ __global__ void __launch_bounds__(512) k_prop_hub(SweepArgs a, R rule, const int
         const int32_t v = list[vi];
         const int32_t b = a.g.indices[v], e = a.g.indices[v + 1], d = e - b;
         const int32_t curr = a.labels[v];
-        if (rule.vertex_ambiguous(d)) {
+        const R vr = rule.at(v);
+        if (vr.vertex_ambiguous(d)) {
             if (tid == 0) push_ambiguous(a, v);
             continue;
         }
@@ -790,7 +794,7 @@ __global__ void __launch_bounds__(512) k_prop_hub(SweepArgs a, R rule, const int
                     tag[u] = Tag{0, 0};
                     key[u] = R::identity();
                     if (sc[u]) {
-                        key[u] = rule.join(v, d, l[u], k[u], a.cm, tag[u]);
+                        key[u] = vr.join(v, d, l[u], k[u], a.cm, tag[u]);
                         if (!R::usable(key[u])) {
                             sc[u] = false;
                             key[u] = R::identity();
@@ -867,7 +871,7 @@ __global__ void __launch_bounds__(512) k_prop_hub(SweepArgs a, R rule, const int
                     tag[u] = Tag{0, 0};
                     key[u] = R::identity();
                     if (sc[u]) {
-                        key[u] = rule.join(v, d, l[u], k[u], a.cm, tag[u]);
+                        key[u] = vr.join(v, d, l[u], k[u], a.cm, tag[u]);
                         if (!R::usable(key[u])) {
                             sc[u] = false;
                             key[u] = R::identity();
@@ -919,7 +923,7 @@ __global__ void __launch_bounds__(512) k_prop_hub(SweepArgs a, R rule, const int
             }
             s.r = r;
             s.off = -1;
-            const int32_t dec = s.amb ? DEC_AMBIGUOUS : rule.decide(c.key, c.ord >= 0, v, d, curr, s.curr_freq, a.cm);
+            const int32_t dec = s.amb ? DEC_AMBIGUOUS : vr.decide(c.key, c.ord >= 0, v, d, curr, s.curr_freq, a.cm);
             if (dec == DEC_AMBIGUOUS) {
                 push_ambiguous(a, v);
             } else {
@@ -955,47 +959,77 @@ struct DrawStore {
 __global__ void k_total_draws(DevCounters *ctr, const uint32_t *total) { ctr->total_draws = *total; }
 
 // frac < 1: whether v draws its ties depends on its frac draw, which depends
-// on every earlier vertex's draw count, so one thread walks the stream in
-// vertex order (src/refinement.cpp:127-132 with one thread).
-__global__ void k_walk(uint32_t seed, int32_t f, int32_t n, uint32_t *ndraw, const int32_t *__restrict__ labels,
-                       int32_t *new_labels, int32_t *skip, DevCounters *ctr) {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    uint32_t x = seed, pos = 0;
-    for (int32_t v = 0; v < n; ++v) {
-        int32_t val = rand_r_dev(x);
-        pos += 1;
-        uint32_t t = ndraw[v];
-        if (val > f) {
-            skip[v] = 1;
-            new_labels[v] = labels[v];
-        } else {
-            skip[v] = 0;
-            if (t < 8) {
-                for (uint32_t j = 0; j < t; ++j) (void)rand_r_dev(x);
+// on every earlier vertex's draw count, so one thread per graph walks that
+// graph's stream in vertex order (src/refinement.cpp:127-132 with one thread).
+// voff null: one graph [0, n) with `seed`; else graph g = [voff[g], voff[g+1])
+// with gseed[g].  Writes each vertex's end position relative to its graph.
+__global__ void k_walk(uint32_t seed, const uint32_t *gseed, const int32_t *voff, int32_t G, int32_t f, int32_t n,
+                       uint32_t *ndraw, const int32_t *__restrict__ labels, int32_t *new_labels, int32_t *skip,
+                       DevCounters *ctr) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < G; g += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t v0 = voff ? voff[g] : 0, v1 = voff ? voff[g + 1] : n;
+        uint32_t x = voff ? gseed[g] : seed, pos = 0;
+        for (int32_t v = v0; v < v1; ++v) {
+            int32_t val = rand_r_dev(x);
+            pos += 1;
+            uint32_t t = ndraw[v];
+            if (val > f) {
+                skip[v] = 1;
+                new_labels[v] = labels[v];
             } else {
-                x = rand_r_jump(x, t);
+                skip[v] = 0;
+                if (t < 8) {
+                    for (uint32_t j = 0; j < t; ++j) (void)rand_r_dev(x);
+                } else {
+                    x = rand_r_jump(x, t);
+                }
+                pos += t;
             }
-            pos += t;
+            ndraw[v] = pos;
         }
-        ndraw[v] = pos;
+        if (!voff) ctr->total_draws = pos;
     }
-    ctr->total_draws = pos;
+}
+
+// Each graph's offset in the scanned stream: the end position of the unit
+// before its first one (units are vertices, or communities for merging).
+__global__ void k_graph_base(const int32_t *first_unit, int32_t G, const uint32_t *endpos, uint32_t *gbase) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < G; g += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t u = first_unit[g];
+        gbase[g] = u > 0 ? endpos[u - 1] : 0u;
+    }
+}
+
+// Graphs whose schedule has ended keep their labels.
+__global__ void k_done_fixup(const int32_t *__restrict__ vgid, const int32_t *__restrict__ gdone,
+                             const int32_t *__restrict__ labels, int32_t *new_labels, int32_t n) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        if (gdone[vgid[v]]) new_labels[v] = labels[v];
 }
 
 // Replay the final level of ties of each recorded vertex/community: the j-th
 // tie (0-based) replaces the holder when rand_r % (j + mod_base) == 0.
 // Propagation: mod_base 2 (src/refinement.cpp:159, ++best_count from 1);
 // merging: mod_base 1 (src/refinement.cpp:250, count++ from 1).
+// Batched: ugid maps a unit to its graph, whose seed is gseed[g] and whose
+// positions are endpos - gbase[g] (+ gextra[g], merge rounds already drawn).
 __global__ void k_resolve(const TieRecord *__restrict__ recs, const DevCounters *ctr,
                           const uint32_t *__restrict__ endpos, const uint32_t *base,
                           const int32_t *__restrict__ tiebuf, int32_t *out, uint32_t seed, int32_t mod_base,
-                          const int32_t *skip) {
+                          const int32_t *skip, const int32_t *__restrict__ ugid, const uint32_t *__restrict__ gseed,
+                          const uint32_t *__restrict__ gbase, const uint32_t *__restrict__ gextra) {
     const int32_t nrec = ctr->n_resolve;
     const uint32_t b0 = base ? *base : 0u;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nrec; i += (int64_t)gridDim.x * blockDim.x) {
         const TieRecord rec = recs[i];
         if (skip && skip[rec.v]) continue;
-        uint32_t x = rand_r_jump(seed, b0 + endpos[rec.v] - (uint32_t)rec.r);
+        uint32_t sd = seed, bb = b0;
+        if (ugid) {
+            const int32_t g = ugid[rec.v];
+            sd = gseed[g];
+            bb = (gextra ? gextra[g] : 0u) - gbase[g];
+        }
+        uint32_t x = rand_r_jump(sd, bb + endpos[rec.v] - (uint32_t)rec.r);
         int32_t best = tiebuf[rec.off];
         for (int32_t j = 0; j < rec.r; ++j) {
             int32_t val = rand_r_dev(x);
@@ -1088,6 +1122,8 @@ void propagate_configure(pcd_ctx *) {}
 
 int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32_t seed, cudaStream_t st) {
     int launches = 0;
+    BatchState *B = g->batch;
+    const BatchView bv = B ? BatchView{B->vgid, B->cgid, B->gm, B->gcc} : BatchView{};
     SweepArgs a;
     a.g = GraphView{g->n, g->m, g->indices, g->adj, g->tri, g->tri_deg, g->cc};
     a.cm = CommView{g->sizes, g->intv, g->extv, g->vol};
@@ -1106,9 +1142,11 @@ int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32
         RuleModInt r;
         r.m = g->m;
         r.two_m = 2LL * g->m;
+        r.bv = bv;
         launches += launch_bins_rule(g, a, r, st);
         RuleModF64 rf;
         rf.m = g->m;
+        rf.bv = bv;
         k_prop_block<RuleModF64, true, 512, 2><<<g->fb_blocks, 512, 0, st>>>(
             a, rf, g->amb, 0, &g->ctr->n_ambiguous, (int32_t)g->fb_slots, g->fb_scratch,
             3 * g->fb_slots + g->max_deg, nullptr);
@@ -1117,10 +1155,12 @@ int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32
     } else if (kind == PCD_RULE_CPM) {
         RuleCPM r;
         r.lambda = lambda;
+        r.bv = bv;
         launches += launch_bins_rule(g, a, r, st);
     } else {
         RuleWCC r;
         r.cc = g->cc;
+        r.bv = bv;
         launches += launch_bins_rule(g, a, r, st);
     }
     const int32_t f = (int32_t)((frac < 1.0 ? frac : 1.0) * 2147483647.0);
@@ -1129,24 +1169,43 @@ int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32
         launches += scan_exclusive(DrawLoad{g->ndraw}, DrawStore{g->ndraw}, g->n, g->scan, st);
         k_total_draws<<<1, 1, 0, st>>>(g->ctr, g->scan_total);
         ++launches;
+        if (B) {
+            launch_graph_base(B->voff, B->G, g->ndraw, B->gbase, st);
+            ++launches;
+        }
         prof_mark(g->ctx, "sweep.draw_scan", st);
     } else {
-        k_walk<<<1, 1, 0, st>>>(seed, f, g->n, g->ndraw, g->labels, g->labels_alt, g->first, g->ctr);
+        const int32_t G = B ? B->G : 1;
+        k_walk<<<(G + 127) / 128, 128, 0, st>>>(seed, B ? B->gseed : nullptr, B ? B->voff : nullptr, G, f, g->n,
+                                                g->ndraw, g->labels, g->labels_alt, g->first, g->ctr);
+        if (B) cudaMemsetAsync(B->gbase, 0, sizeof(uint32_t) * B->G, st);
         skip = g->first;
         ++launches;
         prof_mark(g->ctx, "sweep.draw_walk", st);
     }
     k_resolve<<<g->ctx->num_sms * 4, 256, 0, st>>>(g->recs, g->ctr, g->ndraw, nullptr, g->tiebuf, g->labels_alt,
-                                                  seed, 2, skip);
+                                                  seed, 2, skip, B ? B->vgid : nullptr, B ? B->gseed : nullptr,
+                                                  B ? B->gbase : nullptr, nullptr);
     ++launches;
+    if (B) {
+        k_done_fixup<<<g->ctx->num_sms * 8, 256, 0, st>>>(B->vgid, B->gdone, g->labels, g->labels_alt, g->n);
+        ++launches;
+    }
     prof_mark(g->ctx, "sweep.resolve", st);
     return launches;
 }
 
 void launch_resolve(const TieRecord *recs, const DevCounters *ctr, const uint32_t *endpos, const uint32_t *base,
                     const int32_t *tiebuf, int32_t *out, uint32_t seed, int32_t mod_base, int grid,
-                    cudaStream_t st) {
-    k_resolve<<<grid, 256, 0, st>>>(recs, ctr, endpos, base, tiebuf, out, seed, mod_base, nullptr);
+                    cudaStream_t st, const int32_t *ugid, const uint32_t *gseed, const uint32_t *gbase,
+                    const uint32_t *gextra) {
+    k_resolve<<<grid, 256, 0, st>>>(recs, ctr, endpos, base, tiebuf, out, seed, mod_base, nullptr, ugid, gseed, gbase,
+                                    gextra);
+}
+
+void launch_graph_base(const int32_t *first_unit, int32_t G, const uint32_t *endpos, uint32_t *gbase,
+                       cudaStream_t st) {
+    k_graph_base<<<(G + 255) / 256, 256, 0, st>>>(first_unit, G, endpos, gbase);
 }
 
 }  // namespace pcd

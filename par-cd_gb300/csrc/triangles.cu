@@ -75,20 +75,25 @@ __global__ void k_triangles(const int32_t *__restrict__ indices, const int32_t *
 }
 
 // clustering_coef = sum over v of (tri / (deg (deg - 1.0))) / n, in vertex
-// order (src/graph.cpp:491-499 with one thread).  Lanes compute the terms;
-// lane 0 adds them in order.
+// order (src/graph.cpp:491-499 with one thread).  One warp per graph (voff
+// null: one graph [0, n)); lanes compute the terms, every lane adds them in
+// order, lane 0 writes.
 __global__ void k_clustering_coef(const int32_t *__restrict__ indices, const int32_t *__restrict__ tri, int32_t n,
-                                  double *out) {
+                                  const int32_t *__restrict__ voff, int32_t G, double *out) {
     const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (warp >= G) return;
+    const int32_t v0 = voff ? voff[warp] : 0, v1 = voff ? voff[warp + 1] : n;
+    const int32_t ng = v1 - v0;
     double cc = 0;
-    for (int32_t base = 0; base < n; base += 32) {
+    for (int32_t base = v0; base < v1; base += 32) {
         const int32_t v = base + lane;
         double term = 0.0;
         bool has = false;
-        if (v < n) {
+        if (v < v1) {
             int32_t deg = indices[v + 1] - indices[v];
             if (deg > 1) {
-                term = (tri[v] / (deg * (deg - 1.0))) / n;
+                term = (tri[v] / (deg * (deg - 1.0))) / ng;
                 has = true;
             }
         }
@@ -98,7 +103,7 @@ __global__ void k_clustering_coef(const int32_t *__restrict__ indices, const int
             if ((hm >> i) & 1u) cc += x;
         }
     }
-    if (lane == 0) *out = cc;
+    if (lane == 0) out[warp] = cc;
 }
 
 int launch_triangles(pcd_graph *g, cudaStream_t st) {
@@ -110,7 +115,11 @@ int launch_triangles(pcd_graph *g, cudaStream_t st) {
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
     k_triangles<<<blocks, 256, 0, st>>>(g->indices, g->adj, g->n, nullptr, g->tri, g->tri_deg);
-    k_clustering_coef<<<1, 32, 0, st>>>(g->indices, g->tri, g->n, g->d_score);
+    if (g->batch)
+        k_clustering_coef<<<(g->batch->G + 7) / 8, 256, 0, st>>>(g->indices, g->tri, g->n, g->batch->voff,
+                                                                  g->batch->G, g->batch->gcc);
+    else
+        k_clustering_coef<<<1, 32, 0, st>>>(g->indices, g->tri, g->n, nullptr, 1, g->d_score);
     return 2;
 }
 
@@ -134,45 +143,40 @@ __device__ __forceinline__ DD2 dd2_add(DD2 a, double b) {
     return {hi, lo};
 }
 
-constexpr int WCC_BLOCKS = 256;
+// One block per graph over its vertex range, like k_score_graph.
+constexpr int WCC_THREADS = 1024;
 
-__global__ void __launch_bounds__(256) k_wcc_terms(int32_t n, const int32_t *__restrict__ labels,
-                                                  const int32_t *__restrict__ sizes,
-                                                  const int32_t *__restrict__ tri,
-                                                  const int32_t *__restrict__ tri_deg,
-                                                  const int32_t *__restrict__ it, const int32_t *__restrict__ itd,
-                                                  DD2 *partial) {
+__global__ void __launch_bounds__(WCC_THREADS) k_wcc_graph(int32_t n, const int32_t *__restrict__ voff,
+                                                          const int32_t *__restrict__ labels,
+                                                          const int32_t *__restrict__ sizes,
+                                                          const int32_t *__restrict__ tri,
+                                                          const int32_t *__restrict__ tri_deg,
+                                                          const int32_t *__restrict__ it,
+                                                          const int32_t *__restrict__ itd, double *out) {
+    const int g = blockIdx.x;
+    const int32_t v0 = voff ? voff[g] : 0, v1 = voff ? voff[g + 1] : n;
+    const int32_t ng = v1 - v0;
     DD2 acc{0.0, 0.0};
-    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    for (int32_t v = v0 + threadIdx.x; v < v1; v += WCC_THREADS) {
         int32_t t = tri[v];
         if (t > 0) {
             int32_t size = sizes[labels[v]];
             double a = it[v] / (double)t;
             double b = tri_deg[v] / (double)(size - 1 + tri_deg[v] - itd[v]);
-            acc = dd2_add(acc, (a * b) / n);
+            acc = dd2_add(acc, (a * b) / ng);
         }
     }
-    __shared__ DD2 sh[256];
+    __shared__ DD2 sh[WCC_THREADS];
     sh[threadIdx.x] = acc;
     __syncthreads();
-    for (int s = 128; s > 0; s >>= 1) {
+    for (int s = WCC_THREADS / 2; s > 0; s >>= 1) {
         if ((int)threadIdx.x < s) {
             DD2 x = dd2_add(sh[threadIdx.x], sh[threadIdx.x + s].hi);
             sh[threadIdx.x] = dd2_add(x, sh[threadIdx.x + s].lo);
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
-}
-
-__global__ void k_wcc_final(const DD2 *partial, int nparts, double *out) {
-    if (threadIdx.x) return;
-    DD2 acc{0.0, 0.0};
-    for (int i = 0; i < nparts; ++i) {
-        acc = dd2_add(acc, partial[i].hi);
-        acc = dd2_add(acc, partial[i].lo);
-    }
-    *out = acc.hi + acc.lo;
+    if (threadIdx.x == 0) out[g] = sh[0].hi + sh[0].lo;
 }
 
 int launch_wcc_score(pcd_graph *g, double *d_out, cudaStream_t st) {
@@ -187,10 +191,10 @@ int launch_wcc_score(pcd_graph *g, double *d_out, cudaStream_t st) {
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
     k_triangles<<<blocks, 256, 0, st>>>(g->indices, g->adj, g->n, g->labels, it, itd);
-    DD2 *partial = reinterpret_cast<DD2 *>(g->small);
-    k_wcc_terms<<<WCC_BLOCKS, 256, 0, st>>>(g->n, g->labels, g->sizes, g->tri, g->tri_deg, it, itd, partial);
-    k_wcc_final<<<1, 32, 0, st>>>(partial, WCC_BLOCKS, d_out);
-    return 3;
+    BatchState *B = g->batch;
+    k_wcc_graph<<<B ? B->G : 1, WCC_THREADS, 0, st>>>(g->n, B ? B->voff : nullptr, g->labels, g->sizes, g->tri,
+                                                      g->tri_deg, it, itd, B ? B->gscore : d_out);
+    return 2;
 }
 
 }  // namespace pcd

@@ -77,6 +77,17 @@ def _load() -> C.CDLL:
         "pcd_graph_set_bins": ([vp, C.POINTER(i32)], i32),
         "pcd_graph_get_bins": ([vp, C.POINTER(i32), C.POINTER(i64)], i32),
         "pcd_profile_read": ([vp, C.POINTER(C.c_char_p), C.POINTER(dbl), i32], i32),
+        "pcd_batch_load": ([vp, i32, vp, vp, vp, C.POINTER(vp)], i32),
+        "pcd_batch_load_device": ([vp, i32, vp, vp, vp, C.POINTER(vp)], i32),
+        "pcd_batch_num_graphs": ([vp, C.POINTER(i32)], i32),
+        "pcd_batch_labels_set": ([vp, vp], i32),
+        "pcd_batch_labels_get": ([vp, vp], i32),
+        "pcd_batch_compress": ([vp, vp], i32),
+        "pcd_batch_score": ([vp, C.POINTER(_Rule), vp], i32),
+        "pcd_batch_refine": ([vp, C.POINTER(_Rule), dbl, vp], i32),
+        "pcd_batch_merge": ([vp, C.POINTER(_Rule), i32, vp], i32),
+        "pcd_batch_run": ([vp, C.POINTER(_Rule), i32, dbl, i32, i32, dbl, i32, vp, vp], i32),
+        "pcd_compress_labels_noalloc": ([vp, i32, vp, vp, vp], i32),
         "pcd_rand_seed": ([C.POINTER(_Rand), u32], None),
         "pcd_rand_next": ([C.POINTER(_Rand)], i32),
         "pcd_rand_skip": ([C.POINTER(_Rand), i64], None),
@@ -389,9 +400,17 @@ class RunResult:
     log: list = field(default_factory=list)
 
 
+THRESHOLD_ITER_CAP = 1000
+
+
 def run(g: Graph, rule: Rule, strategy: int = 0, frac: float = 0.5, rounds: int = 1, n_iter: int = -1,
         threshold: float = 0.0, initial: int = 0, keep_raw: bool = False, callback=None) -> RunResult:
-    """The reference driver loop (src/main.cpp:187-266) on the device."""
+    """The reference driver loop (src/main.cpp:187-266) on the device.
+
+    In threshold mode (n_iter == -1) the reference loops until the relative
+    improvement drops to `threshold`, which never happens for a graph whose
+    score stays <= 0 (e.g. a single edge); this loop, like pcd_batch_run, stops
+    after THRESHOLD_ITER_CAP iterations."""
     rand = GlibcRand(1)
     if initial == 1 or rule.kind == 2:
         g.count_triangles()
@@ -409,7 +428,8 @@ def run(g: Graph, rule: Rule, strategy: int = 0, frac: float = 0.5, rounds: int 
     while True:
         k = g.compress()
         score = rule.calculate(g)
-        done = (it >= n_iter) if n_iter != -1 else (prev > 0 and score > 0 and score / prev - 1 <= threshold)
+        done = (it >= n_iter) if n_iter != -1 else (
+            (prev > 0 and score > 0 and score / prev - 1 <= threshold) or it >= THRESHOLD_ITER_CAP - 1)
         if done:
             break
         if strategy == 0 or (strategy == 2 and it % 2 == 0):
@@ -425,3 +445,94 @@ def run(g: Graph, rule: Rule, strategy: int = 0, frac: float = 0.5, rounds: int 
         it += 1
         prev = score
     return RunResult(g.labels, score, it, k, log)
+
+
+# ---------------------------------------------------------------------------
+# batched path
+# ---------------------------------------------------------------------------
+def pack_graphs(graphs):
+    """(vertex_offsets, indices, adj) of the packed CSR of a list of
+    (indices, adj) pairs: union row offsets, each graph's local neighbour ids."""
+    voff = [0]
+    ind_parts, adj_parts = [], []
+    base = 0
+    for ind, adj in graphs:
+        ind = np.asarray(ind, dtype=np.int64)
+        ind_parts.append(ind[:-1] + base)
+        adj_parts.append(np.asarray(adj, dtype=np.int32))
+        base += int(ind[-1])
+        voff.append(voff[-1] + ind.shape[0] - 1)
+    indices = np.concatenate(ind_parts + [np.array([base], np.int64)]).astype(np.int32)
+    adj = np.concatenate(adj_parts) if adj_parts else np.zeros(0, np.int32)
+    return np.asarray(voff, np.int32), indices, adj
+
+
+class Batch:
+    """Many graphs refined together (pcd_batch_* in include/pcd.h)."""
+
+    def __init__(self, ctx: Context, h, voff: np.ndarray):
+        self.ctx, self.h, self.voff = ctx, h, voff
+        self.G = voff.shape[0] - 1
+        self.n = int(voff[-1])
+
+    @classmethod
+    def from_graphs(cls, ctx: Context, graphs) -> "Batch":
+        voff, indices, adj = pack_graphs(graphs)
+        h = C.c_void_p()
+        ctx._check(LIB.pcd_batch_load(ctx.h, voff.shape[0] - 1, _ptr(voff), _ptr(indices), _ptr(adj), C.byref(h)))
+        b = cls(ctx, h, voff)
+        b._hold = (indices, adj)
+        return b
+
+    @classmethod
+    def from_device(cls, ctx: Context, voff: np.ndarray, d_indices: int, d_adj: int) -> "Batch":
+        voff = np.ascontiguousarray(voff, dtype=np.int32)
+        h = C.c_void_p()
+        ctx._check(LIB.pcd_batch_load_device(ctx.h, voff.shape[0] - 1, _ptr(voff), C.c_void_p(d_indices),
+                                             C.c_void_p(d_adj), C.byref(h)))
+        return cls(ctx, h, voff)
+
+    def free(self):
+        if self.h:
+            LIB.pcd_graph_free(self.h)
+            self.h = None
+
+    @property
+    def labels(self) -> np.ndarray:
+        out = np.empty(self.n, np.int32)
+        self.ctx._check(LIB.pcd_batch_labels_get(self.h, _ptr(out)))
+        return out
+
+    @labels.setter
+    def labels(self, lab):
+        lab = _i32(lab)
+        self.ctx._check(LIB.pcd_batch_labels_set(self.h, _ptr(lab)))
+
+    def graph_labels(self, labels: np.ndarray, g: int) -> np.ndarray:
+        return labels[self.voff[g]:self.voff[g + 1]]
+
+    def compress(self) -> np.ndarray:
+        k = np.zeros(self.G, np.int32)
+        self.ctx._check(LIB.pcd_batch_compress(self.h, _ptr(k)))
+        return k
+
+    def score(self, rule: Rule) -> np.ndarray:
+        out = np.zeros(self.G, np.float64)
+        self.ctx._check(LIB.pcd_batch_score(self.h, C.byref(rule._c()), _ptr(out)))
+        return out
+
+    def refine(self, rule: Rule, frac: float, seeds):
+        s = np.ascontiguousarray(seeds, dtype=np.uint32)
+        self.ctx._check(LIB.pcd_batch_refine(self.h, C.byref(rule._c()), float(frac), _ptr(s)))
+
+    def merge(self, rule: Rule, rounds: int, seeds):
+        s = np.ascontiguousarray(seeds, dtype=np.uint32)
+        self.ctx._check(LIB.pcd_batch_merge(self.h, C.byref(rule._c()), int(rounds), _ptr(s)))
+
+    def run(self, rule: Rule, strategy: int = 0, frac: float = 1.0, rounds: int = 1, n_iter: int = 10,
+            threshold: float = 0.0, cuda_graph: bool = True):
+        scores = np.zeros(self.G, np.float64)
+        iters = np.zeros(self.G, np.int32)
+        self.ctx._check(LIB.pcd_batch_run(self.h, C.byref(rule._c()), strategy, float(frac), rounds, n_iter,
+                                          float(threshold), 1 if cuda_graph else 0, _ptr(scores), _ptr(iters)))
+        return scores, iters
