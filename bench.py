@@ -218,6 +218,148 @@ def run_reference_arm(args, rank, world):
     return 0
 
 
+def batch_cpu_baseline(voff, ind, adj, idx, sched, budget_s):
+    """The oracle's driver loop (one host thread per graph, all host cores in
+    parallel) over the sampled graphs until `budget_s` is spent: graphs/s."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import numpy as np
+
+    import oracle
+
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    done = []
+
+    def one(i):
+        if time.perf_counter() - t0 > budget_s:
+            return None
+        a, b = int(voff[i]), int(voff[i + 1])
+        li = (ind[a:b + 1] - ind[a]).astype(np.int32)
+        la = adj[int(ind[a]):int(ind[b])]
+        oracle.run_schedule(oracle.Port(), li, la, sched["metric"], sched["strategy"], sched["frac"],
+                            sched["rounds"], sched["n_iter"], sched["threshold"], 0, 1)
+        return i
+
+    with ThreadPoolExecutor(threads) as ex:
+        for r in ex.map(one, idx):
+            if r is not None:
+                done.append(r)
+    sec = time.perf_counter() - t0
+    return len(done) / sec, len(done), sec, threads
+
+
+def batched_leg(args, ctx, dev):
+    """Many-graph workload: the log-normal batch of SBMs, every graph run
+    through the reference driver's schedule (singleton start, stop test,
+    final labels and score).  Batched = one packed batch through
+    pcd_batch_run (CUDA-graph-captured iterations); plain = the same graphs
+    one after another through the single-graph API.  Both arms start from the
+    graphs' CSR resident in HBM and end with every label and score on the
+    host; per-graph labels, scores and iteration counts must be identical."""
+    import numpy as np
+    import torch
+
+    import graphs
+    import pcd
+
+    t0 = time.time()
+    voff, d_ind, d_adj = graphs.sbm_batch_torch(args.batch_graphs, seed=4, device=dev)
+    torch.cuda.synchronize()
+    Gn = voff.shape[0] - 1
+    N = int(voff[-1])
+    M = int(d_ind[-1].item()) // 2
+    log(f"[bench] batch: {Gn} SBM graphs, n={N} m={M} ({time.time() - t0:.1f}s)")
+    sched = {"metric": args.batch_metric, "strategy": args.batch_strategy, "frac": args.batch_frac,
+             "rounds": 1, "n_iter": args.batch_iters, "threshold": args.batch_threshold}
+    rule = pcd.parse_metric(sched["metric"])
+    h_labels = torch.empty(N, dtype=torch.int32).pin_memory()
+
+    def batched_job():
+        B = pcd.Batch.from_device(ctx, voff, d_ind.data_ptr(), d_adj.data_ptr())
+        scores, iters = B.run(rule, sched["strategy"], sched["frac"], sched["rounds"], sched["n_iter"],
+                              sched["threshold"], True)
+        B.get_labels_ptr(h_labels.data_ptr())
+        B.free()
+        return scores, iters
+
+    scores, iters = batched_job()  # warm-up (and the results checked below)
+    labels_b = h_labels.numpy().copy()
+    times = []
+    for _ in range(max(1, args.batch_reps)):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        s2, i2 = batched_job()
+        times.append(time.perf_counter() - t)
+        assert np.array_equal(s2, scores) and np.array_equal(i2, iters), "batched run not repeatable"
+    batched_s = statistics.median(times)
+
+    # end to end from pinned host buffers
+    h_ind = d_ind.cpu().pin_memory()
+    h_adj = d_adj.cpu().pin_memory()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    B = pcd.Batch.from_host_ptr(ctx, voff, h_ind.data_ptr(), h_adj.data_ptr())
+    s3, _ = B.run(rule, sched["strategy"], sched["frac"], sched["rounds"], sched["n_iter"], sched["threshold"],
+                  True)
+    B.get_labels_ptr(h_labels.data_ptr())
+    B.free()
+    e2e_s = time.perf_counter() - t
+    assert np.array_equal(s3, scores)
+
+    # the plain path, looped over a stride sample of the same graphs
+    stride = max(1, args.batch_plain_stride)
+    idx = list(range(0, Gn, stride))
+    ind_h = h_ind.numpy()
+    loc = []
+    for i in idx:
+        a, b = int(voff[i]), int(voff[i + 1])
+        li = (d_ind[a:b + 1] - d_ind[a]).contiguous()
+        loc.append((i, li, d_adj[int(ind_h[a]):].data_ptr(), b - a, int(ind_h[b] - ind_h[a]) // 2))
+    torch.cuda.synchronize()
+    mism = 0
+    t = time.perf_counter()
+    for i, li, adj_ptr, n_g, m_g in loc:
+        g1 = pcd.Graph.from_device(ctx, n_g, m_g, li.data_ptr(), adj_ptr)
+        res = pcd.run(g1, rule, sched["strategy"], sched["frac"], sched["rounds"], sched["n_iter"],
+                      sched["threshold"], 0)
+        g1.free()
+        if not (res.score == scores[i] and res.iterations == iters[i]
+                and np.array_equal(res.labels, labels_b[voff[i]:voff[i + 1]])):
+            mism += 1
+    plain_s = time.perf_counter() - t
+    assert mism == 0, f"{mism} graphs differ between the batched and the plain path"
+    plain_gps = len(idx) / plain_s
+    batched_gps = Gn / batched_s
+    sample_edges = sum(x[4] for x in loc)
+
+    cpu = None
+    if not args.no_cpu:
+        adj_h = h_adj.numpy()
+        v, k, sec, thr = batch_cpu_baseline(voff, ind_h, adj_h, idx, sched, 20.0)
+        cpu = {"value": v, "unit": "graphs/s", "cores": thr, "kind": "port",
+               "sample": f"{k} graphs of the stride-{stride} sample, oracle driver loop, one graph per host "
+                         f"thread, {thr} threads, {sec:.1f}s"}
+    return {
+        "workload": f"{Gn} SBM graphs, n ~ LogNormal(ln 5000, 1.2) clipped to [200, 300000], n/50 blocks, "
+                    f"intra-degree 12, inter-degree 2, seed 4 (device generator), degree-sorted",
+        "schedule": f"-m {sched['metric']} -s {sched['strategy']} -f {sched['frac']} -n {sched['n_iter']} "
+                    f"-t {sched['threshold']} from singletons",
+        "n": N, "m": M,
+        "graphs_per_s": batched_gps,
+        "ms_per_job": 1000.0 * batched_s,
+        "edges_per_s": M / batched_s,
+        "e2e": {"graphs_per_s": Gn / e2e_s, "ms_per_job": 1000.0 * e2e_s,
+                "h2d_bytes": int(4 * (N + 1) + 8 * M + 4 * (Gn + 1)), "d2h_bytes": int(4 * N + 12 * Gn)},
+        "plain_graphs_per_s": plain_gps,
+        "plain_sample": f"every {stride}th graph ({len(idx)} graphs, m={sample_edges}), {plain_s:.2f}s",
+        "speedup_vs_plain": batched_gps / plain_gps,
+        "iterations_max": int(iters.max()), "iterations_mean": float(iters.mean()),
+        "identical_to_plain": True,
+        "cpu_baseline": cpu,
+    }
+
+
 def workload_config(args, n, m):
     return {
         "workload": f"rmat-s{args.scale}-ef{args.edge_factor} (a,b,c,d)=(.57,.19,.19,.05) seed 2, degree-sorted; "
@@ -242,6 +384,14 @@ def main():
     ap.add_argument("--sweeps", type=int, default=5, help="cycle through the first S sweeps of the schedule")
     ap.add_argument("--bins", default="", help="degree classes, 7 comma-separated bounds (default: library's)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batch-graphs", type=int, default=4096, help="0: skip the many-graph workload")
+    ap.add_argument("--batch-reps", type=int, default=2)
+    ap.add_argument("--batch-plain-stride", type=int, default=8)
+    ap.add_argument("--batch-metric", default="mod")
+    ap.add_argument("--batch-strategy", type=int, default=0)
+    ap.add_argument("--batch-frac", type=float, default=0.5)
+    ap.add_argument("--batch-iters", type=int, default=-1)
+    ap.add_argument("--batch-threshold", type=float, default=0.0)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -400,6 +550,12 @@ def main():
                "note": "each step: pcd_load_csr from pinned host CSR (validation, degree bins, buffers), "
                        "pcd_labels_set, pcd_refine, pcd_labels_get, pcd_graph_free"}
 
+    batched = None
+    if args.batch_graphs > 0:
+        del d_ind, d_adj
+        torch.cuda.empty_cache()
+        batched = batched_leg(args, ctx, dev)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -431,6 +587,7 @@ def main():
                          "sweep_frac": sweep_bytes / (ms_per_step / 1e3) / 1e9 / peak},
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "batched": batched,
             "gpu_launches": int(launches),
             "clocks": clk,
             "phases_ms": {nm: round(ms, 4) for nm, ms in phases},

@@ -105,7 +105,7 @@ pcd_status sync_and_check(pcd_graph *g) {
         return set_error(ctx, s, buf);
     }
     g->info.draws = g->h_ctr->total_draws;
-    g->info.fallback = g->h_ctr->n_ambiguous;
+    g->info.fallback = g->h_ctr->n_ambiguous + g->h_ctr->n_amb_large;
     g->info.resolved = g->h_ctr->n_resolve;
     g->info.merge_pairs = g->h_ctr->n_pairs;
     return PCD_OK;
@@ -300,6 +300,7 @@ static pcd_status graph_setup(pcd_ctx *ctx, pcd_graph *g) {
     g->tiebuf_cap = g->nnz + n + 16;
     TRY(dev_alloc(g, (void **)&g->tiebuf, sizeof(int32_t) * (size_t)g->tiebuf_cap));
     TRY(dev_alloc(g, (void **)&g->recs, sizeof(TieRecord) * nn));
+    TRY(dev_alloc(g, (void **)&g->nties, sizeof(int32_t) * nn));
     TRY(dev_alloc(g, (void **)&g->amb, sizeof(int32_t) * nn));
     TRY(dev_alloc(g, (void **)&g->ctr, sizeof(DevCounters)));
     TRY(dev_alloc(g, (void **)&g->small, 65536));

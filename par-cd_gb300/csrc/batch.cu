@@ -312,7 +312,9 @@ static pcd_status batch_step(pcd_graph *g, const pcd_rule *rule, bool merge, dou
     pcd_ctx *ctx = g->ctx;
     if (rule->kind == PCD_RULE_WCC) TRY(ensure_triangles(g));
     int launches = 0;
+    prof_begin(ctx, ctx->stream);
     TRY(ensure_compressed(g, &launches));
+    if (launches) prof_mark(ctx, "compress+stats", ctx->stream);
     g->labels_vertex_space = false;
     CK(cudaMemcpyAsync(g->batch->gseed, seeds, sizeof(uint32_t) * g->batch->G, cudaMemcpyHostToDevice, ctx->stream),
        "seeds");

@@ -205,78 +205,113 @@ int launch_compress(pcd_graph *g, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------
-// Rule::calculate for Modularity / CPM: per-community FP64 terms in the
-// reference's expression order, summed with a deterministic double-double
-// reduction (fixed grid, fixed tree).
+// Rule::calculate for Modularity / CPM (src/rules.cpp:9-22, 121-129).  The
+// per-community terms are rational with denominator 2m (CPM) or (2m)^2
+// (Modularity), so the sums are taken exactly in integers,
+//     Modularity = I / 2m - S / (2m)^2,   I = sum int_c, S = sum vol_c^2,
+//     CPM        = (I - lambda * P) / 2m, P = sum size_c (size_c - 1),
+// and rounded once at the end (the reference rounds every term and the
+// running sum; the two agree to the reference's own rounding error).  Integer
+// sums do not depend on the order or grouping of the additions, so a graph
+// gets the same score alone or in a batch, from one block or from many.
+// S <= (2m)^2 < 2^64 and P <= n^2 < 2^62 for 32-bit sizes.
 // ---------------------------------------------------------------------------
-struct DD {
-    double hi, lo;
+struct ScoreSums {
+    unsigned long long a, b;
 };
 
-__device__ __forceinline__ DD dd_add(DD a, double b) {
-    double s = a.hi + b;
-    double bb = s - a.hi;
-    double err = (a.hi - (s - bb)) + (b - bb);
-    double lo = a.lo + err;
-    double hi = s + lo;
-    lo = lo - (hi - s);
-    return {hi, lo};
-}
-
-__device__ __forceinline__ DD dd_add(DD a, DD b) {
-    DD r = dd_add(a, b.hi);
-    return dd_add(r, b.lo);
-}
-
-// One block per graph: thread j adds terms j, j + 1024, ... in order in
-// double-double, then a fixed tree.  The same kernel scores a single graph
-// (G = 1) and every graph of a batch, so a graph gets the same score either way.
-// Community range of graph g: [gK[g], gK[g + 1]) (a single graph: [0, k)).
-constexpr int SCORE_THREADS = 1024;
-
-__global__ void __launch_bounds__(SCORE_THREADS) k_score_graph(int32_t kind, double lambda, int32_t m_single,
-                                                              const int32_t *__restrict__ gm,
-                                                              const int32_t *__restrict__ gK,
-                                                              const int32_t *__restrict__ sizes,
-                                                              const int32_t *__restrict__ intv,
-                                                              const int32_t *__restrict__ vol,
-                                                              const DevCounters *ctr, double *out) {
-    const int g = blockIdx.x;
-    const int32_t c0 = gK ? gK[g] : 0, c1 = gK ? gK[g + 1] : ctr->k;
-    const int32_t m = gm ? gm[g] : m_single;
-    DD acc{0.0, 0.0};
-    for (int32_t i = c0 + threadIdx.x; i < c1; i += SCORE_THREADS) {
-        double t;
-        if (kind == 0) {
-            double actual = intv[i] / (2.0 * m);
-            double x = vol[i] / (2.0 * m);
-            double expect = x * x;  // pow(x, 2)
-            t = actual - expect;
-        } else {
-            t = intv[i] - lambda * sizes[i] * (sizes[i] - 1);
-        }
-        acc = dd_add(acc, t);
+__device__ __forceinline__ ScoreSums score_terms(int32_t kind, int64_t i, const int32_t *__restrict__ sizes,
+                                                 const int32_t *__restrict__ intv, const int32_t *__restrict__ vol) {
+    if (kind == 0) {
+        const unsigned long long v = (unsigned)vol[i];
+        return {(unsigned long long)(unsigned)intv[i], v * v};
     }
-    __shared__ DD sh[SCORE_THREADS];
-    sh[threadIdx.x] = acc;
+    const long long sz = sizes[i];
+    return {(unsigned long long)(unsigned)intv[i], (unsigned long long)(sz * (sz - 1))};
+}
+
+__device__ __forceinline__ double score_value(int32_t kind, double lambda, int32_t m, bool empty,
+                                              unsigned long long a, unsigned long long b) {
+    const double tm = 2.0 * (double)m;
+    if (kind == 0) return empty ? 0.0 : (double)a / tm - (double)b / (tm * tm);
+    return ((double)a - lambda * (double)b) / tm;
+}
+
+__device__ __forceinline__ ScoreSums block_sum(ScoreSums x) {
+    __shared__ unsigned long long sa[32], sb[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 16; o; o >>= 1) {
+        x.a += __shfl_down_sync(0xffffffffu, x.a, o);
+        x.b += __shfl_down_sync(0xffffffffu, x.b, o);
+    }
+    if (lane == 0) {
+        sa[w] = x.a;
+        sb[w] = x.b;
+    }
     __syncthreads();
-    for (int s = SCORE_THREADS / 2; s > 0; s >>= 1) {
-        if ((int)threadIdx.x < s) sh[threadIdx.x] = dd_add(sh[threadIdx.x], sh[threadIdx.x + s]);
-        __syncthreads();
+    ScoreSums r{0, 0};
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+            r.a += sa[i];
+            r.b += sb[i];
+        }
+    return r;  // valid in thread 0
+}
+
+// batch: one block per graph, community range [gK[g], gK[g + 1])
+__global__ void __launch_bounds__(256) k_score_graphs(int32_t kind, double lambda, const int32_t *__restrict__ gm,
+                                                      const int32_t *__restrict__ gK,
+                                                      const int32_t *__restrict__ sizes,
+                                                      const int32_t *__restrict__ intv,
+                                                      const int32_t *__restrict__ vol, double *out) {
+    const int g = blockIdx.x;
+    const int32_t c0 = gK[g], c1 = gK[g + 1];
+    ScoreSums acc{0, 0};
+    for (int32_t i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
+        const ScoreSums t = score_terms(kind, i, sizes, intv, vol);
+        acc.a += t.a;
+        acc.b += t.b;
     }
-    if (threadIdx.x == 0) {
-        double s = sh[0].hi + sh[0].lo;
-        if (kind == 1) s = s / (double)(2 * m);
-        out[g] = s;
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) out[g] = score_value(kind, lambda, gm[g], c1 <= c0, acc.a, acc.b);
+}
+
+// one graph: every block adds its partial sums into acc[0..1]
+__global__ void __launch_bounds__(256) k_score_single(int32_t kind, const int32_t *__restrict__ sizes,
+                                                      const int32_t *__restrict__ intv,
+                                                      const int32_t *__restrict__ vol, const DevCounters *ctr,
+                                                      unsigned long long *acc_out) {
+    const int32_t k = ctr->k;
+    ScoreSums acc{0, 0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < k; i += (int64_t)gridDim.x * blockDim.x) {
+        const ScoreSums t = score_terms(kind, i, sizes, intv, vol);
+        acc.a += t.a;
+        acc.b += t.b;
     }
+    acc = block_sum(acc);
+    if (threadIdx.x == 0 && (acc.a | acc.b)) {
+        atomicAdd(acc_out, acc.a);
+        atomicAdd(acc_out + 1, acc.b);
+    }
+}
+
+__global__ void k_score_final(int32_t kind, double lambda, int32_t m, const DevCounters *ctr,
+                              const unsigned long long *acc, double *out) {
+    *out = score_value(kind, lambda, m, ctr->k <= 0, acc[0], acc[1]);
 }
 
 int launch_score(pcd_graph *g, int32_t kind, double lambda, double *d_out, cudaStream_t st) {
     BatchState *B = g->batch;
-    k_score_graph<<<B ? B->G : 1, SCORE_THREADS, 0, st>>>(kind, lambda, g->m, B ? B->gm : nullptr,
-                                                         B ? B->gK : nullptr, g->sizes, g->intv, g->vol, g->ctr,
-                                                         B ? B->gscore : d_out);
-    return 1;
+    if (B) {
+        k_score_graphs<<<B->G, 256, 0, st>>>(kind, lambda, B->gm, B->gK, g->sizes, g->intv, g->vol, B->gscore);
+        return 1;
+    }
+    unsigned long long *acc = reinterpret_cast<unsigned long long *>(g->small);
+    cudaMemsetAsync(acc, 0, 2 * sizeof(unsigned long long), st);
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((g->n + 255) / 256, g->ctx->num_sms * 4ll));
+    k_score_single<<<grid, 256, 0, st>>>(kind, g->sizes, g->intv, g->vol, g->ctr, acc);
+    k_score_final<<<1, 1, 0, st>>>(kind, lambda, g->m, g->ctr, acc, d_out);
+    return 2;
 }
 
 // ---------------------------------------------------------------------------

@@ -75,6 +75,7 @@ struct pcd_graph {
     int32_t *tiebuf = nullptr;
     int64_t tiebuf_cap = 0;
     pcd::TieRecord *recs = nullptr;   // capacity max(n, k)
+    int32_t *nties = nullptr;         // per vertex: final-level ties of the last sweep
     int32_t *amb = nullptr;           // ambiguous vertex list, capacity n
     pcd::DevCounters *ctr = nullptr;  // device counters
     void *small = nullptr;            // 64 KiB of reduction scratch

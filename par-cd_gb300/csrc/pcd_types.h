@@ -15,7 +15,7 @@ struct DevCounters {
     uint32_t total_draws;         // rand_r calls of the sweep (mod 2^32)
     int32_t n_pairs;              // contracted pairs (merge)
     int32_t all_found;            // merge: every community matched
-    int32_t pad;
+    int32_t n_amb_large;          // of those, vertices of degree > 256 (queued from the list's end)
 };
 
 enum : int32_t {

@@ -67,6 +67,7 @@ struct SweepArgs {
     int32_t *tiebuf;
     long long tiebuf_cap;
     TieRecord *recs;
+    int32_t *nties;  // per vertex: final-level ties to replay (0: none)
     int32_t *amb;
     DevCounters *ctr;
 };
@@ -74,23 +75,33 @@ struct SweepArgs {
 // ---------------------------------------------------------------------------
 // output of one analysed vertex
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void push_ambiguous(const SweepArgs &a, int32_t v) {
-    int32_t i = atomicAdd(&a.ctr->n_ambiguous, 1);
-    a.amb[i] = v;
+// Vertices the integer key cannot decide go to one list (capacity n) filled
+// from both ends: degree <= AMB_WARP_MAX from the front (re-evaluated one warp
+// per vertex), larger ones from the back (one block per vertex).
+constexpr int AMB_WARP_MAX = 256;
+
+__device__ __forceinline__ void push_ambiguous(const SweepArgs &a, int32_t v, int32_t d) {
+    if (d <= AMB_WARP_MAX) {
+        const int32_t i = atomicAdd(&a.ctr->n_ambiguous, 1);
+        a.amb[i] = v;
+    } else {
+        const int32_t i = atomicAdd(&a.ctr->n_amb_large, 1);
+        a.amb[a.g.n - 1 - i] = v;
+    }
 }
 
-// Allocates the tie record of a MOVE vertex with r >= 1 ties; returns the
-// buffer offset (or -1 on overflow, flagged).
-__device__ __forceinline__ long long alloc_ties(const SweepArgs &a, int32_t v, int32_t r, int32_t holder) {
-    unsigned long long off = atomicAdd(&a.ctr->tie_used, (unsigned long long)(r + 1));
-    if ((long long)(off + r + 1) > a.tiebuf_cap) {
-        atomicOr(&a.ctr->error, ERR_TIEBUF_OVERFLOW);
-        return -1;
-    }
+// The final-level ties of vertex v live in its own slots of the tie buffer,
+// [indices[v] + v, indices[v + 1] + v + 1): the holder, then the r tied
+// labels in row order (r <= degree).  nties[v] = r tells the replay which
+// vertices to visit; fixed slots need no allocation, so analysing kernels
+// share no counter.  Returns the slot offset, or -1 when nothing is recorded.
+__device__ __forceinline__ long long record_ties(const SweepArgs &a, int32_t v, int32_t row, bool rec, int32_t r,
+                                                 int32_t holder) {
+    a.nties[v] = rec ? r : 0;
+    if (!rec) return -1;
+    const long long off = (long long)row + v;
     a.tiebuf[off] = holder;
-    int32_t ri = atomicAdd(&a.ctr->n_resolve, 1);
-    a.recs[ri] = TieRecord{v, r, (long long)off};
-    return (long long)off;
+    return off;
 }
 
 __device__ __forceinline__ void write_decision(const SweepArgs &a, int32_t v, int32_t dec, int32_t holder,
@@ -200,16 +211,16 @@ __global__ void __launch_bounds__(256) k_prop_group(SweepArgs a, R rule, const i
             if (dec == DEC_AMBIGUOUS) amb = true;
         }
         const bool leader = has_v && gl == 0;
-        const bool want = leader && !amb && dec == DEC_MOVE && r > 0;
-        long long off = alloc_ties_warp(a, v, r, holder, want);
-        off = __shfl_sync(FULL, off, gid * G);
+        const bool rec = has_v && !amb && dec == DEC_MOVE && r > 0;  // the same in every lane of the group
+        const long long off = rec ? (long long)b + v : -1;
         if (off >= 0 && inrun) a.tiebuf[off + 1 + __popc(rm & lanemask_lt())] = lab;
         if (leader) {
             if (amb) {
-                push_ambiguous(a, v);
+                push_ambiguous(a, v, d);
             } else {
                 a.ndraw[v] = (uint32_t)__popc(tm);
                 write_decision(a, v, dec, holder, curr);
+                record_ties(a, v, b, rec, r, holder);
             }
         }
     }
@@ -223,9 +234,101 @@ __global__ void __launch_bounds__(256) k_prop_group(SweepArgs a, R rule, const i
 // Then an ordered warp scan of the gains with the running maximum carried
 // across chunks.
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// One thread per vertex (deg <= MAXD): the reference's candidate loop run as
+// it is written, on a row held in registers.  Counting is a pass over the
+// pairs i < j of the row (an equal later label adds to the earlier one's
+// count and is not a first occurrence), so a label's count sits at its first
+// position; then the first occurrences are scored in row order with the
+// running maximum, its ties (every tie is one rand_r draw) and the positions
+// tied with the final holder (a bit mask).  No lane talks to another, so a
+// warp analyses 32 vertices at once.
+// ---------------------------------------------------------------------------
+template <class R, int MAXD>
+__global__ void __launch_bounds__(256) k_prop_thread(SweepArgs a, R rule, const int32_t *__restrict__ list,
+                                                     int64_t count) {
+    using Key = typename R::Key;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < count;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t v = list[idx];
+        const int32_t b = a.g.indices[v], d = a.g.indices[v + 1] - b;
+        const int32_t curr = a.labels[v];
+        const R vr = rule.at(v);
+        int32_t lab[MAXD];
+        int32_t cnt[MAXD];
+#pragma unroll
+        for (int j = 0; j < MAXD; ++j) lab[j] = j < d ? a.g.adj[b + j] : -1;
+#pragma unroll
+        for (int j = 0; j < MAXD; ++j) {
+            lab[j] = j < d ? a.labels[lab[j]] : -2 - j;  // distinct negative fillers never match
+            cnt[j] = 1;
+        }
+        uint32_t later = 0;  // bit j: lab[j] occurred at an earlier position
+#pragma unroll
+        for (int j = 1; j < MAXD; ++j) {
+#pragma unroll
+            for (int i = 0; i < j; ++i) {
+                const bool e = lab[i] == lab[j];
+                cnt[i] += e ? 1 : 0;
+                later |= e ? (1u << j) : 0u;
+            }
+        }
+        Key best = R::initial();
+        int32_t best_j = -1;
+        Tag htag{0, 0};
+        uint32_t run = 0;  // positions tied with the current holder
+        uint32_t t = 0;
+        bool amb = false;
+        int32_t curr_freq = 0;
+#pragma unroll
+        for (int j = 0; j < MAXD; ++j) {
+            if (j < d && !((later >> j) & 1u)) {
+                if (lab[j] == curr) {
+                    curr_freq = cnt[j];
+                } else {
+                    Tag tag{0, 0};
+                    const Key key = vr.join(v, d, lab[j], cnt[j], a.cm, tag);
+                    if (R::usable(key)) {
+                        if (R::gt(key, best)) {
+                            best = key;
+                            best_j = j;
+                            htag = tag;
+                            run = 0;
+                        } else if (R::eq(key, best)) {
+                            ++t;
+                            run |= 1u << j;
+                            if (R::ambiguous_tie(tag, htag, best_j >= 0)) amb = true;
+                        }
+                    }
+                }
+            }
+        }
+        amb = amb || vr.vertex_ambiguous(d);
+        const int32_t dec = amb ? DEC_AMBIGUOUS : vr.decide(best, best_j >= 0, v, d, curr, curr_freq, a.cm);
+        if (dec == DEC_AMBIGUOUS) {
+            push_ambiguous(a, v, d);
+            continue;
+        }
+        int32_t holder = -1;
+#pragma unroll
+        for (int j = 0; j < MAXD; ++j)
+            if (j == best_j) holder = lab[j];
+        const int32_t r = __popc(run);
+        a.ndraw[v] = t;
+        write_decision(a, v, dec, holder, curr);
+        const long long off = record_ties(a, v, b, dec == DEC_MOVE && r > 0, r, holder);
+        if (off >= 0) {
+            int32_t o = 1;
+#pragma unroll
+            for (int j = 0; j < MAXD; ++j)
+                if ((run >> j) & 1u) a.tiebuf[off + o++] = lab[j];
+        }
+    }
+}
+
 template <class R, int WCAP>
 __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const int32_t *__restrict__ list,
-                                                   int64_t count) {
+                                                   int64_t count, const int32_t *count_dev) {
     constexpr int TS = 2 * WCAP;
     constexpr int PER_WARP = 2 * TS + 4 * WCAP;
     extern __shared__ int32_t smem[];
@@ -240,13 +343,14 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
     int32_t *ties = cvol + WCAP;
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    if (count_dev) count = *count_dev;
     for (int64_t idx = gw; idx < count; idx += nw) {
         const int32_t v = list[idx];
         const int32_t b = a.g.indices[v], e = a.g.indices[v + 1], d = e - b;
         const int32_t curr = a.labels[v];
         const R vr = rule.at(v);
         if (vr.vertex_ambiguous(d)) {
-            if (lane == 0) push_ambiguous(a, v);
+            if (lane == 0) push_ambiguous(a, v, d);
             continue;
         }
         int32_t ts = 64;
@@ -345,14 +449,15 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
         const int32_t holder = has ? clab[carry.ord] : -1;
         int32_t dec = amb ? DEC_AMBIGUOUS : vr.decide(carry.key, has, v, d, curr, curr_freq, a.cm);
         if (dec == DEC_AMBIGUOUS) {
-            if (lane == 0) push_ambiguous(a, v);
+            if (lane == 0) push_ambiguous(a, v, d);
             continue;
         }
-        long long off = alloc_ties_warp(a, v, r, holder, lane == 0 && dec == DEC_MOVE && r > 0);
-        off = __shfl_sync(FULL, off, 0);
+        const bool rec = dec == DEC_MOVE && r > 0;
+        const long long off = rec ? (long long)b + v : -1;
         if (lane == 0) {
             a.ndraw[v] = t;
             write_decision(a, v, dec, holder, curr);
+            record_ties(a, v, b, rec, r, holder);
         }
         if (off >= 0)
             for (int32_t j = lane; j < r; j += 32) a.tiebuf[off + 1 + j] = ties[j];
@@ -410,7 +515,7 @@ template <class R, bool GLOBAL, int BT, int U>
 __global__ void __launch_bounds__(BT) k_prop_block(SweepArgs a, R rule, const int32_t *__restrict__ list,
                                                    int64_t count, const int32_t *count_dev, int32_t table_cap,
                                                    int32_t *gscratch, int64_t gstride,
-                                                   const long long *__restrict__ region_off) {
+                                                   const long long *__restrict__ region_off, int from_end) {
     using Key = typename R::Key;
     using E = Elem<Key>;
     constexpr int NW = BT / 32;
@@ -427,12 +532,12 @@ __global__ void __launch_bounds__(BT) k_prop_block(SweepArgs a, R rule, const in
         }
     }
     for (int64_t vi = blockIdx.x; vi < count; vi += gridDim.x) {
-        const int32_t v = list[vi];
+        const int32_t v = from_end ? list[-1 - vi] : list[vi];
         const int32_t b = a.g.indices[v], e = a.g.indices[v + 1], d = e - b;
         const int32_t curr = a.labels[v];
         const R vr = rule.at(v);
         if (vr.vertex_ambiguous(d)) {
-            if (tid == 0) push_ambiguous(a, v);
+            if (tid == 0) push_ambiguous(a, v, d);
             continue;
         }
         int32_t ts = 64;
@@ -664,11 +769,11 @@ __global__ void __launch_bounds__(BT) k_prop_block(SweepArgs a, R rule, const in
             s.off = -1;
             const int32_t dec = s.amb ? DEC_AMBIGUOUS : vr.decide(c.key, c.ord >= 0, v, d, curr, s.curr_freq, a.cm);
             if (dec == DEC_AMBIGUOUS) {
-                push_ambiguous(a, v);
+                push_ambiguous(a, v, d);
             } else {
                 a.ndraw[v] = s.t;
                 write_decision(a, v, dec, s.fin_label, curr);
-                if (dec == DEC_MOVE && r > 0) s.off = alloc_ties(a, v, r, s.fin_label);
+                s.off = record_ties(a, v, b, dec == DEC_MOVE && r > 0, r, s.fin_label);
             }
         }
         __syncthreads();
@@ -710,7 +815,7 @@ __global__ void __launch_bounds__(512) k_prop_hub(SweepArgs a, R rule, const int
         const int32_t curr = a.labels[v];
         const R vr = rule.at(v);
         if (vr.vertex_ambiguous(d)) {
-            if (tid == 0) push_ambiguous(a, v);
+            if (tid == 0) push_ambiguous(a, v, d);
             continue;
         }
         int32_t ts = 64;
@@ -925,11 +1030,11 @@ __global__ void __launch_bounds__(512) k_prop_hub(SweepArgs a, R rule, const int
             s.off = -1;
             const int32_t dec = s.amb ? DEC_AMBIGUOUS : vr.decide(c.key, c.ord >= 0, v, d, curr, s.curr_freq, a.cm);
             if (dec == DEC_AMBIGUOUS) {
-                push_ambiguous(a, v);
+                push_ambiguous(a, v, d);
             } else {
                 a.ndraw[v] = s.t;
                 write_decision(a, v, dec, s.fin_label, curr);
-                if (dec == DEC_MOVE && r > 0) s.off = alloc_ties(a, v, r, s.fin_label);
+                s.off = record_ties(a, v, b, dec == DEC_MOVE && r > 0, r, s.fin_label);
             }
         }
         __syncthreads();
@@ -959,35 +1064,111 @@ struct DrawStore {
 __global__ void k_total_draws(DevCounters *ctr, const uint32_t *total) { ctr->total_draws = *total; }
 
 // frac < 1: whether v draws its ties depends on its frac draw, which depends
-// on every earlier vertex's draw count, so one thread per graph walks that
-// graph's stream in vertex order (src/refinement.cpp:127-132 with one thread).
+// on every earlier vertex's draw count, so each graph's stream is walked in
+// vertex order (src/refinement.cpp:127-132 with one thread).  One warp per
+// graph: for a chunk of 32 vertices every lane loads its vertex's tie-draw
+// count t and composes the affine map of t rand_r calls (independent of the
+// stream state); then the whole warp steps the state through the chunk in
+// lock-step, so the sequential part is a few integer operations per vertex
+// (the frac draw's three LCG steps are evaluated in parallel from the state).
 // voff null: one graph [0, n) with `seed`; else graph g = [voff[g], voff[g+1])
 // with gseed[g].  Writes each vertex's end position relative to its graph.
-__global__ void k_walk(uint32_t seed, const uint32_t *gseed, const int32_t *voff, int32_t G, int32_t f, int32_t n,
-                       uint32_t *ndraw, const int32_t *__restrict__ labels, int32_t *new_labels, int32_t *skip,
-                       DevCounters *ctr) {
-    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < G; g += (int64_t)gridDim.x * blockDim.x) {
+__device__ __forceinline__ void calls_map(uint32_t calls, uint32_t &a, uint32_t &c) {
+    a = 1u;
+    c = 0u;
+#pragma unroll 1
+    for (int i = 0; calls; ++i, calls >>= 1)
+        if (calls & 1u) {
+            c = c_jump.a[i] * c + c_jump.c[i];
+            a = c_jump.a[i] * a;
+        }
+}
+
+// One vertex of the walk: the frac draw from state x (its three LCG steps
+// evaluated side by side from x; s1 is kept pre-shifted by 4 bits so the 11
+// high-order output bits land in place), then, when the vertex draws, the
+// affine map (ta, tc) of its t tie draws.
+struct WalkStep {
+    static constexpr uint32_t A1 = 1103515245u, C1 = 12345u;
+    static constexpr uint32_t A2 = A1 * A1, C2 = A1 * C1 + C1;
+    static constexpr uint32_t A3 = A1 * A2, C3 = A1 * C2 + C1;
+    __device__ __forceinline__ static bool step(uint32_t &x, uint32_t f, uint32_t ta, uint32_t tc) {
+        const uint32_t s1 = (16u * A1) * x + 16u * C1;
+        const uint32_t s2 = A2 * x + C2;
+        const uint32_t s3 = A3 * x + C3;
+        const uint32_t val = (s1 & 0x7FF00000u) ^ ((s2 >> 6) & 0x000FFC00u) ^ ((s3 >> 16) & 0x3FFu);
+        const bool draws = val <= f;
+        x = draws ? ta * s3 + tc : s3;
+        return draws;
+    }
+};
+
+__global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gseed, const int32_t *voff, int32_t G,
+                                              int32_t f, int32_t n, uint32_t *ndraw,
+                                              const int32_t *__restrict__ labels, int32_t *new_labels,
+                                              int32_t *skip, DevCounters *ctr) {
+    __shared__ uint32_t sh[4][3][32];
+    __shared__ uint32_t jA[32], jC[32];
+    if (threadIdx.x < 32) {
+        jA[threadIdx.x] = c_jump.a[threadIdx.x];
+        jC[threadIdx.x] = c_jump.c[threadIdx.x];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const uint32_t uf = (uint32_t)f;
+    uint32_t *st = sh[wib][0], *sa = sh[wib][1], *sc = sh[wib][2];
+    for (int64_t g = warp; g < G; g += nw) {
         const int32_t v0 = voff ? voff[g] : 0, v1 = voff ? voff[g + 1] : n;
         uint32_t x = voff ? gseed[g] : seed, pos = 0;
-        for (int32_t v = v0; v < v1; ++v) {
-            int32_t val = rand_r_dev(x);
-            pos += 1;
-            uint32_t t = ndraw[v];
-            if (val > f) {
-                skip[v] = 1;
-                new_labels[v] = labels[v];
-            } else {
-                skip[v] = 0;
-                if (t < 8) {
-                    for (uint32_t j = 0; j < t; ++j) (void)rand_r_dev(x);
-                } else {
-                    x = rand_r_jump(x, t);
+        uint32_t t_next = v0 + lane < v1 ? ndraw[v0 + lane] : 0u;
+        for (int32_t c0 = v0; c0 < v1; c0 += 32) {
+            const int32_t v = c0 + lane;
+            const uint32_t t = t_next;
+            // the next chunk's counts are loaded while this chunk is walked
+            t_next = v + 32 < v1 ? ndraw[v + 32] : 0u;
+            uint32_t ta = 1u, tc = 0u;
+#pragma unroll 1
+            for (uint32_t rem = t, i = 0; rem; ++i, rem >>= 1)
+                if (rem & 1u) {
+                    tc = jA[i] * tc + jC[i];
+                    ta = jA[i] * ta;
                 }
-                pos += t;
+            __syncwarp();
+            st[lane] = t;
+            sa[lane] = ta;
+            sc[lane] = tc;
+            __syncwarp();
+            uint32_t my_pos = 0;
+            int32_t my_skip = 0;
+            if (v1 - c0 >= 32) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const bool d = WalkStep::step(x, uf, sa[j], sc[j]);
+                    pos += d ? 1u + st[j] : 1u;
+                    if (lane == j) {
+                        my_pos = pos;
+                        my_skip = d ? 0 : 1;
+                    }
+                }
+            } else {
+                for (int j = 0; j < v1 - c0; ++j) {
+                    const bool d = WalkStep::step(x, uf, sa[j], sc[j]);
+                    pos += d ? 1u + st[j] : 1u;
+                    if (lane == j) {
+                        my_pos = pos;
+                        my_skip = d ? 0 : 1;
+                    }
+                }
             }
-            ndraw[v] = pos;
+            if (v < v1) {
+                ndraw[v] = my_pos;
+                skip[v] = my_skip;
+                if (my_skip) new_labels[v] = labels[v];
+            }
         }
-        if (!voff) ctr->total_draws = pos;
+        if (!voff && lane == 0) ctr->total_draws = pos;
     }
 }
 
@@ -1039,10 +1220,47 @@ __global__ void k_resolve(const TieRecord *__restrict__ recs, const DevCounters 
     }
 }
 
+// Propagation replay over every vertex (mod_base 2): vertices with nties[v] > 0
+// redo the reservoir draws of their final level from their own slots.
+__global__ void __launch_bounds__(256) k_resolve_vertices(
+    int32_t n, const int32_t *__restrict__ nties, const int32_t *__restrict__ indices,
+    const uint32_t *__restrict__ endpos, const int32_t *__restrict__ tiebuf, int32_t *out, uint32_t seed,
+    const int32_t *skip, const int32_t *__restrict__ vgid, const uint32_t *__restrict__ gseed,
+    const uint32_t *__restrict__ gbase, DevCounters *ctr) {
+    int32_t replayed = 0;
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t r = nties[v];
+        if (r <= 0 || (skip && skip[v])) continue;
+        uint32_t sd = seed, bb = 0u;
+        if (vgid) {
+            const int32_t g = vgid[v];
+            sd = gseed[g];
+            bb = 0u - gbase[g];
+        }
+        uint32_t x = rand_r_jump(sd, bb + endpos[v] - (uint32_t)r);
+        const long long off = (long long)indices[v] + v;
+        int32_t best = tiebuf[off];
+        for (int32_t j = 0; j < r; ++j) {
+            const int32_t val = rand_r_dev(x);
+            if (val % (j + 2) == 0) best = tiebuf[off + 1 + j];
+        }
+        out[v] = best;
+        ++replayed;
+    }
+    __shared__ int32_t block_count;
+    if (threadIdx.x == 0) block_count = 0;
+    __syncthreads();
+    replayed = __reduce_add_sync(0xffffffffu, replayed);
+    if ((threadIdx.x & 31) == 0 && replayed) atomicAdd(&block_count, replayed);
+    __syncthreads();
+    if (threadIdx.x == 0 && block_count) atomicAdd(&ctr->n_resolve, block_count);
+}
+
 __global__ void k_reset_sweep(DevCounters *ctr) {
     ctr->tie_used = 0;
     ctr->n_resolve = 0;
     ctr->n_ambiguous = 0;
+    ctr->n_amb_large = 0;
     ctr->error = 0;
     ctr->total_draws = 0;
 }
@@ -1071,21 +1289,32 @@ static void launch_group(pcd_graph *g, const SweepArgs &a, const R &rule, int bi
     prof_mark(g->ctx, name, st);
 }
 
+template <class R, int MAXD>
+static void launch_thread(pcd_graph *g, const SweepArgs &a, const R &rule, int bin, const char *name,
+                          cudaStream_t st, int *launches) {
+    const int64_t c = g->bin_off[bin + 1] - g->bin_off[bin];
+    if (c <= 0) return;
+    k_prop_thread<R, MAXD><<<cap_grid((c + 255) / 256, (int64_t)g->ctx->num_sms * 16), 256, 0, st>>>(
+        a, rule, g->bin_list + g->bin_off[bin], c);
+    ++*launches;
+    prof_mark(g->ctx, name, st);
+}
+
 template <class R>
 static int launch_bins_rule(pcd_graph *g, const SweepArgs &a, const R &rule, cudaStream_t st) {
     const int sms = g->ctx->num_sms;
     int launches = 0;
     const int32_t *L = g->bin_list;
     int64_t c;
-    launch_group<R, 4>(g, a, rule, BIN_G4, "sweep.g4", st, &launches);
-    launch_group<R, 8>(g, a, rule, BIN_G8, "sweep.g8", st, &launches);
-    launch_group<R, 16>(g, a, rule, BIN_G16, "sweep.g16", st, &launches);
+    launch_thread<R, 4>(g, a, rule, BIN_G4, "sweep.g4", st, &launches);
+    launch_thread<R, 8>(g, a, rule, BIN_G8, "sweep.g8", st, &launches);
+    launch_thread<R, 16>(g, a, rule, BIN_G16, "sweep.g16", st, &launches);
     launch_group<R, 32>(g, a, rule, BIN_G32, "sweep.g32", st, &launches);
     if ((c = g->bin_off[BIN_WARP + 1] - g->bin_off[BIN_WARP]) > 0) {
         const size_t smem = 8ull * (2 * 2 * WARP_CAP + 4 * WARP_CAP) * sizeof(int32_t);
         cudaFuncSetAttribute(k_prop_warp<R, WARP_CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_prop_warp<R, WARP_CAP><<<cap_grid((c + 7) / 8, sms * 8), 256, smem, st>>>(a, rule,
-                                                                                L + g->bin_off[BIN_WARP], c);
+        k_prop_warp<R, WARP_CAP><<<cap_grid((c + 7) / 8, sms * 8), 256, smem, st>>>(
+            a, rule, L + g->bin_off[BIN_WARP], c, nullptr);
         ++launches;
         prof_mark(g->ctx, "sweep.warp", st);
     }
@@ -1094,7 +1323,7 @@ static int launch_bins_rule(pcd_graph *g, const SweepArgs &a, const R &rule, cud
         cudaFuncSetAttribute(k_prop_block<R, false, 256, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
         k_prop_block<R, false, 256, 4><<<cap_grid(c, sms * 4), 256, smem, st>>>(
-            a, rule, L + g->bin_off[BIN_BLOCK], c, nullptr, 2 * BLOCK_CAP, nullptr, 0, nullptr);
+            a, rule, L + g->bin_off[BIN_BLOCK], c, nullptr, 2 * BLOCK_CAP, nullptr, 0, nullptr, 0);
         ++launches;
         prof_mark(g->ctx, "sweep.block", st);
     }
@@ -1103,7 +1332,7 @@ static int launch_bins_rule(pcd_graph *g, const SweepArgs &a, const R &rule, cud
         cudaFuncSetAttribute(k_prop_block<R, false, 512, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
         k_prop_block<R, false, 512, 4><<<cap_grid(c, sms), 512, smem, st>>>(
-            a, rule, L + g->bin_off[BIN_BLOCK_L], c, nullptr, 2 * BLOCK_L_CAP, nullptr, 0, nullptr);
+            a, rule, L + g->bin_off[BIN_BLOCK_L], c, nullptr, 2 * BLOCK_L_CAP, nullptr, 0, nullptr, 0);
         ++launches;
         prof_mark(g->ctx, "sweep.block_l", st);
     }
@@ -1133,6 +1362,7 @@ int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32
     a.tiebuf = g->tiebuf;
     a.tiebuf_cap = g->tiebuf_cap;
     a.recs = g->recs;
+    a.nties = g->nties;
     a.amb = g->amb;
     a.ctr = g->ctr;
     k_reset_sweep<<<1, 1, 0, st>>>(g->ctr);
@@ -1144,13 +1374,20 @@ int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32
         r.two_m = 2LL * g->m;
         r.bv = bv;
         launches += launch_bins_rule(g, a, r, st);
+        // FP64 re-evaluation of the vertices the integer key left open; the
+        // list lengths are only known on the device, so both grids stride
         RuleModF64 rf;
         rf.m = g->m;
         rf.bv = bv;
+        const size_t smem = 8ull * (2 * 2 * WARP_CAP + 4 * WARP_CAP) * sizeof(int32_t);
+        cudaFuncSetAttribute(k_prop_warp<RuleModF64, WARP_CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        k_prop_warp<RuleModF64, WARP_CAP><<<g->ctx->num_sms * 8, 256, smem, st>>>(a, rf, g->amb, 0,
+                                                                                  &g->ctr->n_ambiguous);
         k_prop_block<RuleModF64, true, 512, 2><<<g->fb_blocks, 512, 0, st>>>(
-            a, rf, g->amb, 0, &g->ctr->n_ambiguous, (int32_t)g->fb_slots, g->fb_scratch,
-            3 * g->fb_slots + g->max_deg, nullptr);
-        ++launches;
+            a, rf, g->amb + g->n, 0, &g->ctr->n_amb_large, (int32_t)g->fb_slots, g->fb_scratch,
+            3 * g->fb_slots + g->max_deg, nullptr, 1);
+        launches += 2;
         prof_mark(g->ctx, "sweep.fp64_recheck", st);
     } else if (kind == PCD_RULE_CPM) {
         RuleCPM r;
@@ -1176,16 +1413,16 @@ int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32
         prof_mark(g->ctx, "sweep.draw_scan", st);
     } else {
         const int32_t G = B ? B->G : 1;
-        k_walk<<<(G + 127) / 128, 128, 0, st>>>(seed, B ? B->gseed : nullptr, B ? B->voff : nullptr, G, f, g->n,
+        k_walk<<<(unsigned)((G + 3) / 4), 128, 0, st>>>(seed, B ? B->gseed : nullptr, B ? B->voff : nullptr, G, f, g->n,
                                                 g->ndraw, g->labels, g->labels_alt, g->first, g->ctr);
         if (B) cudaMemsetAsync(B->gbase, 0, sizeof(uint32_t) * B->G, st);
         skip = g->first;
         ++launches;
         prof_mark(g->ctx, "sweep.draw_walk", st);
     }
-    k_resolve<<<g->ctx->num_sms * 4, 256, 0, st>>>(g->recs, g->ctr, g->ndraw, nullptr, g->tiebuf, g->labels_alt,
-                                                  seed, 2, skip, B ? B->vgid : nullptr, B ? B->gseed : nullptr,
-                                                  B ? B->gbase : nullptr, nullptr);
+    k_resolve_vertices<<<g->ctx->num_sms * 8, 256, 0, st>>>(g->n, g->nties, g->indices, g->ndraw, g->tiebuf,
+                                                           g->labels_alt, seed, skip, B ? B->vgid : nullptr,
+                                                           B ? B->gseed : nullptr, B ? B->gbase : nullptr, g->ctr);
     ++launches;
     if (B) {
         k_done_fixup<<<g->ctx->num_sms * 8, 256, 0, st>>>(B->vgid, B->gdone, g->labels, g->labels_alt, g->n);

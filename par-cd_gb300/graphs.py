@@ -408,3 +408,123 @@ def sbm_batch(count: int = 4096, seed: int = 4, median: float = 5000, sigma: flo
         sizes[: int(n) - int(sizes.sum())] += 1
         e = sbm_sparse(sizes, deg_in, deg_out, rng)
         yield convert_edges(e, int(n))
+
+
+def sbm_batch_torch(count: int = 4096, seed: int = 4, median: float = 5000, sigma: float = 1.2,
+                    lo: int = 200, hi: int = 300_000, deg_in: float = 12.0, deg_out: float = 2.0,
+                    block: int = 50, device="cuda"):
+    """The batched SBM workload generated with torch on a device (input
+    generation for the benchmark; `sbm_batch` is the numpy version for tests).
+
+    Same laws as `sbm_batch`: log-normal vertex counts (`batch_sizes`), n/block
+    near-equal blocks per graph, Binomial(s(s-1)/2, deg_in/(s-1)) intra pairs per
+    block drawn with 10% oversampling, Poisson(deg_out*n/2) uniform inter pairs
+    that are kept when their endpoints sit in different blocks.  The random
+    streams are torch's, so the graphs differ from `sbm_batch`'s draw for draw.
+    Every graph then gets the converter's semantics: loops and duplicates
+    dropped, vertices relabelled by (degree, id) descending, isolated vertices
+    removed.
+
+    Returns (vertex_offsets numpy int32[G+1], indices torch int32[N+1] union row
+    offsets, adj torch int32[2M] local neighbour ids): the packed layout of
+    pcd_batch_load_device."""
+    import torch
+
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    ns = batch_sizes(count, median, sigma, lo, hi, seed)
+    G = ns.shape[0]
+    nb = np.maximum(1, ns // block)
+    base_sz = ns // nb
+    extra = ns - base_sz * nb
+    first_blk = np.cumsum(nb) - nb
+    blk_local = np.arange(int(nb.sum())) - np.repeat(first_blk, nb)
+    sz_np = np.repeat(base_sz, nb) + (blk_local < np.repeat(extra, nb))
+    goff_np = np.concatenate([[0], np.cumsum(ns)]).astype(np.int64)
+    N = int(goff_np[-1])
+    dev = torch.device(device)
+    sz = torch.from_numpy(sz_np.astype(np.int64)).to(dev)
+    bstart = torch.cumsum(sz, 0) - sz            # graphs are contiguous, blocks tile them
+    ns_t = torch.from_numpy(ns).to(dev)
+    goff = torch.from_numpy(goff_np).to(dev)
+    nblk = sz.shape[0]
+    # intra-block pairs
+    szf = sz.to(torch.float64)
+    pairs = szf * (szf - 1) / 2
+    p = torch.where(sz >= 2, torch.clamp(deg_in / torch.clamp(szf - 1, min=1.0), max=1.0), torch.zeros_like(szf))
+    k = torch.binomial(pairs, p, generator=gen)
+    draws = torch.where(sz >= 2, torch.floor(k * 1.1).to(torch.int64) + 4, torch.zeros_like(sz))
+    rep = torch.repeat_interleave(torch.arange(nblk, device=dev), draws)
+    s_rep = sz[rep]
+    b_rep = bstart[rep]
+    del rep
+
+    def pick(size):
+        r = torch.rand(size.shape[0], generator=gen, device=dev, dtype=torch.float64)
+        return torch.minimum((r * size.to(torch.float64)).to(torch.int64), size - 1)
+
+    a_in = b_rep + pick(s_rep)
+    b_in = b_rep + pick(s_rep)
+    del s_rep, b_rep
+    # inter-block pairs
+    k_out = torch.poisson(ns_t.to(torch.float64) * (deg_out / 2.0), generator=gen).to(torch.int64)
+    grep = torch.repeat_interleave(torch.arange(G, device=dev), k_out)
+    n_rep = ns_t[grep]
+    g_rep = goff[grep]
+    del grep
+    a_out = g_rep + pick(n_rep)
+    b_out = g_rep + pick(n_rep)
+    del n_rep, g_rep
+    vblk = torch.repeat_interleave(torch.arange(nblk, device=dev), sz)
+    ok = vblk[a_out] != vblk[b_out]
+    a = torch.cat([a_in, a_out[ok]])
+    b = torch.cat([b_in, b_out[ok]])
+    del a_in, b_in, a_out, b_out, ok, vblk
+    keep = a != b
+    a, b = a[keep], b[keep]
+    lo_v = torch.minimum(a, b)
+    hi_v = torch.maximum(a, b)
+    del a, b, keep
+    key = torch.unique(lo_v * N + hi_v)
+    del lo_v, hi_v
+    lo_v = key // N
+    hi_v = key % N
+    del key
+    # converter relabelling inside each graph: (degree, id) descending
+    deg = torch.bincount(lo_v, minlength=N) + torch.bincount(hi_v, minlength=N)
+    vgraph = torch.repeat_interleave(torch.arange(G, device=dev), ns_t)
+    local = torch.arange(N, device=dev) - goff[vgraph]
+    skey = (vgraph << 42) | (((1 << 21) - 1 - deg) << 20) | ((1 << 20) - 1 - local)
+    order = torch.argsort(skey)
+    del skey, local
+    rank = torch.empty_like(order)
+    rank[order] = torch.arange(N, device=dev)
+    new_local = rank - goff[vgraph]
+    del rank, order
+    n_new = torch.bincount(vgraph[deg > 0], minlength=G)
+    new_off = torch.zeros(G + 1, dtype=torch.int64, device=dev)
+    new_off[1:] = torch.cumsum(n_new, 0)
+    fid = new_off[vgraph] + new_local            # isolated vertices sort last in their graph
+    del new_local, vgraph, deg
+    Nn = int(new_off[-1])
+    a = fid[lo_v]
+    b = fid[hi_v]
+    del lo_v, hi_v, fid
+    rows = torch.cat([a, b])
+    cols = torch.cat([b, a])
+    del a, b
+    key = torch.sort(rows * Nn + cols).values
+    del rows, cols
+    rows = key // Nn
+    cols = key % Nn
+    del key
+    counts = torch.bincount(rows, minlength=Nn)
+    del rows
+    indices = torch.zeros(Nn + 1, dtype=torch.int64, device=dev)
+    indices[1:] = torch.cumsum(counts, 0)
+    del counts
+    cgraph = torch.repeat_interleave(torch.arange(G, device=dev), n_new)
+    adj = (cols - new_off[cgraph[cols]]).to(torch.int32)
+    del cols, cgraph
+    voff = new_off.cpu().numpy().astype(np.int32)
+    return voff, indices.to(torch.int32), adj

@@ -485,6 +485,19 @@ class Batch:
         return b
 
     @classmethod
+    def from_host_ptr(cls, ctx: Context, voff: np.ndarray, indices_ptr: int, adj_ptr: int) -> "Batch":
+        """Packed CSR already laid out in (pinned) host memory: union row
+        offsets `indices[N+1]`, local neighbour ids `adj`."""
+        voff = np.ascontiguousarray(voff, dtype=np.int32)
+        h = C.c_void_p()
+        ctx._check(LIB.pcd_batch_load(ctx.h, voff.shape[0] - 1, _ptr(voff), C.c_void_p(indices_ptr),
+                                      C.c_void_p(adj_ptr), C.byref(h)))
+        return cls(ctx, h, voff)
+
+    def get_labels_ptr(self, host_ptr: int):
+        self.ctx._check(LIB.pcd_batch_labels_get(self.h, C.c_void_p(host_ptr)))
+
+    @classmethod
     def from_device(cls, ctx: Context, voff: np.ndarray, d_indices: int, d_adj: int) -> "Batch":
         voff = np.ascontiguousarray(voff, dtype=np.int32)
         h = C.c_void_p()

@@ -259,3 +259,49 @@ def test_larger_rmat_sweeps_match_oracle(ctx, port):
         for a, b in zip(got, want):
             bad = np.nonzero(a.raw != b.raw)[0]
             assert bad.size == 0, f"{metric} s{strat} sweep {a.it}: {bad.size} differ"
+
+
+def _regular_bipartite(a, b):
+    """K_{a,b}: every vertex on a side has the same degree, so equal integer
+    keys from different (count, volume) pairs are common."""
+    rows = [[a + j for j in range(b)] for _ in range(a)] + [[i for i in range(a)] for _ in range(b)]
+    ind = np.zeros(a + b + 1, np.int32)
+    ind[1:] = np.cumsum([len(r) for r in rows])
+    return ind, np.concatenate(rows).astype(np.int32)
+
+
+def _ring_lattice(n, k):
+    rows = [sorted({(v + s) % n for s in range(-k, k + 1) if s}) for v in range(n)]
+    ind = np.zeros(n + 1, np.int32)
+    ind[1:] = np.cumsum([len(r) for r in rows])
+    return ind, np.concatenate(rows).astype(np.int32)
+
+
+@pytest.mark.parametrize("shape", ["ring-60-3", "ring-400-10", "kab-40-60", "kab-300-320"])
+def test_fp64_recheck_lists_match_oracle(ctx, port, shape):
+    """Modularity sweeps whose integer keys tie across different (count,
+    volume) pairs or equal the leave key: those vertices are re-evaluated in
+    FP64, one warp per vertex up to degree 256 and one block per vertex above
+    (kab-300-320 has degrees 300 and 320 only)."""
+    import pcd
+
+    kind, x, y = shape.split("-")
+    ind, adj = _ring_lattice(int(x), int(y)) if kind == "ring" else _regular_bipartite(int(x), int(y))
+    n = ind.shape[0] - 1
+    G = pcd.Graph.from_csr(ctx, ind, adj)
+    port.load(ind, adj)
+    rng = np.random.default_rng(21)
+    rechecked = 0
+    for trial in range(8):
+        lab = rng.integers(0, max(2, n // (2 + trial)), size=n).astype(np.int32)
+        comp, _ = port.compress(lab)
+        st = port.stats(comp)
+        seed = int(rng.integers(0, 2**31))
+        G.labels = comp
+        pcd.PropagationRefinement(1.0).refine(G, pcd.ModularityRule(), seed)
+        rechecked += G.info().fallback
+        theirs = port.refine_prop(0, 0.0, comp, 1.0, seed=seed, st=st)
+        bad = np.nonzero(G.labels != theirs)[0]
+        assert bad.size == 0, f"trial {trial}: {bad.size} vertices differ, first {bad[:6]}"
+    G.free()
+    assert rechecked > 0, "no vertex took the FP64 re-evaluation path"
