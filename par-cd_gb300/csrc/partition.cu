@@ -376,8 +376,26 @@ struct BinStore {
     }
 };
 
+// the largest degree in each class (sizes the per-class shared tables)
+__global__ void k_bin_maxdeg(const int32_t *__restrict__ indices, int32_t n, BinConfig cfg, int32_t *out) {
+    __shared__ int32_t sm[NBINS];
+    if (threadIdx.x < NBINS) sm[threadIdx.x] = 0;
+    __syncthreads();
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t d = indices[v + 1] - indices[v];
+        atomicMax(&sm[bin_of(d, cfg)], d);
+    }
+    __syncthreads();
+    if (threadIdx.x < NBINS && sm[threadIdx.x] > 0) atomicMax(&out[threadIdx.x], sm[threadIdx.x]);
+}
+
 int launch_bins(pcd_graph *g, cudaStream_t st) {
     int launches = 0;
+    int32_t *d_max = reinterpret_cast<int32_t *>(g->small);
+    cudaMemsetAsync(d_max, 0, NBINS * sizeof(int32_t), st);
+    k_bin_maxdeg<<<grid_for(g->n, 256), 256, 0, st>>>(g->indices, g->n, g->bins, d_max);
+    cudaMemcpyAsync(g->bin_maxdeg, d_max, NBINS * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    ++launches;
     g->bin_off[0] = 0;
     for (int b = 0; b < NBINS; ++b) {
         launches += scan_exclusive(BinFlag{g->indices, g->bins, b},

@@ -92,6 +92,7 @@ struct pcd_graph {
     // degree bins
     int32_t *bin_list = nullptr;          // vertices grouped by bin
     int64_t bin_off[pcd::NBINS + 1] = {0};
+    int32_t bin_maxdeg[pcd::NBINS] = {0};  // largest degree in each class
     pcd::BinConfig bins{};
     // triangles (WCC)
     int32_t *tri = nullptr, *tri_deg = nullptr;

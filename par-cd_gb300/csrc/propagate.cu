@@ -789,6 +789,264 @@ __global__ void __launch_bounds__(BT) k_prop_block(SweepArgs a, R rule, const in
 }
 
 // ---------------------------------------------------------------------------
+// Packed candidate keys for the one-pass block kernels.  A key must order
+// candidates by gain and let a plain maximum carry what the tie logic needs:
+//   Modularity (exact integer gain N): (N << 14) | k.  |N| <= 2m d <= 2^48
+//     (larger m d goes to the FP64 path first), so the shift cannot overflow,
+//     and k <= d <= 8192 fits the low 14 bits exactly.  Among keys of one
+//     gain level the maximum carries the largest k seen; a tie whose k differs
+//     from it meets a holder with another (k, volume) pair -- equal integer
+//     gain, possibly unequal FP64 gains -- and is re-evaluated in FP64.  The
+//     initial 0.0 packs as k = 0, which no real candidate has.
+//   FP64 rules: the gain itself (NaN gains are not candidates).
+// ---------------------------------------------------------------------------
+template <class R>
+struct PackedKey {
+    using K = double;
+    __device__ static K ident() { return -__longlong_as_double(0x7ff0000000000000LL); }
+    __device__ static K init() { return 0.0; }
+    __device__ static K make(typename R::Key raw, int32_t) { return raw; }
+    __device__ static double level(K x) { return x; }
+    __device__ static bool tie_ambiguous(K, K) { return false; }
+    __device__ static typename R::Key raw_level(K x) { return x; }
+};
+
+template <>
+struct PackedKey<RuleModInt> {
+    using K = long long;
+    __device__ static K ident() { return LLONG_MIN; }
+    __device__ static K init() { return 0; }
+    __device__ static K make(long long n, int32_t k) { return (long long)((unsigned long long)n << 14) | k; }
+    __device__ static long long level(K x) { return x >> 14; }
+    __device__ static bool tie_ambiguous(K c, K pre) { return ((c ^ pre) & 0x3FFF) != 0; }
+    __device__ static long long raw_level(K x) { return x >> 14; }
+};
+
+template <class K>
+__device__ __forceinline__ K kmax(K a, K b) {
+    return a > b ? a : b;
+}
+
+// ---------------------------------------------------------------------------
+// block per vertex, one keyed pass (degrees up to NW * 32 * RPL).
+//   H  histogram: labels into the shared table (label, count, first position by
+//      atomicMin); pos_slot[p] = the slot of p's label for the first lane of
+//      each warp-level match group, -1 for the others (never first positions).
+//   K  every warp owns a contiguous position range, RPL positions per lane in
+//      registers; a position is a candidate iff first[slot] == p.  Packed keys
+//      and the range maximum; one barrier, then every warp knows its carry-in
+//      (the initial 0.0 and the maxima of the ranges before it) and the final
+//      maximum.
+//   S  ordered pass over the range from the carry-in: ties with the running
+//      maximum (one rand_r draw each), FP64 ambiguity, and the final level's
+//      candidates (holder first, then its ties) compacted into the range's own
+//      consumed pos_slot entries.  The table slots are cleared here.
+//   Every warp then derives the same decision from the per-warp totals; warp
+//   0 writes it and each warp writes its share of the final-level ties.
+// ---------------------------------------------------------------------------
+template <class R, int BT, int RPL>
+__global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const int32_t *__restrict__ list,
+                                                    int64_t count, int32_t table_cap) {
+    using PK = PackedKey<R>;
+    using K = typename PK::K;
+    constexpr int NW = BT / 32;
+    extern __shared__ int32_t smem[];
+    int32_t *keys = smem;
+    int32_t *cnts = smem + table_cap;
+    uint32_t *first = reinterpret_cast<uint32_t *>(smem + 2 * table_cap);
+    int32_t *pos_slot = smem + 3 * table_cap;  // NW * 32 * RPL entries
+    __shared__ K s_agg[NW];
+    __shared__ uint32_t s_t[NW];
+    __shared__ int32_t s_nfin[NW];
+    __shared__ int32_t s_amb, s_curr_freq;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    for (int32_t i = tid; i < table_cap; i += BT) {
+        keys[i] = -1;
+        cnts[i] = 0;
+        first[i] = 0xffffffffu;
+    }
+    __syncthreads();
+    for (int64_t vi = blockIdx.x; vi < count; vi += gridDim.x) {
+        const int32_t v = list[vi];
+        const int32_t b = a.g.indices[v], d = a.g.indices[v + 1] - b;
+        const int32_t curr = a.labels[v];
+        const R vr = rule.at(v);
+        if (vr.vertex_ambiguous(d)) {
+            if (tid == 0) push_ambiguous(a, v, d);
+            continue;
+        }
+        int32_t ts = 64;
+        while (ts < 2 * d) ts <<= 1;
+        if (ts > table_cap || d > NW * 32 * RPL) {  // binned past its table: never expected
+            if (tid == 0) atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);
+            continue;
+        }
+        if (tid == 0) {
+            s_amb = 0;
+            s_curr_freq = 0;
+        }
+        // H: histogram, four gathers in flight per thread
+        for (int32_t p0 = 0; p0 < d; p0 += BT * 4) {
+            int32_t lab[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int32_t p = p0 + u * BT + tid;
+                lab[u] = p < d ? a.g.adj[b + p] : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) lab[u] = lab[u] >= 0 ? a.labels[lab[u]] : -2;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int32_t p = p0 + u * BT + tid;
+                const int32_t l = lab[u];
+                const unsigned peers = __match_any_sync(FULL, l);
+                if (p < d) {
+                    int32_t slot = -1;
+                    if (lane == __ffs(peers) - 1) {
+                        uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
+                        for (;;) {
+                            const int32_t kk = keys[h];
+                            if (kk == l) break;
+                            if (kk == -1) {
+                                const int32_t old = atomicCAS(&keys[h], -1, l);
+                                if (old == -1 || old == l) break;
+                            }
+                            h = (h + 1) & (uint32_t)(ts - 1);
+                        }
+                        atomicAdd(&cnts[h], __popc(peers));
+                        atomicMin(&first[h], (uint32_t)p);  // the leader is its group's first position
+                        slot = (int32_t)h;
+                    }
+                    pos_slot[p] = slot;
+                }
+            }
+        }
+        __syncthreads();
+        // K: candidates of this warp's range
+        const int32_t span = ((d + NW - 1) / NW + 31) & ~31;
+        const int32_t lo = min(d, wid * span), hi = min(d, lo + span);
+        K key[RPL];
+        int32_t slot[RPL], lab[RPL];
+        K wmax = PK::ident();
+#pragma unroll
+        for (int i = 0; i < RPL; ++i) {
+            const int32_t p = lo + 32 * i + lane;
+            key[i] = PK::ident();
+            slot[i] = -1;
+            lab[i] = -1;
+            if (p < hi) {
+                const int32_t h = pos_slot[p];
+                if (h >= 0 && first[h] == (uint32_t)p) {
+                    slot[i] = h;
+                    const int32_t l = keys[h], k = cnts[h];
+                    lab[i] = l;
+                    if (l == curr) {
+                        s_curr_freq = k;
+                    } else {
+                        Tag tag{0, 0};
+                        const typename R::Key raw = vr.join(v, d, l, k, a.cm, tag);
+                        if (R::usable(raw)) key[i] = PK::make(raw, k);
+                    }
+                }
+            }
+            wmax = kmax(wmax, key[i]);
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) wmax = kmax(wmax, __shfl_xor_sync(FULL, wmax, o));
+        if (lane == 0) s_agg[wid] = wmax;
+        __syncthreads();
+        K carry = PK::init(), mreal = PK::ident();
+#pragma unroll
+        for (int w2 = 0; w2 < NW; ++w2) {
+            const K x = s_agg[w2];
+            if (w2 < wid) carry = kmax(carry, x);
+            mreal = kmax(mreal, x);
+        }
+        const auto lfin = PK::level(kmax(PK::init(), mreal));
+        // S: ordered ties, final-level candidates, table clearing
+        uint32_t t = 0;
+        int32_t nfin = 0;
+        bool amb = false;
+        int32_t *fin_list = pos_slot + lo;  // this range's entries were all read in K
+#pragma unroll
+        for (int i = 0; i < RPL; ++i) {
+            if (lo + 32 * i >= hi) break;
+            if (slot[i] >= 0) {
+                keys[slot[i]] = -1;
+                cnts[slot[i]] = 0;
+                first[slot[i]] = 0xffffffffu;
+            }
+            const bool cand = key[i] != PK::ident();
+            const bool fin = cand && PK::level(key[i]) == lfin;
+            const unsigned fm = __ballot_sync(FULL, fin);
+            if (fin) fin_list[nfin + __popc(fm & lanemask_lt())] = lab[i];
+            nfin += __popc(fm);
+            if (!__any_sync(FULL, cand && PK::level(key[i]) >= PK::level(carry))) continue;
+            K inc = key[i];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const K y = __shfl_up_sync(FULL, inc, o);
+                if (lane >= o) inc = kmax(inc, y);
+            }
+            K ex = __shfl_up_sync(FULL, inc, 1);
+            if (lane == 0) ex = PK::ident();
+            const K pre = kmax(carry, ex);
+            const bool tie = cand && PK::level(key[i]) == PK::level(pre);
+            if (tie && PK::tie_ambiguous(key[i], pre)) amb = true;
+            t += __popc(__ballot_sync(FULL, tie));
+            carry = kmax(carry, __shfl_sync(FULL, inc, 31));
+        }
+        amb = __any_sync(FULL, amb);
+        if (lane == 0) {
+            s_t[wid] = t;
+            s_nfin[wid] = nfin;
+            if (amb) s_amb = 1;
+        }
+        __syncthreads();
+        // every warp: the same totals and decision
+        uint32_t tt = 0;
+        int32_t nf = 0, before = 0, hw = -1;
+#pragma unroll
+        for (int w2 = 0; w2 < NW; ++w2) {
+            const int32_t c = s_nfin[w2];
+            tt += s_t[w2];
+            if (w2 < wid) before += c;
+            if (hw < 0 && c > 0) hw = w2;
+            nf += c;
+        }
+        const bool has_best = mreal != PK::ident() && PK::level(mreal) > PK::level(PK::init());
+        // the holder is the first final-level candidate: entry 0 of the first
+        // range that has one (that range's warp has not overwritten it: only
+        // its own entries >= 0 are written, and entry 0 is the holder itself)
+        const int32_t holder = has_best ? pos_slot[hw * span] : -1;
+        const int32_t r = has_best ? nf - 1 : 0;
+        int32_t dec = DEC_AMBIGUOUS;
+        if (!s_amb) {
+            const typename R::Key best = has_best ? PK::raw_level(mreal) : R::initial();
+            dec = vr.decide(best, has_best, v, d, curr, s_curr_freq, a.cm);
+        }
+        const bool rec = dec == DEC_MOVE && r > 0;
+        if (tid == 0) {
+            if (dec == DEC_AMBIGUOUS) {
+                push_ambiguous(a, v, d);
+            } else {
+                a.ndraw[v] = tt;
+                write_decision(a, v, dec, holder, curr);
+                record_ties(a, v, b, rec, r, holder);
+            }
+        }
+        if (rec) {  // the same number of iterations in every lane
+            const long long off = (long long)b + v;  // record_ties' slots: holder, then the ties
+            for (int32_t j0 = 0; j0 < nfin; j0 += 32) {
+                const int32_t j = j0 + lane, gi = before + j;  // 0 is the holder
+                if (j < nfin && gi > 0) a.tiebuf[off + gi] = fin_list[j];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // hubs: one 512-thread block per vertex with the table in a per-block HBM
 // slice.  Random HBM traffic is what costs here, so after the histogram the
 // table is walked once in slot order: each candidate is written to
@@ -1092,21 +1350,28 @@ struct WalkStep {
     static constexpr uint32_t A1 = 1103515245u, C1 = 12345u;
     static constexpr uint32_t A2 = A1 * A1, C2 = A1 * C1 + C1;
     static constexpr uint32_t A3 = A1 * A2, C3 = A1 * C2 + C1;
-    __device__ __forceinline__ static bool step(uint32_t &x, uint32_t f, uint32_t ta, uint32_t tc) {
+    // The draw is val = hi | lo with hi = its bits 20..30; when hi differs
+    // from f's bits 20..30 (all but one case in 2048, the same in every lane)
+    // hi alone decides val <= f.
+    __device__ __forceinline__ static bool step(uint32_t &x, uint32_t f, uint32_t fhi, uint32_t ta, uint32_t tc) {
         const uint32_t s1 = (16u * A1) * x + 16u * C1;
-        const uint32_t s2 = A2 * x + C2;
         const uint32_t s3 = A3 * x + C3;
-        const uint32_t val = (s1 & 0x7FF00000u) ^ ((s2 >> 6) & 0x000FFC00u) ^ ((s3 >> 16) & 0x3FFu);
-        const bool draws = val <= f;
+        const uint32_t hi = s1 & 0x7FF00000u;
+        bool draws;
+        if (__builtin_expect(hi != fhi, 1)) {
+            draws = hi < fhi;
+        } else {
+            const uint32_t s2 = A2 * x + C2;
+            draws = (hi | ((s2 >> 6) & 0x000FFC00u) | ((s3 >> 16) & 0x3FFu)) <= f;
+        }
         x = draws ? ta * s3 + tc : s3;
         return draws;
     }
 };
 
 __global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gseed, const int32_t *voff, int32_t G,
-                                              int32_t f, int32_t n, uint32_t *ndraw,
-                                              const int32_t *__restrict__ labels, int32_t *new_labels,
-                                              int32_t *skip, DevCounters *ctr) {
+                                              int32_t f, int32_t n, uint32_t *ndraw, int32_t *skip,
+                                              DevCounters *ctr) {
     __shared__ uint32_t sh[4][3][32];
     __shared__ uint32_t jA[32], jC[32];
     if (threadIdx.x < 32) {
@@ -1117,7 +1382,7 @@ __global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gse
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const uint32_t uf = (uint32_t)f;
+    const uint32_t uf = (uint32_t)f, fhi = uf & 0x7FF00000u;
     uint32_t *st = sh[wib][0], *sa = sh[wib][1], *sc = sh[wib][2];
     for (int64_t g = warp; g < G; g += nw) {
         const int32_t v0 = voff ? voff[g] : 0, v1 = voff ? voff[g + 1] : n;
@@ -1145,7 +1410,7 @@ __global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gse
             if (v1 - c0 >= 32) {
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
-                    const bool d = WalkStep::step(x, uf, sa[j], sc[j]);
+                    const bool d = WalkStep::step(x, uf, fhi, sa[j], sc[j]);
                     pos += d ? 1u + st[j] : 1u;
                     if (lane == j) {
                         my_pos = pos;
@@ -1154,7 +1419,7 @@ __global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gse
                 }
             } else {
                 for (int j = 0; j < v1 - c0; ++j) {
-                    const bool d = WalkStep::step(x, uf, sa[j], sc[j]);
+                    const bool d = WalkStep::step(x, uf, fhi, sa[j], sc[j]);
                     pos += d ? 1u + st[j] : 1u;
                     if (lane == j) {
                         my_pos = pos;
@@ -1165,7 +1430,6 @@ __global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gse
             if (v < v1) {
                 ndraw[v] = my_pos;
                 skip[v] = my_skip;
-                if (my_skip) new_labels[v] = labels[v];
             }
         }
         if (!voff && lane == 0) ctr->total_draws = pos;
@@ -1224,13 +1488,17 @@ __global__ void k_resolve(const TieRecord *__restrict__ recs, const DevCounters 
 // redo the reservoir draws of their final level from their own slots.
 __global__ void __launch_bounds__(256) k_resolve_vertices(
     int32_t n, const int32_t *__restrict__ nties, const int32_t *__restrict__ indices,
-    const uint32_t *__restrict__ endpos, const int32_t *__restrict__ tiebuf, int32_t *out, uint32_t seed,
-    const int32_t *skip, const int32_t *__restrict__ vgid, const uint32_t *__restrict__ gseed,
+    const uint32_t *__restrict__ endpos, const int32_t *__restrict__ tiebuf, const int32_t *__restrict__ labels,
+    int32_t *out, uint32_t seed, const int32_t *skip, const int32_t *__restrict__ vgid, const uint32_t *__restrict__ gseed,
     const uint32_t *__restrict__ gbase, DevCounters *ctr) {
     int32_t replayed = 0;
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        if (skip && skip[v]) {  // no frac draw: the vertex keeps its label
+            out[v] = labels[v];
+            continue;
+        }
         const int32_t r = nties[v];
-        if (r <= 0 || (skip && skip[v])) continue;
+        if (r <= 0) continue;
         uint32_t sd = seed, bb = 0u;
         if (vgid) {
             const int32_t g = vgid[v];
@@ -1289,6 +1557,22 @@ static void launch_group(pcd_graph *g, const SweepArgs &a, const R &rule, int bi
     prof_mark(g->ctx, name, st);
 }
 
+// One-pass block kernel for a class whose largest degree is dmax: the table
+// holds 2 dmax slots rounded up to a power of two, so small classes keep many
+// blocks resident per SM.
+template <class R, int BT, int RPL>
+static void launch_block1(pcd_graph *g, const SweepArgs &a, const R &rule, const int32_t *list, int64_t c,
+                          int32_t dmax, cudaStream_t st) {
+    int32_t cap = 64;
+    while (cap < 2 * dmax) cap <<= 1;
+    const size_t smem = (3ull * cap + (size_t)BT * RPL) * sizeof(int32_t);
+    cudaFuncSetAttribute(k_prop_block1<R, BT, RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_prop_block1<R, BT, RPL>, BT, smem);
+    k_prop_block1<R, BT, RPL><<<cap_grid(c, (int64_t)g->ctx->num_sms * std::max(1, per_sm)), BT, smem, st>>>(
+        a, rule, list, c, cap);
+}
+
 template <class R, int MAXD>
 static void launch_thread(pcd_graph *g, const SweepArgs &a, const R &rule, int bin, const char *name,
                           cudaStream_t st, int *launches) {
@@ -1309,7 +1593,7 @@ static int launch_bins_rule(pcd_graph *g, const SweepArgs &a, const R &rule, cud
     launch_thread<R, 4>(g, a, rule, BIN_G4, "sweep.g4", st, &launches);
     launch_thread<R, 8>(g, a, rule, BIN_G8, "sweep.g8", st, &launches);
     launch_thread<R, 16>(g, a, rule, BIN_G16, "sweep.g16", st, &launches);
-    launch_group<R, 32>(g, a, rule, BIN_G32, "sweep.g32", st, &launches);
+    launch_thread<R, 32>(g, a, rule, BIN_G32, "sweep.g32", st, &launches);
     if ((c = g->bin_off[BIN_WARP + 1] - g->bin_off[BIN_WARP]) > 0) {
         const size_t smem = 8ull * (2 * 2 * WARP_CAP + 4 * WARP_CAP) * sizeof(int32_t);
         cudaFuncSetAttribute(k_prop_warp<R, WARP_CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1319,20 +1603,22 @@ static int launch_bins_rule(pcd_graph *g, const SweepArgs &a, const R &rule, cud
         prof_mark(g->ctx, "sweep.warp", st);
     }
     if ((c = g->bin_off[BIN_BLOCK + 1] - g->bin_off[BIN_BLOCK]) > 0) {
-        const size_t smem = (3ull * 2 * BLOCK_CAP + BLOCK_CAP) * sizeof(int32_t);
-        cudaFuncSetAttribute(k_prop_block<R, false, 256, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-        k_prop_block<R, false, 256, 4><<<cap_grid(c, sms * 4), 256, smem, st>>>(
-            a, rule, L + g->bin_off[BIN_BLOCK], c, nullptr, 2 * BLOCK_CAP, nullptr, 0, nullptr, 0);
+        const int32_t dm = std::max(1, g->bin_maxdeg[BIN_BLOCK]), *lst = L + g->bin_off[BIN_BLOCK];
+        if (dm <= 512)
+            launch_block1<R, 256, 2>(g, a, rule, lst, c, dm, st);
+        else if (dm <= 1024)
+            launch_block1<R, 256, 4>(g, a, rule, lst, c, dm, st);
+        else
+            launch_block1<R, 256, 8>(g, a, rule, lst, c, dm, st);
         ++launches;
         prof_mark(g->ctx, "sweep.block", st);
     }
     if ((c = g->bin_off[BIN_BLOCK_L + 1] - g->bin_off[BIN_BLOCK_L]) > 0) {
-        const size_t smem = (3ull * 2 * BLOCK_L_CAP + BLOCK_L_CAP) * sizeof(int32_t);
-        cudaFuncSetAttribute(k_prop_block<R, false, 512, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-        k_prop_block<R, false, 512, 4><<<cap_grid(c, sms), 512, smem, st>>>(
-            a, rule, L + g->bin_off[BIN_BLOCK_L], c, nullptr, 2 * BLOCK_L_CAP, nullptr, 0, nullptr, 0);
+        const int32_t dm = std::max(1, g->bin_maxdeg[BIN_BLOCK_L]), *lst = L + g->bin_off[BIN_BLOCK_L];
+        if (dm <= 4096)
+            launch_block1<R, 512, 8>(g, a, rule, lst, c, dm, st);
+        else
+            launch_block1<R, 512, 16>(g, a, rule, lst, c, dm, st);
         ++launches;
         prof_mark(g->ctx, "sweep.block_l", st);
     }
@@ -1413,15 +1699,15 @@ int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32
         prof_mark(g->ctx, "sweep.draw_scan", st);
     } else {
         const int32_t G = B ? B->G : 1;
-        k_walk<<<(unsigned)((G + 3) / 4), 128, 0, st>>>(seed, B ? B->gseed : nullptr, B ? B->voff : nullptr, G, f, g->n,
-                                                g->ndraw, g->labels, g->labels_alt, g->first, g->ctr);
+        k_walk<<<(unsigned)((G + 3) / 4), 128, 0, st>>>(seed, B ? B->gseed : nullptr, B ? B->voff : nullptr, G, f,
+                                                         g->n, g->ndraw, g->first, g->ctr);
         if (B) cudaMemsetAsync(B->gbase, 0, sizeof(uint32_t) * B->G, st);
         skip = g->first;
         ++launches;
         prof_mark(g->ctx, "sweep.draw_walk", st);
     }
     k_resolve_vertices<<<g->ctx->num_sms * 8, 256, 0, st>>>(g->n, g->nties, g->indices, g->ndraw, g->tiebuf,
-                                                           g->labels_alt, seed, skip, B ? B->vgid : nullptr,
+                                                           g->labels, g->labels_alt, seed, skip, B ? B->vgid : nullptr,
                                                            B ? B->gseed : nullptr, B ? B->gbase : nullptr, g->ctr);
     ++launches;
     if (B) {
