@@ -591,7 +591,8 @@ def main():
             "gpu_launches": int(launches),
             "clocks": clk,
             "phases_ms": {nm: round(ms, 4) for nm, ms in phases},
-            "per_sweep_ms": [round(statistics.mean(sweep_ms[j::args.sweeps]), 3) for j in range(args.sweeps)],
+            "per_sweep_ms": [round(statistics.mean(sweep_ms[j::args.sweeps]), 3)
+                             for j in range(min(args.sweeps, len(sweep_ms)))],
             "bins": bins_now,
             "sweep_info": {"draws": info.draws, "fp64_recheck_vertices": info.fallback,
                            "tie_replays": info.resolved},

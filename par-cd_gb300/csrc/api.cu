@@ -95,9 +95,11 @@ pcd_status sync_and_check(pcd_graph *g) {
     int32_t err = g->h_ctr->error;
     if (err) {
         char buf[160];
-        snprintf(buf, sizeof buf, "device error flags 0x%x (1 tie buffer, 2 wait limit, 4 scratch, 8 label range)",
-                 (unsigned)err);
+        snprintf(buf, sizeof buf,
+                 "device error flags 0x%x (1 tie buffer, 2 wait limit, 4 scratch, 8 label range, 16 check 0x%x)",
+                 (unsigned)err, (unsigned)g->h_ctr->check_where);
         cudaMemsetAsync(&g->ctr->error, 0, sizeof(int32_t), ctx->stream);
+        cudaMemsetAsync(&g->ctr->check_where, 0, sizeof(int32_t), ctx->stream);
         cudaStreamSynchronize(ctx->stream);
         pcd_status s = (err & ERR_WAIT_TIMEOUT) ? PCD_ERR_DEVICE_TIMEOUT
                        : (err & ERR_LABEL_RANGE) ? PCD_ERR_INVALID_ARGUMENT

@@ -16,6 +16,8 @@ struct DevCounters {
     int32_t n_pairs;              // contracted pairs (merge)
     int32_t all_found;            // merge: every community matched
     int32_t n_amb_large;          // of those, vertices of degree > 256 (queued from the list's end)
+    int32_t check_where;          // bits of failed internal consistency checks (ERR_CHECK)
+    int32_t pad;
 };
 
 enum : int32_t {
@@ -23,6 +25,7 @@ enum : int32_t {
     ERR_WAIT_TIMEOUT = 2,
     ERR_SCRATCH_OVERFLOW = 4,
     ERR_LABEL_RANGE = 8,
+    ERR_CHECK = 16,
 };
 
 // A vertex (or community) whose winner is picked by replaying its final

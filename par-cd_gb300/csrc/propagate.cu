@@ -1499,6 +1499,11 @@ __global__ void __launch_bounds__(256) k_resolve_vertices(
         }
         const int32_t r = nties[v];
         if (r <= 0) continue;
+        if (r > indices[v + 1] - indices[v]) {  // more ties than neighbours: an internal error
+            atomicOr(&ctr->check_where, 32);
+            atomicOr(&ctr->error, ERR_CHECK);
+            continue;
+        }
         uint32_t sd = seed, bb = 0u;
         if (vgid) {
             const int32_t g = vgid[v];
@@ -1529,6 +1534,7 @@ __global__ void k_reset_sweep(DevCounters *ctr) {
     ctr->n_resolve = 0;
     ctr->n_ambiguous = 0;
     ctr->n_amb_large = 0;
+    ctr->check_where = 0;
     ctr->error = 0;
     ctr->total_draws = 0;
 }
