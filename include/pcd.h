@@ -102,6 +102,24 @@ pcd_status pcd_graph_free(pcd_graph *g);
 pcd_status pcd_graph_set_bins(pcd_graph *g, const int32_t max_deg[7]);
 pcd_status pcd_graph_get_bins(pcd_graph *g, int32_t max_deg[7], int64_t counts[8]);
 
+/* Device memory a graph or batch holds right now (every buffer libpcd
+ * allocated for it, merge buffers and seed tables included).  No counterpart
+ * in the reference (its device buffers come from one global allocator,
+ * framework-cuda.cu:14). */
+pcd_status pcd_graph_device_bytes(pcd_graph *g, int64_t *bytes);
+
+/* Upper bound of the device memory that loading and running a graph (or a
+ * packed batch of num_graphs graphs with n vertices and nnz adjacency entries
+ * in all) needs at its peak, from sizes known before loading: the largest
+ * degree, the number of vertices above 8192 neighbours, the iteration cap of
+ * pcd_batch_run (n_iter, or 1000 in threshold mode), whether merges run, and
+ * the device's SM count.  Used for HBM admission in the serving loop. */
+pcd_status pcd_estimate_device_bytes(int32_t n, int64_t nnz, int32_t max_deg, int64_t num_hubs, int32_t num_graphs,
+                                     int32_t iteration_cap, int32_t merges, int32_t num_sms, int64_t *bytes);
+
+/* SM count of the context's device. */
+pcd_status pcd_device_sm_count(pcd_ctx *ctx, int32_t *sms);
+
 /* cuda_labels_to_device / cuda_labels_from_device
  * (src/framework-cuda.cu:135-143).  Host arrays of n labels. */
 pcd_status pcd_labels_set(pcd_graph *g, const int32_t *labels);

@@ -32,6 +32,7 @@ pcd_status dev_alloc(pcd_graph *g, void **p, size_t bytes) {
         return check_cuda(g->ctx, e, "cudaMalloc");
     }
     g->allocs.push_back(*p);
+    g->dev_bytes += bytes;
     return PCD_OK;
 }
 
@@ -204,8 +205,10 @@ pcd_status pcd_graph_free(pcd_graph *g) {
     if (ctx && ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (void *p : g->allocs)
         if (p) cudaFree(p);
+    if (g->hub_scratch) cudaFree(g->hub_scratch);
     if (g->merge_buf) cudaFree(g->merge_buf);
     if (g->h_ctr) cudaFreeHost(g->h_ctr);
+    if (g->batch && g->batch->seed_table) cudaFree(g->batch->seed_table);
     delete g->batch;
     if (ctx) ctx->graphs.erase(std::remove(ctx->graphs.begin(), ctx->graphs.end(), g), ctx->graphs.end());
     delete g;
@@ -260,6 +263,39 @@ int32_t pcd_profile_read(pcd_ctx *ctx, const char **names, double *ms, int32_t c
 pcd_status pcd_synchronize(pcd_ctx *ctx) {
     if (!ctx || !ctx->stream) return PCD_ERR_INVALID_ARGUMENT;
     CK(cudaStreamSynchronize(ctx->stream), "pcd_synchronize");
+    return PCD_OK;
+}
+
+// Hub tables: one HBM slice per block, as many blocks as there are hub vertices
+// (at most one per SM); grown when the degree classes change.  Slices start
+// empty (keys -1, counts 0, first positions 0xffffffff) and the hub kernel
+// leaves them empty.
+static pcd_status ensure_hub_scratch(pcd_graph *g) {
+    pcd_ctx *ctx = g->ctx;
+    const int64_t hubs = g->bin_off[NBINS] - g->bin_off[BIN_HUB];
+    const int32_t want = (int32_t)std::min<int64_t>(ctx->num_sms, hubs);
+    if (want <= g->hub_blocks) return PCD_OK;
+    const int64_t slots = g->fb_slots, stride = 3 * slots + 2ll * g->max_deg;
+    cudaStream_t st = ctx->stream;
+    CK(cudaStreamSynchronize(st), "hub scratch");
+    if (g->hub_scratch) {
+        cudaFree(g->hub_scratch);
+        g->dev_bytes -= g->hub_bytes;
+    }
+    g->hub_scratch = nullptr;
+    g->hub_blocks = 0;
+    g->hub_bytes = 0;
+    const size_t bytes = sizeof(int32_t) * (size_t)(stride * want);
+    CK(cudaMalloc((void **)&g->hub_scratch, bytes), "hub scratch");
+    for (int32_t bk = 0; bk < want; ++bk) {
+        int32_t *base = g->hub_scratch + (int64_t)bk * stride;
+        CK(cudaMemsetAsync(base, 0xff, sizeof(int32_t) * (size_t)slots, st), "hub scratch");
+        CK(cudaMemsetAsync(base + slots, 0, sizeof(int32_t) * (size_t)slots, st), "hub scratch");
+        CK(cudaMemsetAsync(base + 2 * slots, 0xff, sizeof(int32_t) * (size_t)slots, st), "hub scratch");
+    }
+    g->hub_blocks = want;
+    g->hub_bytes = bytes;
+    g->dev_bytes += bytes;
     return PCD_OK;
 }
 
@@ -324,19 +360,10 @@ static pcd_status graph_setup(pcd_ctx *ctx, pcd_graph *g) {
         CK(cudaMemsetAsync(base + slots, 0, sizeof(int32_t) * (size_t)slots, st), "fallback scratch");
         CK(cudaMemsetAsync(base + 2 * slots, 0xff, sizeof(int32_t) * (size_t)slots, st), "fallback scratch");
     }
-    // hub slices: the same tables plus labels and counts by position
-    const int64_t hub_stride = 3 * slots + 2ll * g->max_deg;
-    g->hub_blocks = (int32_t)std::min<int64_t>(ctx->num_sms, std::max<int64_t>(8, (int64_t)(4ll << 30) / (4 * hub_stride)));
-    TRY(dev_alloc(g, (void **)&g->hub_scratch, sizeof(int32_t) * (size_t)(hub_stride * g->hub_blocks)));
-    for (int32_t bk = 0; bk < g->hub_blocks; ++bk) {
-        int32_t *base = g->hub_scratch + (int64_t)bk * hub_stride;
-        CK(cudaMemsetAsync(base, 0xff, sizeof(int32_t) * (size_t)slots, st), "hub scratch");
-        CK(cudaMemsetAsync(base + slots, 0, sizeof(int32_t) * (size_t)slots, st), "hub scratch");
-        CK(cudaMemsetAsync(base + 2 * slots, 0xff, sizeof(int32_t) * (size_t)slots, st), "hub scratch");
-    }
-    // degree bins
+    // degree bins, then the hub slices (the same tables plus labels and counts by position)
     g->bins = BinConfig{{4, 8, 16, 32, 256, 2048, 8192}};
     if (n > 0) launch_bins(g, st);
+    TRY(ensure_hub_scratch(g));
     // initial labels: singletons 0..n-1 (already compressed)
     g->k = g->n;
     g->compressed = false;
@@ -378,6 +405,7 @@ static pcd_status load_common(pcd_ctx *ctx, int32_t n, int32_t m, const int32_t 
     if (s != PCD_OK) {
         for (void *p : g->allocs)
             if (p) cudaFree(p);
+        if (g->hub_scratch) cudaFree(g->hub_scratch);
         if (g->h_ctr) cudaFreeHost(g->h_ctr);
         delete g;
         return s;
@@ -397,6 +425,51 @@ pcd_status pcd_load_csr_device(pcd_ctx *ctx, int32_t n, int32_t m, const int32_t
     return load_common(ctx, n, m, d_indices, d_adj, cudaMemcpyDeviceToDevice, out);
 }
 
+pcd_status pcd_device_sm_count(pcd_ctx *ctx, int32_t *sms) {
+    if (!ctx || !sms) return PCD_ERR_INVALID_ARGUMENT;
+    *sms = ctx->num_sms;
+    return PCD_OK;
+}
+
+pcd_status pcd_graph_device_bytes(pcd_graph *g, int64_t *bytes) {
+    if (!g || !bytes) return PCD_ERR_INVALID_ARGUMENT;
+    int64_t b = (int64_t)g->dev_bytes + (int64_t)g->merge_bytes;
+    if (g->batch) b += 4ll * g->batch->seed_iters * g->batch->G;
+    *bytes = b;
+    return PCD_OK;
+}
+
+// Upper bound of what pcd_batch_load + pcd_batch_run (or pcd_load_csr and the
+// phase calls, num_graphs = 1) hold on the device at their peak, from sizes
+// the caller knows before loading.  Mirrors the allocations of graph_setup,
+// ensure_hub_scratch, batch_setup, the batch staging copies, the seed table
+// of pcd_batch_run (iteration cap) and the merge buffers.
+pcd_status pcd_estimate_device_bytes(int32_t n, int64_t nnz, int32_t max_deg, int64_t num_hubs, int32_t num_graphs,
+                                     int32_t iteration_cap, int32_t merges, int32_t num_sms, int64_t *bytes) {
+    if (!bytes || n < 0 || nnz < 0 || max_deg < 0 || num_hubs < 0 || num_graphs < 1 || num_sms < 1)
+        return PCD_ERR_INVALID_ARGUMENT;
+    const int64_t nn = std::max<int64_t>(n, 1), e = std::max<int64_t>(nnz, 1), G = num_graphs;
+    int64_t b = 4 * (nn + 1) + 4 * e;                                                  // CSR
+    b += 60 * nn;                                                                      // per-vertex state
+    b += 4 * ((std::max<int64_t>({nn, e, 512ll * num_sms}) + 2047) / 2048 + 2) + 16;  // scan tiles
+    b += 4 * (e + nn + 16);                                                            // tie slots
+    b += 8 * nn;                                                                       // triangles (WCC)
+    b += 65536 + 64 + 64 + 256;                                                        // counters, reductions
+    int64_t slots = 64;
+    while (slots < 2 * (int64_t)std::max(max_deg, 1)) slots <<= 1;
+    const int64_t fb_stride = 3 * slots + max_deg;
+    b += 4 * fb_stride * std::min<int64_t>(8, std::max<int64_t>(1, (1ll << 29) / (4 * fb_stride)));
+    b += 4 * (3 * slots + 2ll * max_deg) * std::min<int64_t>(num_sms, num_hubs);
+    // batch state, the staging copies of a batch load, the seed table of a run
+    b += 8 * nn + 8 * (G + 1) + 52 * G + 64;
+    b += 4 * (nn + 1) + 4 * e + 8 + 4 * (G + 1) + 4 * nn;
+    b += 4 * G * std::max(iteration_cap, 1) + 12 * G + 64;
+    if (merges) b += 60 * e + 24 * nn + 4 + 1024ll * 2 * num_sms + 256 * 21;
+    b += 40 * 512;  // allocation granularity
+    *bytes = b;
+    return PCD_OK;
+}
+
 pcd_status pcd_graph_set_bins(pcd_graph *g, const int32_t max_deg[7]) {
     if (!g || !max_deg) return PCD_ERR_INVALID_ARGUMENT;
     static const int32_t cap[7] = {4, 8, 16, 32, 256, 2048, 8192};
@@ -408,6 +481,7 @@ pcd_status pcd_graph_set_bins(pcd_graph *g, const int32_t max_deg[7]) {
     CK(cudaStreamSynchronize(ctx->stream), "set_bins");
     for (int i = 0; i < 7; ++i) g->bins.max_deg[i] = max_deg[i];
     if (g->n > 0) launch_bins(g, ctx->stream);
+    TRY(ensure_hub_scratch(g));
     return check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "set_bins");
 }
 

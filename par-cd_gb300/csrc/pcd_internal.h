@@ -89,6 +89,8 @@ struct pcd_graph {
     // hub tables: the same layout, one slice per hub block
     int32_t *hub_scratch = nullptr;
     int32_t hub_blocks = 0;
+    size_t hub_bytes = 0;
+    size_t dev_bytes = 0;             // device memory held through dev_alloc and the hub slices
     // degree bins
     int32_t *bin_list = nullptr;          // vertices grouped by bin
     int64_t bin_off[pcd::NBINS + 1] = {0};
