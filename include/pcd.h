@@ -218,6 +218,63 @@ pcd_status pcd_batch_run(pcd_graph *batch, const pcd_rule *rule, int32_t strateg
                          int32_t rounds, int32_t n_iter, double threshold, int32_t use_cuda_graph,
                          double *scores, int32_t *iterations);
 
+/* ------------------------------------------------------------------------
+ * Serving loop.  No counterpart in the reference (its drivers run one graph
+ * per process, src/main.cpp).  Requests -- a graph and a driver schedule --
+ * queue in arrival order; `workers` threads, each with its own context and
+ * stream, take batches of requests that share a schedule (at most
+ * max_batch_graphs graphs and max_batch_edges adjacency entries) and run them
+ * with pcd_batch_run, so batches of different workers overlap on the GPU.  A
+ * batch is admitted only while the device memory of every batch in flight,
+ * counted with pcd_estimate_device_bytes, stays within hbm_budget_bytes; a
+ * request that alone exceeds the budget fails with PCD_ERR_OUT_OF_MEMORY.  A
+ * batch smaller than max_batch_graphs starts once its oldest request has
+ * waited max_wait_ms.  Every graph gets exactly its result alone.
+ * ------------------------------------------------------------------------ */
+typedef struct pcd_server pcd_server;
+typedef struct pcd_schedule {
+    pcd_rule rule;      /* Modularity or CPM (WCC needs the clustering start) */
+    int32_t strategy;   /* -s: 0 propagation, 1 merging, 2 alternate          */
+    double frac;        /* -f                                                 */
+    int32_t rounds;     /* -r                                                 */
+    int32_t n_iter;     /* -n, or -1: stop on -t threshold                    */
+    double threshold;   /* -t                                                 */
+} pcd_schedule;
+typedef struct pcd_serve_config {
+    int32_t device;
+    int32_t workers;
+    int32_t max_batch_graphs;
+    int64_t max_batch_edges;
+    int64_t hbm_budget_bytes;
+    double max_wait_ms;
+    int32_t use_cuda_graph;  /* passed to pcd_batch_run */
+} pcd_serve_config;
+typedef struct pcd_serve_stats {
+    int64_t submitted, completed, failed, batches, batched_graphs, queue_len;
+    int64_t bytes_in_flight;     /* estimated bytes of the batches running now */
+    int64_t bytes_peak;          /* largest estimated total in flight so far   */
+    int64_t bytes_measured_peak; /* largest pcd_graph_device_bytes of a batch  */
+    int64_t estimate_exceeded;   /* batches that held more than their estimate */
+} pcd_serve_stats;
+typedef struct pcd_serve_timing {
+    double queue_ms;        /* submit -> its batch started */
+    double latency_ms;      /* submit -> result ready      */
+    int64_t batch_graphs;   /* graphs in its batch          */
+} pcd_serve_timing;
+pcd_status pcd_serve_start(const pcd_serve_config *cfg, pcd_server **out);
+/* Copies the graph (host CSR, checked here) and queues it; returns at once. */
+pcd_status pcd_serve_submit(pcd_server *s, int32_t n, int32_t m, const int32_t *indices, const int32_t *adj,
+                            const pcd_schedule *sched, uint64_t *ticket);
+pcd_status pcd_serve_poll(pcd_server *s, uint64_t ticket, int32_t *done);
+/* Blocks until the request is done and releases its ticket; labels: n host
+ * int32 (may be NULL); returns the request's own status. */
+pcd_status pcd_serve_wait(pcd_server *s, uint64_t ticket, int32_t *labels, double *score, int32_t *iterations,
+                          pcd_serve_timing *timing);
+pcd_status pcd_serve_stats_get(pcd_server *s, pcd_serve_stats *out);
+/* Runs what is queued, stops the workers, frees the server (no call may use
+ * it afterwards, including pending waits). */
+pcd_status pcd_serve_stop(pcd_server *s);
+
 /* compress_labels on caller-owned device buffers, with no device allocation.
  * No counterpart in the reference: it exists for callers that cannot call
  * cudaMalloc where they relabel (inside another framework's memory arena,

@@ -21,7 +21,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpcd.so")
 MAIN = os.path.join(HERE, "main-cuda")
-SOURCES = ["api.cu", "partition.cu", "propagate.cu", "merge.cu", "triangles.cu", "batch.cu", "noalloc.cu", "hostside.cpp"]
+SOURCES = ["api.cu", "partition.cu", "propagate.cu", "merge.cu", "triangles.cu", "batch.cu", "noalloc.cu", "hostside.cpp", "serve.cpp"]
 HEADERS = ["pcd_device.cuh", "pcd_scan.cuh", "pcd_internal.h", "pcd_types.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -58,7 +58,8 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
     def compile_one(job):
         s, o = job
         if s.endswith(".cpp"):
-            cmd = ["g++", "-c", s, "-o", o, "-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fno-fast-math"]
+            cmd = ["g++", "-c", s, "-o", o, "-O2", "-fPIC", "-std=c++17", "-pthread", "-ffp-contract=off",
+                   "-fno-fast-math", "-I", os.path.join(HERE, "..", "include")]
         else:
             cmd = [nvcc(), "-c", s, "-o", o] + flags(extra)
         if verbose:
@@ -75,7 +76,7 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
                     print(msg)
     objs = [os.path.join(BUILD, os.path.splitext(s)[0] + ".o") for s in SOURCES]
     if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc(), "-shared", "-o", LIB] + objs + ARCH + ["-Xcompiler", "-fPIC"]
+        cmd = [nvcc(), "-shared", "-o", LIB] + objs + ARCH + ["-Xcompiler", "-fPIC,-pthread", "-lpthread"]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.run(cmd, check=True)
