@@ -46,6 +46,27 @@ class _Rand(C.Structure):
     _fields_ = [("r", C.c_uint32 * 34), ("pos", C.c_int32)]
 
 
+class _Schedule(C.Structure):
+    _fields_ = [("rule", _Rule), ("strategy", C.c_int32), ("frac", C.c_double), ("rounds", C.c_int32),
+                ("n_iter", C.c_int32), ("threshold", C.c_double)]
+
+
+class _ServeConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("workers", C.c_int32), ("max_batch_graphs", C.c_int32),
+                ("max_batch_edges", C.c_int64), ("hbm_budget_bytes", C.c_int64), ("max_wait_ms", C.c_double),
+                ("use_cuda_graph", C.c_int32)]
+
+
+class _ServeStats(C.Structure):
+    _fields_ = [(nm, C.c_int64) for nm in ("submitted", "completed", "failed", "batches", "batched_graphs",
+                                           "queue_len", "bytes_in_flight", "bytes_peak", "bytes_measured_peak",
+                                           "estimate_exceeded")]
+
+
+class _ServeTiming(C.Structure):
+    _fields_ = [("queue_ms", C.c_double), ("latency_ms", C.c_double), ("batch_graphs", C.c_int64)]
+
+
 def _load() -> C.CDLL:
     if not os.path.exists(LIB_PATH):
         raise ImportError(f"libpcd.so is not built ({LIB_PATH}); run par-cd_gb300/build.py")
@@ -88,6 +109,15 @@ def _load() -> C.CDLL:
         "pcd_batch_merge": ([vp, C.POINTER(_Rule), i32, vp], i32),
         "pcd_batch_run": ([vp, C.POINTER(_Rule), i32, dbl, i32, i32, dbl, i32, vp, vp], i32),
         "pcd_compress_labels_noalloc": ([vp, i32, vp, vp, vp], i32),
+        "pcd_graph_device_bytes": ([vp, C.POINTER(i64)], i32),
+        "pcd_estimate_device_bytes": ([i32, i64, i32, i64, i32, i32, i32, i32, C.POINTER(i64)], i32),
+        "pcd_device_sm_count": ([vp, C.POINTER(i32)], i32),
+        "pcd_serve_start": ([C.POINTER(_ServeConfig), C.POINTER(vp)], i32),
+        "pcd_serve_submit": ([vp, i32, i32, vp, vp, C.POINTER(_Schedule), C.POINTER(C.c_uint64)], i32),
+        "pcd_serve_poll": ([vp, C.c_uint64, C.POINTER(i32)], i32),
+        "pcd_serve_wait": ([vp, C.c_uint64, vp, C.POINTER(dbl), C.POINTER(i32), C.POINTER(_ServeTiming)], i32),
+        "pcd_serve_stats_get": ([vp, C.POINTER(_ServeStats)], i32),
+        "pcd_serve_stop": ([vp], i32),
         "pcd_rand_seed": ([C.POINTER(_Rand), u32], None),
         "pcd_rand_next": ([C.POINTER(_Rand)], i32),
         "pcd_rand_skip": ([C.POINTER(_Rand), i64], None),
@@ -549,3 +579,91 @@ class Batch:
         self.ctx._check(LIB.pcd_batch_run(self.h, C.byref(rule._c()), strategy, float(frac), rounds, n_iter,
                                           float(threshold), 1 if cuda_graph else 0, _ptr(scores), _ptr(iters)))
         return scores, iters
+
+
+# ---------------------------------------------------------------------------
+# serving loop
+# ---------------------------------------------------------------------------
+def estimate_device_bytes(n: int, nnz: int, max_deg: int, num_hubs: int = 0, num_graphs: int = 1,
+                          iteration_cap: int = 1000, merges: bool = False, num_sms: int = 152) -> int:
+    """Upper bound of the device memory a (batch) load and run needs
+    (pcd_estimate_device_bytes)."""
+    out = C.c_int64()
+    st = LIB.pcd_estimate_device_bytes(int(n), int(nnz), int(max_deg), int(num_hubs), int(num_graphs),
+                                       int(iteration_cap), 1 if merges else 0, int(num_sms), C.byref(out))
+    if st:
+        raise PcdError(st, "pcd_estimate_device_bytes")
+    return out.value
+
+
+@dataclass
+class ServeResult:
+    labels: np.ndarray
+    score: float
+    iterations: int
+    latency_ms: float
+    queue_ms: float
+    batch_graphs: int
+
+
+class Server:
+    """Requests served in batches by worker threads (pcd_serve_* in
+    include/pcd.h).  submit() copies the graph and returns a ticket; wait()
+    blocks for that ticket's result."""
+
+    def __init__(self, device: int = 0, workers: int = 2, max_batch_graphs: int = 256,
+                 max_batch_edges: int = 1 << 30, hbm_budget_bytes: int = 150 * 10**9, max_wait_ms: float = 2.0,
+                 cuda_graph: bool = False):
+        cfg = _ServeConfig(device, workers, max_batch_graphs, max_batch_edges, hbm_budget_bytes, max_wait_ms,
+                           1 if cuda_graph else 0)
+        self.h = C.c_void_p()
+        st = LIB.pcd_serve_start(C.byref(cfg), C.byref(self.h))
+        if st:
+            raise PcdError(st, "pcd_serve_start")
+        self._n = {}
+
+    def submit(self, indices, adj, rule: Rule, strategy: int = 0, frac: float = 1.0, rounds: int = 1,
+               n_iter: int = -1, threshold: float = 0.0) -> int:
+        ind = _i32(indices)
+        a = _i32(adj)
+        sched = _Schedule(rule._c(), strategy, float(frac), rounds, n_iter, float(threshold))
+        t = C.c_uint64()
+        st = LIB.pcd_serve_submit(self.h, ind.shape[0] - 1, a.shape[0] // 2, _ptr(ind), _ptr(a), C.byref(sched),
+                                  C.byref(t))
+        if st:
+            raise PcdError(st, "pcd_serve_submit")
+        self._n[t.value] = ind.shape[0] - 1
+        return t.value
+
+    def done(self, ticket: int) -> bool:
+        d = C.c_int32()
+        st = LIB.pcd_serve_poll(self.h, C.c_uint64(ticket), C.byref(d))
+        if st:
+            raise PcdError(st, "pcd_serve_poll")
+        return bool(d.value)
+
+    def wait(self, ticket: int) -> ServeResult:
+        lab = np.empty(self._n.pop(ticket), np.int32)
+        score = C.c_double()
+        it = C.c_int32()
+        tm = _ServeTiming()
+        st = LIB.pcd_serve_wait(self.h, C.c_uint64(ticket), _ptr(lab), C.byref(score), C.byref(it), C.byref(tm))
+        if st:
+            raise PcdError(st, f"request {ticket}")
+        return ServeResult(lab, score.value, it.value, tm.latency_ms, tm.queue_ms, tm.batch_graphs)
+
+    def stats(self) -> dict:
+        out = _ServeStats()
+        LIB.pcd_serve_stats_get(self.h, C.byref(out))
+        return {nm: getattr(out, nm) for nm, _ in _ServeStats._fields_}
+
+    def stop(self):
+        if self.h:
+            LIB.pcd_serve_stop(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.stop()
