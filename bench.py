@@ -360,6 +360,121 @@ def batched_leg(args, ctx, dev):
     }
 
 
+def serve_pool(dev):
+    """The served mix's graphs (seed 5): SBMs with log-uniform sizes in
+    [1000, 50000] (n/50 blocks, intra-degree 12, inter-degree 2), LFR-style
+    power-law graphs (degree exponent 2.5 in [8, 5000], community sizes 1.5 in
+    [20, 20000], mu 0.3) and one R-MAT scale 22; host CSR arrays."""
+    import numpy as np
+    import torch
+
+    import graphs
+
+    rng = np.random.default_rng(5)
+    ns = np.rint(np.exp(rng.uniform(np.log(1000), np.log(50000), 64))).astype(np.int64)
+    voff, ind, adj = graphs.sbm_batch_torch(len(ns), seed=5, device=dev, sizes=ns)
+    sbm = graphs.unpack(voff, ind.cpu().numpy(), adj.cpu().numpy())
+    pl = []
+    for k, n in enumerate((100_000, 250_000, 600_000)):
+        e = graphs.powerlaw(n, 2.5, 8, 5000, 1.5, 20, 20000, 0.3, seed=50 + k)
+        i, a, _ = graphs.csr_from_edges_torch(torch.from_numpy(e[:, 0]).to(dev), torch.from_numpy(e[:, 1]).to(dev), n)
+        pl.append((i, a))
+    i, a, _ = graphs.rmat_torch(22, 16, 0.57, 0.19, 0.19, seed=5, device=dev)
+    torch.cuda.empty_cache()
+    return sbm, pl, [(i, a)]
+
+
+def served_leg(args, dev):
+    """Requests arrive as a Poisson stream (seed 5): 90% SBM, 9% power-law, 1%
+    R-MAT s22, each Modularity or CPM(0.01) with the reference's default stop
+    test (-s 0 -t 0, frac 1.0).  Served: pcd.Server (batches under a 150 GB
+    HBM budget).  Plain: the same requests in arrival order through the
+    single-graph path, one at a time (FIFO queue: latency = wait + service).
+    Every served result must equal the plain one."""
+    import numpy as np
+
+    import pcd
+
+    t0 = time.time()
+    sbm, pl, rm = serve_pool(dev)
+    log(f"[bench] serve pool: {len(sbm)} SBM, {len(pl)} power-law, {len(rm)} R-MAT s22 ({time.time() - t0:.1f}s)")
+    rng = np.random.default_rng(5)
+    reqs = []
+    for _ in range(args.serve_requests):
+        u = rng.random()
+        pool = sbm if u < 0.90 else (pl if u < 0.99 else rm)
+        g = pool[int(rng.integers(len(pool)))]
+        reqs.append((g, "mod" if rng.random() < 0.5 else "cpm-0.01"))
+    gaps = rng.exponential(1.0, size=len(reqs))
+    edges = sum(len(g[1]) // 2 for g, _ in reqs)
+
+    # plain: service times, one request after another
+    ctx = pcd.Context(int(str(dev).split(":")[-1]) if ":" in str(dev) else 0)
+    plain = []
+    for g, metric in reqs[:3]:  # warm-up
+        G = pcd.Graph.from_csr(ctx, g[0], g[1])
+        pcd.run(G, pcd.parse_metric(metric), 0, 1.0, 1, -1, 0.0, 0)
+        G.free()
+    for g, metric in reqs:
+        t = time.perf_counter()
+        G = pcd.Graph.from_csr(ctx, g[0], g[1])
+        res = pcd.run(G, pcd.parse_metric(metric), 0, 1.0, 1, -1, 0.0, 0)
+        G.free()
+        plain.append((time.perf_counter() - t, res))
+    ctx.close()
+    service = np.array([p[0] for p in plain])
+
+    def pct(x):
+        return {k: round(float(np.percentile(x, q)) * 1000.0, 3) for k, q in (("p50", 50), ("p90", 90), ("p99", 99))} | \
+               {"max": round(float(np.max(x)) * 1000.0, 3)}
+
+    out = {"requests": len(reqs), "edges": int(edges),
+           "mix": "90% SBM n~LogUniform[1e3, 5e4] (64-graph pool), 9% power-law n in {1e5, 2.5e5, 6e5}, "
+                  "1% R-MAT s22; mod or cpm-0.01 each with p 1/2; -s 0 -f 1.0 -t 0 from singletons",
+           "hbm_budget_bytes": 150 * 10**9, "rates": []}
+    for rate in args.serve_rates:
+        arrival = np.cumsum(gaps / rate)
+        # plain FIFO queue
+        fin = np.zeros(len(reqs))
+        prev = 0.0
+        for k in range(len(reqs)):
+            prev = max(arrival[k], prev) + service[k]
+            fin[k] = prev
+        plain_lat = fin - arrival
+        with pcd.Server(device=0, workers=args.serve_workers, max_batch_graphs=256,
+                        hbm_budget_bytes=150 * 10**9, max_wait_ms=2.0) as srv:
+            tickets = []
+            start = time.perf_counter()
+            for k, (g, metric) in enumerate(reqs):
+                delay = start + arrival[k] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                tickets.append(srv.submit(g[0], g[1], pcd.parse_metric(metric), 0, 1.0, 1, -1, 0.0))
+            lat, same = [], 0
+            for k, t in enumerate(tickets):
+                r = srv.wait(t)
+                lat.append(r.latency_ms / 1000.0)
+                p = plain[k][1]
+                same += int(np.array_equal(r.labels, p.labels) and r.score == p.score and r.iterations == p.iterations)
+            wall = time.perf_counter() - start
+            st = srv.stats()
+        assert same == len(reqs), f"{len(reqs) - same} served results differ from the plain path"
+        lat = np.array(lat)
+        out["rates"].append({
+            "arrival_rate": rate,
+            "served": {"graphs_per_s": len(reqs) / wall, "latency_ms": pct(lat), "batches": st["batches"],
+                       "mean_batch_graphs": st["batched_graphs"] / max(1, st["batches"]),
+                       "hbm_peak_estimated_bytes": st["bytes_peak"], "hbm_batch_measured_peak_bytes":
+                           st["bytes_measured_peak"], "estimate_exceeded": st["estimate_exceeded"]},
+            "plain": {"graphs_per_s": len(reqs) / float(fin[-1]), "latency_ms": pct(plain_lat)},
+            "identical_to_plain": True,
+        })
+        log(f"[bench] served at {rate}/s: {out['rates'][-1]['served']['graphs_per_s']:.0f} graphs/s, "
+            f"p99 {out['rates'][-1]['served']['latency_ms']['p99']} ms (plain p99 "
+            f"{out['rates'][-1]['plain']['latency_ms']['p99']} ms)")
+    return out
+
+
 def workload_config(args, n, m):
     return {
         "workload": f"rmat-s{args.scale}-ef{args.edge_factor} (a,b,c,d)=(.57,.19,.19,.05) seed 2, degree-sorted; "
@@ -392,6 +507,9 @@ def main():
     ap.add_argument("--batch-frac", type=float, default=0.5)
     ap.add_argument("--batch-iters", type=int, default=-1)
     ap.add_argument("--batch-threshold", type=float, default=0.0)
+    ap.add_argument("--serve-requests", type=int, default=600, help="0: skip the served workload")
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[200.0, 2000.0])
+    ap.add_argument("--serve-workers", type=int, default=4)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -556,6 +674,11 @@ def main():
         torch.cuda.empty_cache()
         batched = batched_leg(args, ctx, dev)
 
+    served = None
+    if args.serve_requests > 0:
+        torch.cuda.empty_cache()
+        served = served_leg(args, dev)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -588,6 +711,7 @@ def main():
             "cpu_baseline": cpu,
             "e2e": e2e,
             "batched": batched,
+            "served": served,
             "gpu_launches": int(launches),
             "clocks": clk,
             "phases_ms": {nm: round(ms, 4) for nm, ms in phases},

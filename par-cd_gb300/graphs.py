@@ -412,7 +412,7 @@ def sbm_batch(count: int = 4096, seed: int = 4, median: float = 5000, sigma: flo
 
 def sbm_batch_torch(count: int = 4096, seed: int = 4, median: float = 5000, sigma: float = 1.2,
                     lo: int = 200, hi: int = 300_000, deg_in: float = 12.0, deg_out: float = 2.0,
-                    block: int = 50, device="cuda"):
+                    block: int = 50, device="cuda", sizes=None):
     """The batched SBM workload generated with torch on a device (input
     generation for the benchmark; `sbm_batch` is the numpy version for tests).
 
@@ -425,6 +425,9 @@ def sbm_batch_torch(count: int = 4096, seed: int = 4, median: float = 5000, sigm
     dropped, vertices relabelled by (degree, id) descending, isolated vertices
     removed.
 
+    `sizes` (optional) gives the vertex counts directly instead of the
+    log-normal law.
+
     Returns (vertex_offsets numpy int32[G+1], indices torch int32[N+1] union row
     offsets, adj torch int32[2M] local neighbour ids): the packed layout of
     pcd_batch_load_device."""
@@ -432,7 +435,7 @@ def sbm_batch_torch(count: int = 4096, seed: int = 4, median: float = 5000, sigm
 
     gen = torch.Generator(device=device)
     gen.manual_seed(seed)
-    ns = batch_sizes(count, median, sigma, lo, hi, seed)
+    ns = batch_sizes(count, median, sigma, lo, hi, seed) if sizes is None else np.asarray(sizes, np.int64)
     G = ns.shape[0]
     nb = np.maximum(1, ns // block)
     base_sz = ns // nb
@@ -528,3 +531,12 @@ def sbm_batch_torch(count: int = 4096, seed: int = 4, median: float = 5000, sigm
     del cols, cgraph
     voff = new_off.cpu().numpy().astype(np.int32)
     return voff, indices.to(torch.int32), adj
+
+
+def unpack(voff, indices, adj):
+    """Per-graph (indices, adj) numpy pairs of a packed batch (host arrays)."""
+    out = []
+    for g in range(len(voff) - 1):
+        a, b = int(voff[g]), int(voff[g + 1])
+        out.append(((indices[a:b + 1] - indices[a]).astype(np.int32), np.ascontiguousarray(adj[indices[a]:indices[b]])))
+    return out
