@@ -399,12 +399,13 @@ def served_leg(args, dev):
     sbm, pl, rm = serve_pool(dev)
     log(f"[bench] serve pool: {len(sbm)} SBM, {len(pl)} power-law, {len(rm)} R-MAT s22 ({time.time() - t0:.1f}s)")
     rng = np.random.default_rng(5)
-    reqs = []
+    reqs, kinds = [], []
     for _ in range(args.serve_requests):
         u = rng.random()
         pool = sbm if u < 0.90 else (pl if u < 0.99 else rm)
         g = pool[int(rng.integers(len(pool)))]
         reqs.append((g, "mod" if rng.random() < 0.5 else "cpm-0.01"))
+        kinds.append("sbm" if u < 0.90 else ("powerlaw" if u < 0.99 else "rmat22"))
     gaps = rng.exponential(1.0, size=len(reqs))
     edges = sum(len(g[1]) // 2 for g, _ in reqs)
 
@@ -431,7 +432,14 @@ def served_leg(args, dev):
     out = {"requests": len(reqs), "edges": int(edges),
            "mix": "90% SBM n~LogUniform[1e3, 5e4] (64-graph pool), 9% power-law n in {1e5, 2.5e5, 6e5}, "
                   "1% R-MAT s22; mod or cpm-0.01 each with p 1/2; -s 0 -f 1.0 -t 0 from singletons",
-           "hbm_budget_bytes": 150 * 10**9, "rates": []}
+           "hbm_budget_bytes": 150 * 10**9, "rates": [],
+           "plain_service_by_type": {k: {"requests": int(sum(1 for x in kinds if x == k)),
+                                         "mean_ms": round(1000.0 * float(np.mean([service[i] for i in range(len(reqs))
+                                                                                  if kinds[i] == k])), 3),
+                                         "mean_iterations": float(np.mean([plain[i][1].iterations
+                                                                           for i in range(len(reqs))
+                                                                           if kinds[i] == k]))}
+                                     for k in ("sbm", "powerlaw", "rmat22") if k in kinds}}
     for rate in args.serve_rates:
         arrival = np.cumsum(gaps / rate)
         # plain FIFO queue

@@ -229,7 +229,10 @@ pcd_status pcd_batch_run(pcd_graph *batch, const pcd_rule *rule, int32_t strateg
  * counted with pcd_estimate_device_bytes, stays within hbm_budget_bytes; a
  * request that alone exceeds the budget fails with PCD_ERR_OUT_OF_MEMORY.  A
  * batch smaller than max_batch_graphs starts once its oldest request has
- * waited max_wait_ms.  Every graph gets exactly its result alone.
+ * waited max_wait_ms.  A batch holds one size class (small / medium / large
+ * by adjacency entries; a large graph runs alone), and at most workers - 1
+ * batches of medium or large graphs run at once, so small requests always
+ * have a worker.  Every graph gets exactly its result alone.
  * ------------------------------------------------------------------------ */
 typedef struct pcd_server pcd_server;
 typedef struct pcd_schedule {
@@ -247,7 +250,9 @@ typedef struct pcd_serve_config {
     int64_t max_batch_edges;
     int64_t hbm_budget_bytes;
     double max_wait_ms;
-    int32_t use_cuda_graph;  /* passed to pcd_batch_run */
+    int32_t use_cuda_graph;     /* passed to pcd_batch_run */
+    int64_t small_graph_edges;  /* size classes by adjacency entries: small <= this,   */
+    int64_t large_graph_edges;  /* medium <= this, large above (one graph per batch)   */
 } pcd_serve_config;
 typedef struct pcd_serve_stats {
     int64_t submitted, completed, failed, batches, batched_graphs, queue_len;

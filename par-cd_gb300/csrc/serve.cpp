@@ -48,6 +48,7 @@ struct Request {
     double score = 0.0;
     int32_t iterations = 0;
     int64_t batch_graphs = 0;
+    int32_t cls = 0;  // size class: 0 small, 1 medium, 2 large (runs alone)
 };
 
 bool same_schedule(const pcd_schedule &a, const pcd_schedule &b) {
@@ -68,6 +69,7 @@ struct pcd_server {
     bool stopping = false;
     uint64_t next_id = 1;
     int64_t in_flight = 0;
+    int32_t big_in_flight = 0;  // batches of medium or large graphs running
     pcd_serve_stats stats{};
     pcd_status start_status = PCD_OK;
     int32_t started = 0;
@@ -95,15 +97,30 @@ struct pcd_server {
 };
 
 // Forms the next batch, or returns false when stopping with an empty queue.
-// Requests too large for the whole budget fail here.
+// Requests too large for the whole budget fail here.  A batch holds one size
+// class only, and while workers - 1 batches of medium or large graphs run, a
+// free worker serves the oldest small request instead, so small graphs never
+// wait behind long runs of big ones.
 bool pcd_server::take_batch(std::vector<std::shared_ptr<Request>> &batch, int64_t &bytes) {
     std::unique_lock<std::mutex> lock(mu);
     for (;;) {
         cv_work.wait(lock, [&] { return stopping || !queue.empty(); });
         if (queue.empty()) return false;  // stopping
-        const std::shared_ptr<Request> head = queue.front();
+        std::shared_ptr<Request> head = queue.front();
+        if (head->cls > 0 && cfg.workers > 1 && big_in_flight >= cfg.workers - 1) {
+            head = nullptr;
+            for (const auto &r : queue)
+                if (r->cls == 0) {
+                    head = r;
+                    break;
+                }
+            if (!head) {  // only big requests wait: hold this worker back
+                cv_work.wait(lock);
+                continue;
+            }
+        }
         if (estimate({head}) > cfg.hbm_budget_bytes) {
-            queue.pop_front();
+            queue.erase(std::find(queue.begin(), queue.end(), head));
             head->status = PCD_ERR_OUT_OF_MEMORY;
             head->done = true;
             head->t_start = head->t_done = Clock::now();
@@ -115,9 +132,10 @@ bool pcd_server::take_batch(std::vector<std::shared_ptr<Request>> &batch, int64_
         // requests of the head's schedule, in arrival order, within the caps
         std::vector<std::shared_ptr<Request>> pick;
         int64_t edges = 0;
+        const int32_t cap = head->cls == 2 ? 1 : cfg.max_batch_graphs;
         for (const auto &r : queue) {
-            if ((int32_t)pick.size() >= cfg.max_batch_graphs) break;
-            if (!same_schedule(r->sched, head->sched)) continue;
+            if ((int32_t)pick.size() >= cap) break;
+            if (r->cls != head->cls || !same_schedule(r->sched, head->sched)) continue;
             if (!pick.empty() && edges + 2ll * r->m > cfg.max_batch_edges) break;
             pick.push_back(r);
             if (estimate(pick) > cfg.hbm_budget_bytes - in_flight) {
@@ -131,7 +149,7 @@ bool pcd_server::take_batch(std::vector<std::shared_ptr<Request>> &batch, int64_
             continue;
         }
         // a partial batch waits for company until its oldest request is max_wait_ms old
-        if ((int32_t)pick.size() < cfg.max_batch_graphs && !stopping && cfg.max_wait_ms > 0) {
+        if ((int32_t)pick.size() < cap && !stopping && cfg.max_wait_ms > 0) {
             const auto deadline = head->t_submit + std::chrono::microseconds((int64_t)(cfg.max_wait_ms * 1000.0));
             if (Clock::now() < deadline) {
                 cv_work.wait_until(lock, deadline);
@@ -139,6 +157,7 @@ bool pcd_server::take_batch(std::vector<std::shared_ptr<Request>> &batch, int64_
             }
         }
         bytes = estimate(pick);
+        if (head->cls > 0) ++big_in_flight;
         in_flight += bytes;
         stats.bytes_in_flight = in_flight;
         stats.bytes_peak = std::max(stats.bytes_peak, in_flight);
@@ -193,6 +212,7 @@ void pcd_server::run_batch(pcd_ctx *ctx, std::vector<std::shared_ptr<Request>> &
     }
     const auto t_done = Clock::now();
     std::lock_guard<std::mutex> lock(mu);
+    if (batch.front()->cls > 0) --big_in_flight;
     in_flight -= bytes;
     stats.bytes_in_flight = in_flight;
     stats.bytes_measured_peak = std::max(stats.bytes_measured_peak, held);
@@ -247,7 +267,8 @@ extern "C" {
 
 pcd_status pcd_serve_start(const pcd_serve_config *cfg, pcd_server **out) {
     if (!cfg || !out || cfg->workers < 1 || cfg->max_batch_graphs < 1 || cfg->max_batch_edges < 1 ||
-        cfg->hbm_budget_bytes < 1 || cfg->max_wait_ms < 0)
+        cfg->hbm_budget_bytes < 1 || cfg->max_wait_ms < 0 || cfg->small_graph_edges < 0 ||
+        cfg->large_graph_edges < cfg->small_graph_edges)
         return PCD_ERR_INVALID_ARGUMENT;
     *out = nullptr;
     pcd_server *s = new (std::nothrow) pcd_server;
@@ -302,6 +323,7 @@ pcd_status pcd_serve_submit(pcd_server *s, int32_t n, int32_t m, const int32_t *
         r->max_deg = std::max(r->max_deg, e - b);
         if (e - b > 8192) ++r->hubs;
     }
+    r->cls = 2ll * m <= s->cfg.small_graph_edges ? 0 : (2ll * m <= s->cfg.large_graph_edges ? 1 : 2);
     r->indices.assign(indices, indices + n + 1);
     r->adj.assign(adj, adj + 2 * (size_t)m);
     {

@@ -54,7 +54,7 @@ class _Schedule(C.Structure):
 class _ServeConfig(C.Structure):
     _fields_ = [("device", C.c_int32), ("workers", C.c_int32), ("max_batch_graphs", C.c_int32),
                 ("max_batch_edges", C.c_int64), ("hbm_budget_bytes", C.c_int64), ("max_wait_ms", C.c_double),
-                ("use_cuda_graph", C.c_int32)]
+                ("use_cuda_graph", C.c_int32), ("small_graph_edges", C.c_int64), ("large_graph_edges", C.c_int64)]
 
 
 class _ServeStats(C.Structure):
@@ -612,10 +612,10 @@ class Server:
     blocks for that ticket's result."""
 
     def __init__(self, device: int = 0, workers: int = 2, max_batch_graphs: int = 256,
-                 max_batch_edges: int = 1 << 30, hbm_budget_bytes: int = 150 * 10**9, max_wait_ms: float = 2.0,
-                 cuda_graph: bool = False):
+                 max_batch_edges: int = 1 << 28, hbm_budget_bytes: int = 150 * 10**9, max_wait_ms: float = 2.0,
+                 cuda_graph: bool = False, small_graph_edges: int = 1 << 20, large_graph_edges: int = 1 << 24):
         cfg = _ServeConfig(device, workers, max_batch_graphs, max_batch_edges, hbm_budget_bytes, max_wait_ms,
-                           1 if cuda_graph else 0)
+                           1 if cuda_graph else 0, small_graph_edges, large_graph_edges)
         self.h = C.c_void_p()
         st = LIB.pcd_serve_start(C.byref(cfg), C.byref(self.h))
         if st:

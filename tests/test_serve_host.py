@@ -31,9 +31,10 @@ def test_serve_start_rejects_bad_config():
     import pcd
 
     h = C.c_void_p()
-    for bad in (dict(workers=0), dict(max_batch_graphs=0), dict(hbm_budget_bytes=0), dict(max_wait_ms=-1.0)):
+    for bad in (dict(workers=0), dict(max_batch_graphs=0), dict(hbm_budget_bytes=0), dict(max_wait_ms=-1.0),
+                dict(large_graph_edges=1 << 5)):
         kw = dict(device=0, workers=1, max_batch_graphs=8, max_batch_edges=1 << 20, hbm_budget_bytes=1 << 30,
-                  max_wait_ms=1.0, use_cuda_graph=0)
+                  max_wait_ms=1.0, use_cuda_graph=0, small_graph_edges=1 << 10, large_graph_edges=1 << 20)
         kw.update(bad)
         cfg = pcd._ServeConfig(**kw)
         assert pcd.LIB.pcd_serve_start(C.byref(cfg), C.byref(h)) == 1
