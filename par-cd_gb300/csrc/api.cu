@@ -26,10 +26,12 @@ pcd_status check_cuda(pcd_ctx *ctx, cudaError_t e, const char *what) {
 
 pcd_status dev_alloc(pcd_graph *g, void **p, size_t bytes) {
     if (bytes == 0) bytes = 16;
-    cudaError_t e = cudaMalloc(p, bytes);
+    // stream-ordered: no device-wide synchronisation, so contexts on other
+    // streams (the serving workers) keep running while graphs come and go
+    cudaError_t e = cudaMallocAsync(p, bytes, g->ctx->stream);
     if (e != cudaSuccess) {
         *p = nullptr;
-        return check_cuda(g->ctx, e, "cudaMalloc");
+        return check_cuda(g->ctx, e, "cudaMallocAsync");
     }
     g->allocs.push_back(*p);
     g->dev_bytes += bytes;
@@ -147,6 +149,19 @@ pcd_status check_rule(pcd_graph *g, const pcd_rule *r) {
     return PCD_OK;
 }
 
+namespace pcd {
+// Lets the device's default memory pool keep up to `bytes` of freed memory
+// mapped, so that graphs loaded one after another reuse it instead of mapping
+// and releasing device memory each time (used by the serving loop).
+pcd_status keep_pool_memory(int32_t device, int64_t bytes) {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) != cudaSuccess) return PCD_ERR_CUDA;
+    uint64_t thr = (uint64_t)std::max<int64_t>(bytes, 0);
+    return cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr) == cudaSuccess ? PCD_OK
+                                                                                                : PCD_ERR_CUDA;
+}
+}  // namespace pcd
+
 extern "C" {
 
 const char *pcd_status_string(pcd_status s) {
@@ -175,6 +190,8 @@ pcd_status pcd_init(pcd_ctx **out, int32_t device) {
     if (s == PCD_OK) s = check_cuda(ctx, cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking),
                                     "cudaStreamCreate");
     if (s == PCD_OK) s = check_cuda(ctx, cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking), "side stream");
+    if (s == PCD_OK)
+        s = check_cuda(ctx, cudaMallocHost((void **)&ctx->h_ctr, sizeof(DevCounters)), "cudaMallocHost");
     if (s == PCD_OK) s = check_cuda(ctx, cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming), "event");
     if (s == PCD_OK) s = check_cuda(ctx, cudaEventCreateWithFlags(&ctx->join, cudaEventDisableTiming), "event");
     if (s == PCD_OK) {
@@ -203,12 +220,12 @@ pcd_status pcd_graph_free(pcd_graph *g) {
     if (!g) return PCD_ERR_INVALID_ARGUMENT;
     pcd_ctx *ctx = g->ctx;
     if (ctx && ctx->stream) cudaStreamSynchronize(ctx->stream);
+    cudaStream_t fs = ctx ? ctx->stream : nullptr;
     for (void *p : g->allocs)
-        if (p) cudaFree(p);
-    if (g->hub_scratch) cudaFree(g->hub_scratch);
-    if (g->merge_buf) cudaFree(g->merge_buf);
-    if (g->h_ctr) cudaFreeHost(g->h_ctr);
-    if (g->batch && g->batch->seed_table) cudaFree(g->batch->seed_table);
+        if (p) cudaFreeAsync(p, fs);
+    if (g->hub_scratch) cudaFreeAsync(g->hub_scratch, fs);
+    if (g->merge_buf) cudaFreeAsync(g->merge_buf, fs);
+    if (g->batch && g->batch->seed_table) cudaFreeAsync(g->batch->seed_table, fs);
     delete g->batch;
     if (ctx) ctx->graphs.erase(std::remove(ctx->graphs.begin(), ctx->graphs.end(), g), ctx->graphs.end());
     delete g;
@@ -229,6 +246,7 @@ pcd_status pcd_destroy(pcd_ctx *ctx) {
         cudaStreamSynchronize(ctx->own_stream);
         cudaStreamDestroy(ctx->own_stream);
     }
+    if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
     delete ctx;
     return PCD_OK;
 }
@@ -279,14 +297,14 @@ static pcd_status ensure_hub_scratch(pcd_graph *g) {
     cudaStream_t st = ctx->stream;
     CK(cudaStreamSynchronize(st), "hub scratch");
     if (g->hub_scratch) {
-        cudaFree(g->hub_scratch);
+        cudaFreeAsync(g->hub_scratch, st);
         g->dev_bytes -= g->hub_bytes;
     }
     g->hub_scratch = nullptr;
     g->hub_blocks = 0;
     g->hub_bytes = 0;
     const size_t bytes = sizeof(int32_t) * (size_t)(stride * want);
-    CK(cudaMalloc((void **)&g->hub_scratch, bytes), "hub scratch");
+    CK(cudaMallocAsync((void **)&g->hub_scratch, bytes, st), "hub scratch");
     for (int32_t bk = 0; bk < want; ++bk) {
         int32_t *base = g->hub_scratch + (int64_t)bk * stride;
         CK(cudaMemsetAsync(base, 0xff, sizeof(int32_t) * (size_t)slots, st), "hub scratch");
@@ -344,7 +362,7 @@ static pcd_status graph_setup(pcd_ctx *ctx, pcd_graph *g) {
     TRY(dev_alloc(g, (void **)&g->small, 65536));
     TRY(dev_alloc(g, (void **)&g->d_score, 64));
     TRY(dev_alloc(g, (void **)&g->bin_list, sizeof(int32_t) * nn));
-    CK(cudaMallocHost((void **)&g->h_ctr, sizeof(DevCounters)), "cudaMallocHost");
+    g->h_ctr = ctx->h_ctr;  // pinned, one per context (calls on a context come from one thread)
     CK(cudaMemsetAsync(g->ctr, 0, sizeof(DevCounters), st), "memset");
     // FP64 re-evaluation tables: one HBM slice per block, empty between uses
     // (keys -1, counts 0, first positions 0xffffffff; position arrays need no init)
@@ -403,10 +421,10 @@ static pcd_status load_common(pcd_ctx *ctx, int32_t n, int32_t m, const int32_t 
         s = check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "init labels");
     }
     if (s != PCD_OK) {
+        cudaStreamSynchronize(ctx->stream);
         for (void *p : g->allocs)
-            if (p) cudaFree(p);
-        if (g->hub_scratch) cudaFree(g->hub_scratch);
-        if (g->h_ctr) cudaFreeHost(g->h_ctr);
+            if (p) cudaFreeAsync(p, ctx->stream);
+        if (g->hub_scratch) cudaFreeAsync(g->hub_scratch, ctx->stream);
         delete g;
         return s;
     }
@@ -424,6 +442,7 @@ pcd_status pcd_load_csr_device(pcd_ctx *ctx, int32_t n, int32_t m, const int32_t
                                pcd_graph **out) {
     return load_common(ctx, n, m, d_indices, d_adj, cudaMemcpyDeviceToDevice, out);
 }
+
 
 pcd_status pcd_device_sm_count(pcd_ctx *ctx, int32_t *sms) {
     if (!ctx || !sms) return PCD_ERR_INVALID_ARGUMENT;

@@ -177,17 +177,14 @@ static pcd_status batch_load(pcd_ctx *ctx, int32_t G, const int32_t *voff, const
     int32_t *d_ind = nullptr, *d_adj = nullptr, *d_flag = nullptr, *d_voff = nullptr, *d_vgid = nullptr;
     cudaStream_t st = ctx->stream;
     auto cleanup = [&]() {
-        cudaFree(d_ind);
-        cudaFree(d_adj);
-        cudaFree(d_flag);
-        cudaFree(d_voff);
-        cudaFree(d_vgid);
+        for (int32_t *p : {d_ind, d_adj, d_flag, d_voff, d_vgid})
+            if (p) cudaFreeAsync(p, st);
     };
-    if (cudaMalloc(&d_ind, sizeof(int32_t) * ((size_t)N + 1)) != cudaSuccess ||
-        cudaMalloc(&d_adj, sizeof(int32_t) * std::max<int64_t>(nnz, 1)) != cudaSuccess ||
-        cudaMalloc(&d_flag, sizeof(int32_t)) != cudaSuccess ||
-        cudaMalloc(&d_voff, sizeof(int32_t) * ((size_t)G + 1)) != cudaSuccess ||
-        cudaMalloc(&d_vgid, sizeof(int32_t) * std::max(N, 1)) != cudaSuccess) {
+    if (cudaMallocAsync(&d_ind, sizeof(int32_t) * ((size_t)N + 1), st) != cudaSuccess ||
+        cudaMallocAsync(&d_adj, sizeof(int32_t) * std::max<int64_t>(nnz, 1), st) != cudaSuccess ||
+        cudaMallocAsync(&d_flag, sizeof(int32_t), st) != cudaSuccess ||
+        cudaMallocAsync(&d_voff, sizeof(int32_t) * ((size_t)G + 1), st) != cudaSuccess ||
+        cudaMallocAsync(&d_vgid, sizeof(int32_t) * std::max(N, 1), st) != cudaSuccess) {
         cleanup();
         return set_error(ctx, PCD_ERR_OUT_OF_MEMORY, "batch staging buffers");
     }
@@ -362,14 +359,14 @@ pcd_status pcd_batch_run(pcd_graph *g, const pcd_rule *rule, int32_t strategy, d
         for (int32_t it = 0; it < cap; ++it) table[(size_t)it * G + gi] = (uint32_t)pcd_rand_next(&r);
     }
     if (B->seed_iters < cap) {
-        if (B->seed_table) cudaFree(B->seed_table);
+        if (B->seed_table) cudaFreeAsync(B->seed_table, st);
         B->seed_table = nullptr;
-        CK(cudaMalloc(&B->seed_table, sizeof(uint32_t) * table.size()), "seed table");
+        CK(cudaMallocAsync(&B->seed_table, sizeof(uint32_t) * table.size(), st), "seed table");
         B->seed_iters = cap;
     }
     int32_t *iters_d = nullptr;
     double *final_d = nullptr;
-    CK(cudaMalloc(&iters_d, sizeof(int32_t) * G + sizeof(double) * G + 64), "run buffers");
+    CK(cudaMallocAsync(&iters_d, sizeof(int32_t) * G + sizeof(double) * G + 64, st), "run buffers");
     final_d = reinterpret_cast<double *>(reinterpret_cast<char *>(iters_d) + ((sizeof(int32_t) * G + 63) & ~63ull));
     CK(cudaMemcpyAsync(B->seed_table, table.data(), sizeof(uint32_t) * table.size(), cudaMemcpyHostToDevice, st),
        "seeds");
@@ -461,7 +458,7 @@ pcd_status pcd_batch_run(pcd_graph *g, const pcd_rule *rule, int32_t strategy, d
         s = check_cuda(ctx, cudaMemcpyAsync(iterations, iters_d, sizeof(int32_t) * G, cudaMemcpyDeviceToHost, st),
                        "iterations");
     if (s == PCD_OK) s = sync_and_check(g);
-    cudaFree(iters_d);
+    cudaFreeAsync(iters_d, st);
     return s;
 }
 

@@ -379,10 +379,10 @@ static pcd_status merge_buffers(pcd_graph *g, int64_t E, int64_t k, int grid, Me
     size_t o_ss = take(4 * kk), o_se = take(4 * kk), o_best = take(4 * kk), o_found = take(4 * kk);
     size_t o_tie = take(4 * (e + kk + 1)), o_nd = take(4 * kk), o_hist = take(4ull * 256 * grid);
     if (need > g->merge_bytes) {
-        if (g->merge_buf) cudaFree(g->merge_buf);
+        if (g->merge_buf) cudaFreeAsync(g->merge_buf, g->ctx->stream);
         g->merge_buf = nullptr;
         g->merge_bytes = 0;
-        cudaError_t err = cudaMalloc(&g->merge_buf, need);
+        cudaError_t err = cudaMallocAsync(&g->merge_buf, need, g->ctx->stream);
         if (err != cudaSuccess) return check_cuda(g->ctx, err, "merge buffers");
         g->merge_bytes = need;
     }

@@ -25,6 +25,7 @@ struct pcd_ctx {
     std::vector<cudaEvent_t> prof_pool;
     std::vector<const char *> prof_names;
     size_t prof_used = 0;
+    pcd::DevCounters *h_ctr = nullptr;  // pinned copy of a graph's counters (shared by its graphs)
 };
 
 // Per-graph state of a batch: many graphs refined as one disjoint union whose

@@ -27,6 +27,10 @@
 
 #include "pcd.h"
 
+namespace pcd {
+pcd_status keep_pool_memory(int32_t device, int64_t bytes);  // api.cu
+}
+
 namespace {
 
 using Clock = std::chrono::steady_clock;
@@ -282,6 +286,7 @@ pcd_status pcd_serve_start(const pcd_serve_config *cfg, pcd_server **out) {
         s->num_sms = std::max(sms, 1);
     }
     if (probe) pcd_destroy(probe);
+    if (st == PCD_OK) st = pcd::keep_pool_memory(cfg->device, cfg->hbm_budget_bytes);
     if (st != PCD_OK) {
         delete s;
         return st;
