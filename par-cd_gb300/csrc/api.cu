@@ -284,16 +284,15 @@ pcd_status pcd_synchronize(pcd_ctx *ctx) {
     return PCD_OK;
 }
 
-// Hub tables: one HBM slice per block, as many blocks as there are hub vertices
-// (at most one per SM); grown when the degree classes change.  Slices start
-// empty (keys -1, counts 0, first positions 0xffffffff) and the hub kernel
-// leaves them empty.
+// Hub slices: per block, a packed key and a label for every position of the
+// largest row; as many blocks as there are hub vertices (at most one per SM);
+// grown when the degree classes change.  No initial contents are needed.
 static pcd_status ensure_hub_scratch(pcd_graph *g) {
     pcd_ctx *ctx = g->ctx;
     const int64_t hubs = g->bin_off[NBINS] - g->bin_off[BIN_HUB];
     const int32_t want = (int32_t)std::min<int64_t>(ctx->num_sms, hubs);
     if (want <= g->hub_blocks) return PCD_OK;
-    const int64_t slots = g->fb_slots, stride = 3 * slots + 2ll * g->max_deg;
+    const int64_t stride = hub_stride(g->max_deg);
     cudaStream_t st = ctx->stream;
     CK(cudaStreamSynchronize(st), "hub scratch");
     if (g->hub_scratch) {
@@ -305,12 +304,6 @@ static pcd_status ensure_hub_scratch(pcd_graph *g) {
     g->hub_bytes = 0;
     const size_t bytes = sizeof(int32_t) * (size_t)(stride * want);
     CK(cudaMallocAsync((void **)&g->hub_scratch, bytes, st), "hub scratch");
-    for (int32_t bk = 0; bk < want; ++bk) {
-        int32_t *base = g->hub_scratch + (int64_t)bk * stride;
-        CK(cudaMemsetAsync(base, 0xff, sizeof(int32_t) * (size_t)slots, st), "hub scratch");
-        CK(cudaMemsetAsync(base + slots, 0, sizeof(int32_t) * (size_t)slots, st), "hub scratch");
-        CK(cudaMemsetAsync(base + 2 * slots, 0xff, sizeof(int32_t) * (size_t)slots, st), "hub scratch");
-    }
     g->hub_blocks = want;
     g->hub_bytes = bytes;
     g->dev_bytes += bytes;
@@ -478,7 +471,7 @@ pcd_status pcd_estimate_device_bytes(int32_t n, int64_t nnz, int32_t max_deg, in
     while (slots < 2 * (int64_t)std::max(max_deg, 1)) slots <<= 1;
     const int64_t fb_stride = 3 * slots + max_deg;
     b += 4 * fb_stride * std::min<int64_t>(8, std::max<int64_t>(1, (1ll << 29) / (4 * fb_stride)));
-    b += 4 * (3 * slots + 2ll * max_deg) * std::min<int64_t>(num_sms, num_hubs);
+    b += 4 * hub_stride(max_deg) * std::min<int64_t>(num_sms, num_hubs);
     // batch state, the staging copies of a batch load, the seed table of a run
     b += 8 * nn + 8 * (G + 1) + 52 * G + 64;
     b += 4 * (nn + 1) + 4 * e + 8 + 4 * (G + 1) + 4 * nn;

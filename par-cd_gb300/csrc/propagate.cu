@@ -1047,6 +1047,234 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
 }
 
 // ---------------------------------------------------------------------------
+// Hubs: one 1024-thread block per vertex, tables in shared memory.  A hub's
+// labels are split by hash into P parts of at most part_labels distinct
+// labels; each part is histogrammed in the shared table, its first
+// occurrences are keyed, and the table is cleared, before the next part.
+// Position-indexed arrays in a per-block global slice carry the row between
+// parts: pos_lab[p] (the label at position p, gathered once) and pos_key[p]
+// (the packed key of p if it is a candidate, the identity otherwise; every
+// position is written by the part its label belongs to).  The ordered pass
+// of the one-pass kernel then runs over pos_key: range maxima, carry-ins,
+// ties and the final level.  All global traffic is coalesced and the slices
+// are small enough to stay in L2.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t hub_part(uint32_t hv, int32_t parts) {
+    return (uint32_t)(((unsigned long long)hv * (uint32_t)parts) >> 32);
+}
+
+template <class R>
+__global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, const int32_t *__restrict__ list,
+                                                         int64_t count, int32_t table_cap, int32_t part_labels,
+                                                         int32_t *gscratch, int64_t gstride, int32_t pos_cap) {
+    using PK = PackedKey<R>;
+    using K = typename PK::K;
+    constexpr int BT = 1024, NW = 32;
+    extern __shared__ int32_t smem[];
+    int32_t *keys = smem;
+    int32_t *cnts = smem + table_cap;
+    uint32_t *first = reinterpret_cast<uint32_t *>(smem + 2 * table_cap);
+    __shared__ K s_agg[NW];
+    __shared__ uint32_t s_t[NW];
+    __shared__ int32_t s_nfin[NW];
+    __shared__ int32_t s_amb, s_curr_freq;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    K *pos_key = reinterpret_cast<K *>(gscratch + (int64_t)blockIdx.x * gstride);
+    int32_t *pos_lab = reinterpret_cast<int32_t *>(pos_key + pos_cap);
+    for (int32_t i = tid; i < table_cap; i += BT) {
+        keys[i] = -1;
+        cnts[i] = 0;
+        first[i] = 0xffffffffu;
+    }
+    __syncthreads();
+    for (int64_t vi = blockIdx.x; vi < count; vi += gridDim.x) {
+        const int32_t v = list[vi];
+        const int32_t b = a.g.indices[v], d = a.g.indices[v + 1] - b;
+        const int32_t curr = a.labels[v];
+        const R vr = rule.at(v);
+        if (vr.vertex_ambiguous(d)) {
+            if (tid == 0) push_ambiguous(a, v, d);
+            continue;
+        }
+        if (d > pos_cap) {  // the slices hold the largest degree: never expected
+            if (tid == 0) atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);
+            continue;
+        }
+        const int32_t parts = max(1, (d + part_labels - 1) / part_labels);
+        int32_t ts = 64;
+        while (ts < 2 * min(d, part_labels) && ts < table_cap) ts <<= 1;
+        if (parts > 1) ts = table_cap;
+        if (tid == 0) {
+            s_amb = 0;
+            s_curr_freq = 0;
+        }
+        // the row's labels by position, gathered once
+        for (int32_t p0 = 0; p0 < d; p0 += BT * 4) {
+            int32_t l[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int32_t p = p0 + u * BT + tid;
+                l[u] = p < d ? a.g.adj[b + p] : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int32_t p = p0 + u * BT + tid;
+                if (p < d) pos_lab[p] = a.labels[l[u]];
+            }
+        }
+        __syncthreads();
+        for (int32_t part = 0; part < parts; ++part) {
+            // histogram of this part's labels
+            for (int32_t p0 = 0; p0 < d; p0 += BT) {
+                const int32_t p = p0 + tid;
+                const int32_t l = p < d ? pos_lab[p] : -2;
+                const uint32_t hv = hash_label(l);
+                const bool in = p < d && hub_part(hv, parts) == (uint32_t)part;
+                const unsigned peers = __match_any_sync(FULL, in ? l : -3 - lane);
+                if (in && lane == __ffs(peers) - 1) {
+                    uint32_t h = hv & (uint32_t)(ts - 1);
+                    int32_t probes = 0;
+                    for (; probes < ts; ++probes) {
+                        const int32_t kk = keys[h];
+                        if (kk == l) break;
+                        if (kk == -1) {
+                            const int32_t old = atomicCAS(&keys[h], -1, l);
+                            if (old == -1 || old == l) break;
+                        }
+                        h = (h + 1) & (uint32_t)(ts - 1);
+                    }
+                    if (probes < ts) {
+                        atomicAdd(&cnts[h], __popc(peers));
+                        atomicMin(&first[h], (uint32_t)p);
+                    } else {
+                        atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);  // a part overfilled the table
+                    }
+                }
+            }
+            __syncthreads();
+            // keys of this part's positions
+            for (int32_t p = tid; p < d; p += BT) {
+                const int32_t l = pos_lab[p];
+                const uint32_t hv = hash_label(l);
+                if (hub_part(hv, parts) != (uint32_t)part) continue;
+                uint32_t h = hv & (uint32_t)(ts - 1);
+                int32_t probes = 0;
+                while (probes < ts && keys[h] != l) {
+                    h = (h + 1) & (uint32_t)(ts - 1);
+                    ++probes;
+                }
+                K key = PK::ident();
+                if (probes < ts && first[h] == (uint32_t)p) {
+                    const int32_t k = cnts[h];
+                    if (l == curr) {
+                        s_curr_freq = k;
+                    } else {
+                        Tag tag{0, 0};
+                        const typename R::Key raw = vr.join(v, d, l, k, a.cm, tag);
+                        if (R::usable(raw)) key = PK::make(raw, k);
+                    }
+                }
+                pos_key[p] = key;
+            }
+            __syncthreads();
+            for (int32_t i = tid; i < ts; i += BT) {
+                keys[i] = -1;
+                cnts[i] = 0;
+                first[i] = 0xffffffffu;
+            }
+            __syncthreads();
+        }
+        // ordered pass over the keyed positions, one contiguous range per warp
+        const int32_t span = ((d + NW - 1) / NW + 31) & ~31;
+        const int32_t lo = min(d, wid * span), hi = min(d, lo + span);
+        K wmax = PK::ident();
+        for (int32_t p = lo + lane; p < hi; p += 32) wmax = kmax(wmax, pos_key[p]);
+#pragma unroll
+        for (int o = 16; o; o >>= 1) wmax = kmax(wmax, __shfl_xor_sync(FULL, wmax, o));
+        if (lane == 0) s_agg[wid] = wmax;
+        __syncthreads();
+        K carry = PK::init(), mreal = PK::ident();
+        for (int w2 = 0; w2 < NW; ++w2) {
+            const K x = s_agg[w2];
+            if (w2 < wid) carry = kmax(carry, x);
+            mreal = kmax(mreal, x);
+        }
+        const auto lfin = PK::level(kmax(PK::init(), mreal));
+        uint32_t t = 0;
+        int32_t nfin = 0;
+        bool amb = false;
+        int32_t *fin_list = pos_lab + lo;  // entries already read are overwritten
+        for (int32_t base = lo; base < hi; base += 32) {
+            const int32_t p = base + lane;
+            const K key = p < hi ? pos_key[p] : PK::ident();
+            const bool cand = key != PK::ident();
+            const int32_t l = cand ? pos_lab[p] : -1;
+            __syncwarp();
+            const bool fin = cand && PK::level(key) == lfin;
+            const unsigned fm = __ballot_sync(FULL, fin);
+            if (fin) fin_list[nfin + __popc(fm & lanemask_lt())] = l;
+            nfin += __popc(fm);
+            if (!__any_sync(FULL, cand && PK::level(key) >= PK::level(carry))) continue;
+            K inc = key;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const K y = __shfl_up_sync(FULL, inc, o);
+                if (lane >= o) inc = kmax(inc, y);
+            }
+            K ex = __shfl_up_sync(FULL, inc, 1);
+            if (lane == 0) ex = PK::ident();
+            const K pre = kmax(carry, ex);
+            const bool tie = cand && PK::level(key) == PK::level(pre);
+            if (tie && PK::tie_ambiguous(key, pre)) amb = true;
+            t += __popc(__ballot_sync(FULL, tie));
+            carry = kmax(carry, __shfl_sync(FULL, inc, 31));
+        }
+        amb = __any_sync(FULL, amb);
+        if (lane == 0) {
+            s_t[wid] = t;
+            s_nfin[wid] = nfin;
+            if (amb) s_amb = 1;
+        }
+        __syncthreads();
+        uint32_t tt = 0;
+        int32_t nf = 0, before = 0, hw = -1;
+        for (int w2 = 0; w2 < NW; ++w2) {
+            const int32_t c = s_nfin[w2];
+            tt += s_t[w2];
+            if (w2 < wid) before += c;
+            if (hw < 0 && c > 0) hw = w2;
+            nf += c;
+        }
+        const bool has_best = mreal != PK::ident() && PK::level(mreal) > PK::level(PK::init());
+        const int32_t holder = has_best && hw >= 0 ? pos_lab[hw * span] : -1;
+        const int32_t r = has_best ? nf - 1 : 0;
+        int32_t dec = DEC_AMBIGUOUS;
+        if (!s_amb) {
+            const typename R::Key best = has_best ? PK::raw_level(mreal) : R::initial();
+            dec = vr.decide(best, has_best, v, d, curr, s_curr_freq, a.cm);
+        }
+        const bool rec = dec == DEC_MOVE && r > 0;
+        if (tid == 0) {
+            if (dec == DEC_AMBIGUOUS) {
+                push_ambiguous(a, v, d);
+            } else {
+                a.ndraw[v] = tt;
+                write_decision(a, v, dec, holder, curr);
+                record_ties(a, v, b, rec, r, holder);
+            }
+        }
+        if (rec) {  // the same number of iterations in every lane
+            const long long off = (long long)b + v;
+            for (int32_t j0 = 0; j0 < nfin; j0 += 32) {
+                const int32_t j = j0 + lane, gi = before + j;  // 0 is the holder
+                if (j < nfin && gi > 0) a.tiebuf[off + gi] = fin_list[j];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // hubs: one 512-thread block per vertex with the table in a per-block HBM
 // slice.  Random HBM traffic is what costs here, so after the histogram the
 // table is walked once in slot order: each candidate is written to
@@ -1629,10 +1857,14 @@ static int launch_bins_rule(pcd_graph *g, const SweepArgs &a, const R &rule, cud
         prof_mark(g->ctx, "sweep.block_l", st);
     }
     if ((c = g->bin_off[BIN_HUB + 1] - g->bin_off[BIN_HUB]) > 0) {
-        // hubs: 512-thread blocks, tables in per-block HBM slices kept empty between vertices
-        k_prop_hub<R, 4><<<cap_grid(c, g->hub_blocks), 512, 0, st>>>(
-            a, rule, L + g->bin_off[BIN_HUB], c, (int32_t)g->fb_slots, g->hub_scratch,
-            3 * g->fb_slots + 2ll * g->max_deg);
+        // hubs: 1024-thread blocks, shared tables filled part by part, position
+        // arrays in per-block slices of hub_scratch
+        constexpr int32_t cap = HUB_TABLE_CAP;
+        const size_t smem = 3ull * cap * sizeof(int32_t);
+        cudaFuncSetAttribute(k_prop_hub_parts<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_prop_hub_parts<R><<<cap_grid(c, g->hub_blocks), 1024, smem, st>>>(
+            a, rule, L + g->bin_off[BIN_HUB], c, cap, HUB_PART_LABELS, g->hub_scratch, hub_stride(g->max_deg),
+            g->max_deg);
         ++launches;
         prof_mark(g->ctx, "sweep.hub", st);
     }
