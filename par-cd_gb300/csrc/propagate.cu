@@ -1074,6 +1074,7 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
     int32_t *keys = smem;
     int32_t *cnts = smem + table_cap;
     uint32_t *first = reinterpret_cast<uint32_t *>(smem + 2 * table_cap);
+    __shared__ int32_t s_start[HUB_MAX_PARTS + 1], s_cur[HUB_MAX_PARTS];
     __shared__ K s_agg[NW];
     __shared__ uint32_t s_t[NW];
     __shared__ int32_t s_nfin[NW];
@@ -1081,6 +1082,7 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     K *pos_key = reinterpret_cast<K *>(gscratch + (int64_t)blockIdx.x * gstride);
     int32_t *pos_lab = reinterpret_cast<int32_t *>(pos_key + pos_cap);
+    int32_t *bucket = pos_lab + pos_cap;  // positions grouped by part
     for (int32_t i = tid; i < table_cap; i += BT) {
         keys[i] = -1;
         cnts[i] = 0;
@@ -1100,15 +1102,14 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
             if (tid == 0) atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);
             continue;
         }
-        const int32_t parts = max(1, (d + part_labels - 1) / part_labels);
-        int32_t ts = 64;
-        while (ts < 2 * min(d, part_labels) && ts < table_cap) ts <<= 1;
-        if (parts > 1) ts = table_cap;
+        const int32_t parts = min(HUB_MAX_PARTS, max(1, (d + part_labels - 1) / part_labels));
+        for (int32_t i = tid; i < parts; i += BT) s_cur[i] = 0;
         if (tid == 0) {
             s_amb = 0;
             s_curr_freq = 0;
         }
-        // the row's labels by position, gathered once
+        __syncthreads();
+        // the row's labels by position (gathered once) and the part sizes
         for (int32_t p0 = 0; p0 < d; p0 += BT * 4) {
             int32_t l[4];
 #pragma unroll
@@ -1119,20 +1120,58 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int32_t p = p0 + u * BT + tid;
-                if (p < d) pos_lab[p] = a.labels[l[u]];
+                int32_t pt = -1 - lane;
+                if (p < d) {
+                    l[u] = a.labels[l[u]];
+                    pos_lab[p] = l[u];
+                    pt = (int32_t)hub_part(hash_label(l[u]), parts);
+                }
+                const unsigned peers = __match_any_sync(FULL, pt);
+                if (p < d && lane == __ffs(peers) - 1) atomicAdd(&s_cur[pt], __popc(peers));
             }
         }
         __syncthreads();
+        if (wid == 0) {  // exclusive scan of the part sizes
+            int32_t carry = 0;
+            for (int32_t i0 = 0; i0 < parts; i0 += 32) {
+                const int32_t i = i0 + lane;
+                const int32_t c = i < parts ? s_cur[i] : 0;
+                int32_t inc = c;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int32_t y = __shfl_up_sync(FULL, inc, o);
+                    if (lane >= o) inc += y;
+                }
+                if (i < parts) s_start[i] = carry + inc - c;
+                carry += __shfl_sync(FULL, inc, 31);
+            }
+            if (lane == 0) s_start[parts] = carry;
+        }
+        __syncthreads();
+        for (int32_t i = tid; i < parts; i += BT) s_cur[i] = s_start[i];
+        __syncthreads();
+        for (int32_t p0 = 0; p0 < d; p0 += BT) {  // positions into their part's bucket
+            const int32_t p = p0 + tid;
+            const int32_t pt = p < d ? (int32_t)hub_part(hash_label(pos_lab[p]), parts) : -1 - lane;
+            const unsigned peers = __match_any_sync(FULL, pt);
+            int32_t base = 0;
+            if (p < d && lane == __ffs(peers) - 1) base = atomicAdd(&s_cur[pt], __popc(peers));
+            base = __shfl_sync(FULL, base, __ffs(peers) - 1);
+            if (p < d) bucket[base + __popc(peers & lanemask_lt())] = p;
+        }
+        __syncthreads();
         for (int32_t part = 0; part < parts; ++part) {
+            const int32_t i0 = s_start[part], i1 = s_start[part + 1];
+            int32_t ts = 64;
+            while (ts < 2 * (i1 - i0) && ts < table_cap) ts <<= 1;
             // histogram of this part's labels
-            for (int32_t p0 = 0; p0 < d; p0 += BT) {
-                const int32_t p = p0 + tid;
-                const int32_t l = p < d ? pos_lab[p] : -2;
-                const uint32_t hv = hash_label(l);
-                const bool in = p < d && hub_part(hv, parts) == (uint32_t)part;
-                const unsigned peers = __match_any_sync(FULL, in ? l : -3 - lane);
-                if (in && lane == __ffs(peers) - 1) {
-                    uint32_t h = hv & (uint32_t)(ts - 1);
+            for (int32_t j0 = i0; j0 < i1; j0 += BT) {
+                const int32_t j = j0 + tid;
+                const int32_t p = j < i1 ? bucket[j] : -1;
+                const int32_t l = p >= 0 ? pos_lab[p] : -2;
+                const unsigned peers = __match_any_sync(FULL, p >= 0 ? l : -3 - lane);
+                if (p >= 0 && lane == __ffs(peers) - 1) {
+                    uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
                     int32_t probes = 0;
                     for (; probes < ts; ++probes) {
                         const int32_t kk = keys[h];
@@ -1153,11 +1192,10 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
             }
             __syncthreads();
             // keys of this part's positions
-            for (int32_t p = tid; p < d; p += BT) {
+            for (int32_t j = i0 + tid; j < i1; j += BT) {
+                const int32_t p = bucket[j];
                 const int32_t l = pos_lab[p];
-                const uint32_t hv = hash_label(l);
-                if (hub_part(hv, parts) != (uint32_t)part) continue;
-                uint32_t h = hv & (uint32_t)(ts - 1);
+                uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
                 int32_t probes = 0;
                 while (probes < ts && keys[h] != l) {
                     h = (h + 1) & (uint32_t)(ts - 1);
