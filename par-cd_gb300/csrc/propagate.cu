@@ -1170,6 +1170,8 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                 const int32_t p = j < i1 ? bucket[j] : -1;
                 const int32_t l = p >= 0 ? pos_lab[p] : -2;
                 const unsigned peers = __match_any_sync(FULL, p >= 0 ? l : -3 - lane);
+                // bucket order is not position order: the group's first position is its minimum
+                const uint32_t pmin = __reduce_min_sync(peers, (uint32_t)p);
                 if (p >= 0 && lane == __ffs(peers) - 1) {
                     uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
                     int32_t probes = 0;
@@ -1184,7 +1186,7 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                     }
                     if (probes < ts) {
                         atomicAdd(&cnts[h], __popc(peers));
-                        atomicMin(&first[h], (uint32_t)p);
+                        atomicMin(&first[h], pmin);
                     } else {
                         atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);  // a part overfilled the table
                     }
