@@ -1047,7 +1047,7 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
 }
 
 // ---------------------------------------------------------------------------
-// Hubs: one 1024-thread block per vertex, tables in shared memory.  A hub's
+// Hubs: one 512-thread block per vertex (two per SM), tables in shared memory.  A hub's
 // labels are split by hash into P parts of at most part_labels distinct
 // labels; each part is histogrammed in the shared table, its first
 // occurrences are keyed, and the table is cleared, before the next part.
@@ -1064,12 +1064,12 @@ __device__ __forceinline__ uint32_t hub_part(uint32_t hv, int32_t parts) {
 }
 
 template <class R>
-__global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, const int32_t *__restrict__ list,
-                                                         int64_t count, int32_t table_cap, int32_t part_labels,
-                                                         int32_t *gscratch, int64_t gstride, int32_t pos_cap) {
+__global__ void __launch_bounds__(512, 2) k_prop_hub_parts(SweepArgs a, R rule, const int32_t *__restrict__ list,
+                                                           int64_t count, int32_t table_cap, int32_t part_labels,
+                                                           int32_t *gscratch, int64_t gstride, int32_t pos_cap) {
     using PK = PackedKey<R>;
     using K = typename PK::K;
-    constexpr int BT = 1024, NW = 32;
+    constexpr int BT = 512, NW = 16;
     extern __shared__ int32_t smem[];
     int32_t *keys = smem;
     int32_t *cnts = smem + table_cap;
@@ -1082,7 +1082,8 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     K *pos_key = reinterpret_cast<K *>(gscratch + (int64_t)blockIdx.x * gstride);
     int32_t *pos_lab = reinterpret_cast<int32_t *>(pos_key + pos_cap);
-    int32_t *bucket = pos_lab + pos_cap;  // positions grouped by part
+    // (position, label) grouped by part; starts on an 8-byte boundary whatever pos_cap is
+    int2 *bucket = reinterpret_cast<int2 *>(pos_lab + ((pos_cap + 1) & ~1));
     for (int32_t i = tid; i < table_cap; i += BT) {
         keys[i] = -1;
         cnts[i] = 0;
@@ -1157,7 +1158,7 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
             int32_t base = 0;
             if (p < d && lane == __ffs(peers) - 1) base = atomicAdd(&s_cur[pt], __popc(peers));
             base = __shfl_sync(FULL, base, __ffs(peers) - 1);
-            if (p < d) bucket[base + __popc(peers & lanemask_lt())] = p;
+            if (p < d) bucket[base + __popc(peers & lanemask_lt())] = make_int2(p, pos_lab[p]);
         }
         __syncthreads();
         for (int32_t part = 0; part < parts; ++part) {
@@ -1167,8 +1168,8 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
             // histogram of this part's labels
             for (int32_t j0 = i0; j0 < i1; j0 += BT) {
                 const int32_t j = j0 + tid;
-                const int32_t p = j < i1 ? bucket[j] : -1;
-                const int32_t l = p >= 0 ? pos_lab[p] : -2;
+                const int2 e = j < i1 ? bucket[j] : make_int2(-1, -2);
+                const int32_t p = e.x, l = e.y;
                 const unsigned peers = __match_any_sync(FULL, p >= 0 ? l : -3 - lane);
                 // bucket order is not position order: the group's first position is its minimum
                 const uint32_t pmin = __reduce_min_sync(peers, (uint32_t)p);
@@ -1195,8 +1196,8 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
             __syncthreads();
             // keys of this part's positions
             for (int32_t j = i0 + tid; j < i1; j += BT) {
-                const int32_t p = bucket[j];
-                const int32_t l = pos_lab[p];
+                const int2 e = bucket[j];
+                const int32_t p = e.x, l = e.y;
                 uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
                 int32_t probes = 0;
                 while (probes < ts && keys[h] != l) {
@@ -1897,12 +1898,12 @@ static int launch_bins_rule(pcd_graph *g, const SweepArgs &a, const R &rule, cud
         prof_mark(g->ctx, "sweep.block_l", st);
     }
     if ((c = g->bin_off[BIN_HUB + 1] - g->bin_off[BIN_HUB]) > 0) {
-        // hubs: 1024-thread blocks, shared tables filled part by part, position
-        // arrays in per-block slices of hub_scratch
+        // hubs: 512-thread blocks (two per SM), shared tables filled part by
+        // part, position arrays in per-block slices of hub_scratch
         constexpr int32_t cap = HUB_TABLE_CAP;
         const size_t smem = 3ull * cap * sizeof(int32_t);
         cudaFuncSetAttribute(k_prop_hub_parts<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_prop_hub_parts<R><<<cap_grid(c, g->hub_blocks), 1024, smem, st>>>(
+        k_prop_hub_parts<R><<<cap_grid(c, g->hub_blocks), 512, smem, st>>>(
             a, rule, L + g->bin_off[BIN_HUB], c, cap, HUB_PART_LABELS, g->hub_scratch, hub_stride(g->max_deg),
             g->max_deg);
         ++launches;
