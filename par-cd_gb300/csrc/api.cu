@@ -290,7 +290,7 @@ pcd_status pcd_synchronize(pcd_ctx *ctx) {
 static pcd_status ensure_hub_scratch(pcd_graph *g) {
     pcd_ctx *ctx = g->ctx;
     const int64_t hubs = g->bin_off[NBINS] - g->bin_off[BIN_HUB];
-    const int32_t want = (int32_t)std::min<int64_t>(2ll * ctx->num_sms, hubs);  // two blocks per SM
+    const int32_t want = (int32_t)std::min<int64_t>(ctx->num_sms, hubs);
     if (want <= g->hub_blocks) return PCD_OK;
     const int64_t stride = hub_stride(g->max_deg);
     cudaStream_t st = ctx->stream;
@@ -471,7 +471,7 @@ pcd_status pcd_estimate_device_bytes(int32_t n, int64_t nnz, int32_t max_deg, in
     while (slots < 2 * (int64_t)std::max(max_deg, 1)) slots <<= 1;
     const int64_t fb_stride = 3 * slots + max_deg;
     b += 4 * fb_stride * std::min<int64_t>(8, std::max<int64_t>(1, (1ll << 29) / (4 * fb_stride)));
-    b += 4 * hub_stride(max_deg) * std::min<int64_t>(2ll * num_sms, num_hubs);
+    b += 4 * hub_stride(max_deg) * std::min<int64_t>(num_sms, num_hubs);
     // batch state, the staging copies of a batch load, the seed table of a run
     b += 8 * nn + 8 * (G + 1) + 52 * G + 64;
     b += 4 * (nn + 1) + 4 * e + 8 + 4 * (G + 1) + 4 * nn;

@@ -127,8 +127,8 @@ int launch_validate(const int32_t *indices, const int32_t *adj, int32_t n, int32
                     int32_t *d_flag, cudaStream_t st);
 int launch_bins(pcd_graph *g, cudaStream_t st);
 // hub kernel: shared table slots, distinct labels per part, per-block slice in int32 units
-constexpr int32_t HUB_TABLE_CAP = 8192;   // 96 KiB of table: two blocks per SM
-constexpr int32_t HUB_PART_LABELS = 3072;
+constexpr int32_t HUB_TABLE_CAP = 16384;  // 192 KiB of table: one 1024-thread block per SM
+constexpr int32_t HUB_PART_LABELS = 6144;
 constexpr int32_t HUB_MAX_PARTS = 1024;   // rows above HUB_MAX_PARTS * HUB_PART_LABELS labels fill parts faster
 // per position: an 8-byte key, a 4-byte label and an 8-byte (position, label) bucket entry
 inline int64_t hub_stride(int64_t max_deg) { return (5 * std::max<int64_t>(max_deg, 1) + 3) & ~1ll; }  // fills bin_list / bin_off (syncs)

@@ -1047,7 +1047,7 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
 }
 
 // ---------------------------------------------------------------------------
-// Hubs: one 512-thread block per vertex (two per SM), tables in shared memory.  A hub's
+// Hubs: one 1024-thread block per vertex (one per SM), tables in shared memory.  A hub's
 // labels are split by hash into P parts of at most part_labels distinct
 // labels; each part is histogrammed in the shared table, its first
 // occurrences are keyed, and the table is cleared, before the next part.
@@ -1064,12 +1064,12 @@ __device__ __forceinline__ uint32_t hub_part(uint32_t hv, int32_t parts) {
 }
 
 template <class R>
-__global__ void __launch_bounds__(512, 2) k_prop_hub_parts(SweepArgs a, R rule, const int32_t *__restrict__ list,
-                                                           int64_t count, int32_t table_cap, int32_t part_labels,
-                                                           int32_t *gscratch, int64_t gstride, int32_t pos_cap) {
+__global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, const int32_t *__restrict__ list,
+                                                         int64_t count, int32_t table_cap, int32_t part_labels,
+                                                         int32_t *gscratch, int64_t gstride, int32_t pos_cap) {
     using PK = PackedKey<R>;
     using K = typename PK::K;
-    constexpr int BT = 512, NW = 16;
+    constexpr int BT = 1024, NW = 32;
     extern __shared__ int32_t smem[];
     int32_t *keys = smem;
     int32_t *cnts = smem + table_cap;
@@ -1898,12 +1898,12 @@ static int launch_bins_rule(pcd_graph *g, const SweepArgs &a, const R &rule, cud
         prof_mark(g->ctx, "sweep.block_l", st);
     }
     if ((c = g->bin_off[BIN_HUB + 1] - g->bin_off[BIN_HUB]) > 0) {
-        // hubs: 512-thread blocks (two per SM), shared tables filled part by
+        // hubs: 1024-thread blocks (one per SM), shared tables filled part by
         // part, position arrays in per-block slices of hub_scratch
         constexpr int32_t cap = HUB_TABLE_CAP;
         const size_t smem = 3ull * cap * sizeof(int32_t);
         cudaFuncSetAttribute(k_prop_hub_parts<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_prop_hub_parts<R><<<cap_grid(c, g->hub_blocks), 512, smem, st>>>(
+        k_prop_hub_parts<R><<<cap_grid(c, g->hub_blocks), 1024, smem, st>>>(
             a, rule, L + g->bin_off[BIN_HUB], c, cap, HUB_PART_LABELS, g->hub_scratch, hub_stride(g->max_deg),
             g->max_deg);
         ++launches;
