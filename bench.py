@@ -624,13 +624,15 @@ def main():
     # per-phase profile of one more step (events between kernel groups)
     ctx.profile(True)
     step(0)
-    phases = ctx.profile_read()
+    phases = {}
+    for nm, ms in ctx.profile_read():  # a class may run as several launches (degree sub-ranges)
+        phases[nm] = phases.get(nm, 0.0) + ms
     ctx.profile(False)
     info = G.info()
     bins_now = G.get_bins()
     peak, peak_kind = load_peaks()
     bb = bins_bytes(ind)
-    sweep_phases = {nm: ms for nm, ms in phases if nm.startswith("sweep.")}
+    sweep_phases = {nm: ms for nm, ms in phases.items() if nm.startswith("sweep.")}
     dom = max(((nm, ms) for nm, ms in sweep_phases.items() if nm in bb), key=lambda x: x[1])
     dom_gbs = bb[dom[0]] / (dom[1] / 1e3) / 1e9
     sweep_bytes = 16 * m + 12 * n + 4
@@ -722,7 +724,7 @@ def main():
             "served": served,
             "gpu_launches": int(launches),
             "clocks": clk,
-            "phases_ms": {nm: round(ms, 4) for nm, ms in phases},
+            "phases_ms": {nm: round(ms, 4) for nm, ms in phases.items()},
             "per_sweep_ms": [round(statistics.mean(sweep_ms[j::args.sweeps]), 3)
                              for j in range(min(args.sweeps, len(sweep_ms)))],
             "bins": bins_now,

@@ -357,55 +357,104 @@ __device__ __forceinline__ int32_t bin_of(int32_t d, const BinConfig &b) {
     return NBINS - 1;
 }
 
-struct BinFlag {
+struct SubFlag {
     const int32_t *indices;
     BinConfig cfg;
-    int32_t bin;
-    __device__ uint32_t operator()(int64_t v) const {
-        return bin_of(indices[v + 1] - indices[v], cfg) == bin ? 1u : 0u;
+    int32_t bin, lo, hi;
+    __device__ bool in(int64_t v) const {
+        const int32_t d = indices[v + 1] - indices[v];
+        return d > lo && d <= hi && bin_of(d, cfg) == bin;
     }
+    __device__ uint32_t operator()(int64_t v) const { return in(v) ? 1u : 0u; }
 };
 
-struct BinStore {
-    const int32_t *indices;
-    BinConfig cfg;
-    int32_t bin;
+struct SubStore {
+    SubFlag f;
     int32_t *out;
     __device__ void operator()(int64_t v, uint32_t x, uint32_t) const {
-        if (bin_of(indices[v + 1] - indices[v], cfg) == bin) out[x] = (int32_t)v;
+        if (f.in(v)) out[x] = (int32_t)v;
     }
 };
 
-// the largest degree in each class (sizes the per-class shared tables)
-__global__ void k_bin_maxdeg(const int32_t *__restrict__ indices, int32_t n, BinConfig cfg, int32_t *out) {
-    __shared__ int32_t sm[NBINS];
-    if (threadIdx.x < NBINS) sm[threadIdx.x] = 0;
+constexpr int MAX_SUBS = 16;
+struct SubBounds {
+    int32_t count;
+    int32_t lo[MAX_SUBS], hi[MAX_SUBS];
+};
+
+// the largest degree in each sub-range (sizes the shared tables of its launch)
+__global__ void k_sub_maxdeg(const int32_t *__restrict__ indices, int32_t n, SubBounds sb, int32_t *out) {
+    __shared__ int32_t sm[MAX_SUBS];
+    if (threadIdx.x < MAX_SUBS) sm[threadIdx.x] = 0;
     __syncthreads();
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
         const int32_t d = indices[v + 1] - indices[v];
-        atomicMax(&sm[bin_of(d, cfg)], d);
+        for (int s = 0; s < sb.count; ++s)
+            if (d > sb.lo[s] && d <= sb.hi[s]) {
+                atomicMax(&sm[s], d);
+                break;
+            }
     }
     __syncthreads();
-    if (threadIdx.x < NBINS && sm[threadIdx.x] > 0) atomicMax(&out[threadIdx.x], sm[threadIdx.x]);
+    if (threadIdx.x < MAX_SUBS && sm[threadIdx.x] > 0) atomicMax(&out[threadIdx.x], sm[threadIdx.x]);
 }
 
+// Classes, and inside the warp and block classes sub-ranges at powers of two
+// (warp: 64, 128; block: 512, 1024; large block: 4096), each a stable
+// compaction of the vertices with that degree range.
 int launch_bins(pcd_graph *g, cudaStream_t st) {
     int launches = 0;
-    int32_t *d_max = reinterpret_cast<int32_t *>(g->small);
-    cudaMemsetAsync(d_max, 0, NBINS * sizeof(int32_t), st);
-    k_bin_maxdeg<<<grid_for(g->n, 256), 256, 0, st>>>(g->indices, g->n, g->bins, d_max);
-    cudaMemcpyAsync(g->bin_maxdeg, d_max, NBINS * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
-    ++launches;
-    g->bin_off[0] = 0;
+    std::vector<pcd_graph::SubRange> subs;
     for (int b = 0; b < NBINS; ++b) {
-        launches += scan_exclusive(BinFlag{g->indices, g->bins, b},
-                                   BinStore{g->indices, g->bins, b, g->bin_list + g->bin_off[b]}, g->n,
-                                   g->scan, st);
+        const int32_t lo = b == 0 ? -1 : g->bins.max_deg[b - 1];
+        const int32_t hi = b == NBINS - 1 ? INT_MAX : g->bins.max_deg[b];
+        std::vector<int32_t> cuts;
+        if (b == BIN_WARP) cuts = {64, 128};
+        if (b == BIN_BLOCK) cuts = {512, 1024};
+        if (b == BIN_BLOCK_L) cuts = {4096};
+        int32_t s_lo = lo;
+        for (int32_t c : cuts)
+            if (c > lo && c < hi) {
+                subs.push_back({b, s_lo, c, 0, 0, 0});
+                s_lo = c;
+            }
+        subs.push_back({b, s_lo, hi, 0, 0, 0});
+    }
+    SubBounds sb{};
+    sb.count = (int32_t)subs.size();
+    for (int s = 0; s < sb.count; ++s) {
+        sb.lo[s] = subs[(size_t)s].lo;
+        sb.hi[s] = subs[(size_t)s].hi;
+    }
+    int32_t *d_max = reinterpret_cast<int32_t *>(g->small);
+    cudaMemsetAsync(d_max, 0, MAX_SUBS * sizeof(int32_t), st);
+    k_sub_maxdeg<<<grid_for(g->n, 256), 256, 0, st>>>(g->indices, g->n, sb, d_max);
+    int32_t h_max[MAX_SUBS] = {0};
+    cudaMemcpyAsync(h_max, d_max, MAX_SUBS * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    ++launches;
+    int64_t off = 0;
+    for (int b = 0; b < NBINS; ++b) g->bin_maxdeg[b] = 0;
+    for (size_t s = 0; s < subs.size(); ++s) {
+        auto &r = subs[s];
+        const SubFlag f{g->indices, g->bins, r.bin, r.lo, r.hi};
+        launches += scan_exclusive(f, SubStore{f, g->bin_list + off}, g->n, g->scan, st);
         uint32_t cnt = 0;
         cudaMemcpyAsync(&cnt, g->scan_total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
         cudaStreamSynchronize(st);
-        g->bin_off[b + 1] = g->bin_off[b] + cnt;
+        r.off = off;
+        r.cnt = cnt;
+        r.maxdeg = h_max[s];
+        g->bin_maxdeg[r.bin] = std::max(g->bin_maxdeg[r.bin], r.maxdeg);
+        off += cnt;
     }
+    g->bin_off[0] = 0;
+    for (int b = 0; b < NBINS; ++b) {
+        int64_t end = g->bin_off[b];
+        for (const auto &r : subs)
+            if (r.bin == b) end = r.off + r.cnt;
+        g->bin_off[b + 1] = end;
+    }
+    g->subs = subs;
     return launches;
 }
 

@@ -96,6 +96,14 @@ struct pcd_graph {
     int32_t *bin_list = nullptr;          // vertices grouped by bin
     int64_t bin_off[pcd::NBINS + 1] = {0};
     int32_t bin_maxdeg[pcd::NBINS] = {0};  // largest degree in each class
+    // degree sub-ranges inside the classes (each launched with tables sized to
+    // its own largest degree); a class's sub-ranges tile its part of bin_list
+    struct SubRange {
+        int32_t bin, lo, hi;  // degrees in (lo, hi]
+        int64_t off, cnt;
+        int32_t maxdeg;
+    };
+    std::vector<SubRange> subs;
     pcd::BinConfig bins{};
     // triangles (WCC)
     int32_t *tri = nullptr, *tri_deg = nullptr;
@@ -125,13 +133,13 @@ int launch_stats(pcd_graph *g, cudaStream_t st);
 int launch_score(pcd_graph *g, int32_t kind, double lambda, double *d_out, cudaStream_t st);
 int launch_validate(const int32_t *indices, const int32_t *adj, int32_t n, int32_t m,
                     int32_t *d_flag, cudaStream_t st);
-int launch_bins(pcd_graph *g, cudaStream_t st);
+int launch_bins(pcd_graph *g, cudaStream_t st);  // fills bin_list, bin_off, subs (syncs)
 // hub kernel: shared table slots, distinct labels per part, per-block slice in int32 units
 constexpr int32_t HUB_TABLE_CAP = 16384;  // 192 KiB of table: one 1024-thread block per SM
 constexpr int32_t HUB_PART_LABELS = 6144;
 constexpr int32_t HUB_MAX_PARTS = 1024;   // rows above HUB_MAX_PARTS * HUB_PART_LABELS labels fill parts faster
 // per position: an 8-byte key, a 4-byte label and an 8-byte (position, label) bucket entry
-inline int64_t hub_stride(int64_t max_deg) { return (5 * std::max<int64_t>(max_deg, 1) + 3) & ~1ll; }  // fills bin_list / bin_off (syncs)
+inline int64_t hub_stride(int64_t max_deg) { return (5 * std::max<int64_t>(max_deg, 1) + 3) & ~1ll; }
 
 // propagate.cu
 int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32_t seed,

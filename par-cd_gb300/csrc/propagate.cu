@@ -1832,6 +1832,18 @@ static void launch_group(pcd_graph *g, const SweepArgs &a, const R &rule, int bi
     prof_mark(g->ctx, name, st);
 }
 
+// Warp per vertex for degrees up to WCAP: shared tables of 8 warps per block.
+template <class R, int WCAP>
+static void launch_warp(pcd_graph *g, const SweepArgs &a, const R &rule, const int32_t *list, int64_t c,
+                        cudaStream_t st) {
+    const size_t smem = 8ull * (2 * 2 * WCAP + 4 * WCAP) * sizeof(int32_t);
+    cudaFuncSetAttribute(k_prop_warp<R, WCAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_prop_warp<R, WCAP>, 256, smem);
+    k_prop_warp<R, WCAP><<<cap_grid((c + 7) / 8, (int64_t)g->ctx->num_sms * std::max(1, per_sm)), 256, smem, st>>>(
+        a, rule, list, c, nullptr);
+}
+
 // One-pass block kernel for a class whose largest degree is dmax: the table
 // holds 2 dmax slots rounded up to a power of two, so small classes keep many
 // blocks resident per SM.
@@ -1869,33 +1881,32 @@ static int launch_bins_rule(pcd_graph *g, const SweepArgs &a, const R &rule, cud
     launch_thread<R, 8>(g, a, rule, BIN_G8, "sweep.g8", st, &launches);
     launch_thread<R, 16>(g, a, rule, BIN_G16, "sweep.g16", st, &launches);
     launch_thread<R, 32>(g, a, rule, BIN_G32, "sweep.g32", st, &launches);
-    if ((c = g->bin_off[BIN_WARP + 1] - g->bin_off[BIN_WARP]) > 0) {
-        const size_t smem = 8ull * (2 * 2 * WARP_CAP + 4 * WARP_CAP) * sizeof(int32_t);
-        cudaFuncSetAttribute(k_prop_warp<R, WARP_CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_prop_warp<R, WARP_CAP><<<cap_grid((c + 7) / 8, sms * 8), 256, smem, st>>>(
-            a, rule, L + g->bin_off[BIN_WARP], c, nullptr);
-        ++launches;
-        prof_mark(g->ctx, "sweep.warp", st);
-    }
-    if ((c = g->bin_off[BIN_BLOCK + 1] - g->bin_off[BIN_BLOCK]) > 0) {
-        const int32_t dm = std::max(1, g->bin_maxdeg[BIN_BLOCK]), *lst = L + g->bin_off[BIN_BLOCK];
-        if (dm <= 512)
+    // warp and block classes: one launch per degree sub-range, tables sized to its largest degree
+    for (const auto &sr : g->subs) {
+        if (sr.cnt <= 0 || sr.bin < BIN_WARP || sr.bin > BIN_BLOCK_L) continue;
+        const int32_t dm = std::max(1, sr.maxdeg), *lst = L + sr.off;
+        c = sr.cnt;
+        if (sr.bin == BIN_WARP) {
+            if (dm <= 64)
+                launch_warp<R, 64>(g, a, rule, lst, c, st);
+            else if (dm <= 128)
+                launch_warp<R, 128>(g, a, rule, lst, c, st);
+            else
+                launch_warp<R, WARP_CAP>(g, a, rule, lst, c, st);
+        } else if (dm <= 512) {
             launch_block1<R, 256, 2>(g, a, rule, lst, c, dm, st);
-        else if (dm <= 1024)
+        } else if (dm <= 1024) {
             launch_block1<R, 256, 4>(g, a, rule, lst, c, dm, st);
-        else
+        } else if (dm <= 2048) {
             launch_block1<R, 256, 8>(g, a, rule, lst, c, dm, st);
-        ++launches;
-        prof_mark(g->ctx, "sweep.block", st);
-    }
-    if ((c = g->bin_off[BIN_BLOCK_L + 1] - g->bin_off[BIN_BLOCK_L]) > 0) {
-        const int32_t dm = std::max(1, g->bin_maxdeg[BIN_BLOCK_L]), *lst = L + g->bin_off[BIN_BLOCK_L];
-        if (dm <= 4096)
+        } else if (dm <= 4096) {
             launch_block1<R, 512, 8>(g, a, rule, lst, c, dm, st);
-        else
+        } else {
             launch_block1<R, 512, 16>(g, a, rule, lst, c, dm, st);
+        }
         ++launches;
-        prof_mark(g->ctx, "sweep.block_l", st);
+        prof_mark(g->ctx, sr.bin == BIN_WARP ? "sweep.warp" : (sr.bin == BIN_BLOCK ? "sweep.block" : "sweep.block_l"),
+                  st);
     }
     if ((c = g->bin_off[BIN_HUB + 1] - g->bin_off[BIN_HUB]) > 0) {
         // hubs: 1024-thread blocks (one per SM), shared tables filled part by
