@@ -147,7 +147,7 @@ __global__ void k_stats_warp(const int32_t *__restrict__ indices, const int32_t 
             me = indices[v + 1];
         }
         int32_t my_di = 0;
-        const int cnt = (int)min<int64_t>(32, count - base);
+        const int cnt = count - base < 32 ? (int)(count - base) : 32;
         for (int i = 0; i < cnt; ++i) {
             const int32_t l = __shfl_sync(FULL, ml, i), b = __shfl_sync(FULL, mb, i), e = __shfl_sync(FULL, me, i);
             int32_t di = 0;
