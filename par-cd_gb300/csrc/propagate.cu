@@ -876,7 +876,7 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
             continue;
         }
         int32_t ts = 64;
-        while (2 * ts < 3 * d) ts <<= 1;  // load factor at most 2/3
+        while (ts < 2 * d) ts <<= 1;
         if (ts > table_cap || d > NW * 32 * RPL) {  // binned past its table: never expected
             if (tid == 0) atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);
             continue;
@@ -1845,13 +1845,13 @@ static void launch_warp(pcd_graph *g, const SweepArgs &a, const R &rule, const i
 }
 
 // One-pass block kernel for a class whose largest degree is dmax: the table
-// holds 1.5 dmax slots rounded up to a power of two, so small classes keep
-// many blocks resident per SM.
+// holds 2 dmax slots rounded up to a power of two, so small classes keep many
+// blocks resident per SM.
 template <class R, int BT, int RPL>
 static void launch_block1(pcd_graph *g, const SweepArgs &a, const R &rule, const int32_t *list, int64_t c,
                           int32_t dmax, cudaStream_t st) {
     int32_t cap = 64;
-    while (2 * cap < 3 * dmax) cap <<= 1;
+    while (cap < 2 * dmax) cap <<= 1;
     const size_t smem = (3ull * cap + (size_t)BT * RPL) * sizeof(int32_t);
     cudaFuncSetAttribute(k_prop_block1<R, BT, RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 1;
