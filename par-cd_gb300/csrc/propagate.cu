@@ -1683,66 +1683,38 @@ __global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gse
             // state); its end state is the next round's x.
             const int cnt = min(32, v1 - c0);
             uint32_t dmask = 0;
-            // this lane's path maps of a round: state before each of its 5
-            // vertices, and after the round (tie maps picked with selects, no
-            // branch on the lane's bits)
-            auto path_maps = [&](int r0, uint32_t *Am, uint32_t *Cm, uint32_t &AE, uint32_t &CE) {
-                uint32_t A = 1u, C = 0u;
-#pragma unroll
-                for (int i = 0; i < 5; ++i) {
-                    Am[i] = A;
-                    Cm[i] = C;
-                    const bool bit = (lane >> i) & 1;
-                    const int j = min(r0 + i, 31);
-                    const uint32_t ta = bit ? sa[j] : 1u, tc = bit ? sc[j] : 0u;
-                    const uint32_t ja = WalkStep::A3 * A, jc = WalkStep::A3 * C + WalkStep::C3;
-                    A = ta * ja;
-                    C = ta * jc + tc;
-                    if (i == min(5, cnt - r0) - 1) {
-                        AE = A;
-                        CE = C;
-                    }
-                }
-            };
-            uint32_t Am[5], Cm[5], AE = 1u, CE = 0u;
-            path_maps(0, Am, Cm, AE, CE);
             for (int r0 = 0; r0 < cnt; r0 += 5) {
                 const int k = min(5, cnt - r0);
-                bool ok = true, rare = false;
+                uint32_t A = 1u, C = 0u;  // state before vertex r0 + i along this lane's path
+                bool ok = true;
 #pragma unroll
                 for (int i = 0; i < 5; ++i) {
-                    const uint32_t xi = Am[i] * x + Cm[i];
-                    const uint32_t hi = ((16u * WalkStep::A1) * xi + 16u * WalkStep::C1) & 0x7FF00000u;
-                    const bool bit = (lane >> i) & 1;
-                    ok = ok && (i >= k || (hi < fhi) == bit);
-                    rare = rare || (i < k && hi == fhi);
-                }
-                if (__any_sync(FULL, rare)) {  // one draw in 2048: the low bits decide
-                    ok = true;
-#pragma unroll
-                    for (int i = 0; i < 5; ++i) {
-                        const uint32_t xi = Am[i] * x + Cm[i];
+                    if (i < k) {
+                        const uint32_t xi = A * x + C;
                         const uint32_t s1 = (16u * WalkStep::A1) * xi + 16u * WalkStep::C1;
-                        const uint32_t s2 = WalkStep::A2 * xi + WalkStep::C2;
-                        const uint32_t s3 = WalkStep::A3 * xi + WalkStep::C3;
-                        const uint32_t val = (s1 & 0x7FF00000u) | ((s2 >> 6) & 0x000FFC00u) | ((s3 >> 16) & 0x3FFu);
-                        ok = ok && (i >= k || (val <= uf) == (bool)((lane >> i) & 1));
+                        const uint32_t hi = s1 & 0x7FF00000u;
+                        bool d = hi < fhi;
+                        if (hi == fhi) {  // one case in 2048: the low bits decide
+                            const uint32_t s2 = WalkStep::A2 * xi + WalkStep::C2;
+                            const uint32_t s3 = WalkStep::A3 * xi + WalkStep::C3;
+                            d = (hi | ((s2 >> 6) & 0x000FFC00u) | ((s3 >> 16) & 0x3FFu)) <= uf;
+                        }
+                        const bool bit = (lane >> i) & 1;
+                        ok = ok && d == bit;
+                        const uint32_t ja = WalkStep::A3 * A, jc = WalkStep::A3 * C + WalkStep::C3;  // the frac draw
+                        if (bit) {  // then its tie draws
+                            const uint32_t ta_i = sa[r0 + i], tc_i = sc[r0 + i];
+                            A = ta_i * ja;
+                            C = ta_i * jc + tc_i;
+                        } else {
+                            A = ja;
+                            C = jc;
+                        }
                     }
                 }
-                const uint32_t xe = AE * x + CE;
-                // the next round's maps do not depend on x: built while the vote resolves
-                uint32_t An[5], Cn[5], AEn = 1u, CEn = 0u;
-                if (r0 + 5 < cnt) path_maps(r0 + 5, An, Cn, AEn, CEn);
                 const int w = __ffs(__ballot_sync(FULL, ok)) - 1;  // lanes equal in the k low bits agree
-                x = __shfl_sync(FULL, xe, w);
+                x = __shfl_sync(FULL, A * x + C, w);
                 dmask |= ((uint32_t)w & ((1u << k) - 1u)) << r0;
-#pragma unroll
-                for (int i = 0; i < 5; ++i) {
-                    Am[i] = An[i];
-                    Cm[i] = Cn[i];
-                }
-                AE = AEn;
-                CE = CEn;
             }
             // each vertex's end position: the chunk start, one frac draw per
             // vertex so far, the tie draws of the vertices that drew
