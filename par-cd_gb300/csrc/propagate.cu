@@ -1674,63 +1674,32 @@ __global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gse
             sa[lane] = ta;
             sc[lane] = tc;
             __syncwarp();
-            // Lookahead: 5 vertices per round.  Lane L assumes the frac
-            // decisions of the round's vertices are the bits of L; its path is
-            // an affine map of the round's start state x, composed without x,
-            // so all 32 paths are evaluated from x at once.  The lane whose
-            // assumed decisions match the ones its states produce is the true
-            // path (a path that deviates meets its first wrong bit at a true
-            // state); its end state is the next round's x.
-            const int cnt = min(32, v1 - c0);
-            uint32_t dmask = 0;
-            for (int r0 = 0; r0 < cnt; r0 += 5) {
-                const int k = min(5, cnt - r0);
-                uint32_t A = 1u, C = 0u;  // state before vertex r0 + i along this lane's path
-                bool ok = true;
+            uint32_t my_pos = 0;
+            int32_t my_skip = 0;
+            if (v1 - c0 >= 32) {
 #pragma unroll
-                for (int i = 0; i < 5; ++i) {
-                    if (i < k) {
-                        const uint32_t xi = A * x + C;
-                        const uint32_t s1 = (16u * WalkStep::A1) * xi + 16u * WalkStep::C1;
-                        const uint32_t hi = s1 & 0x7FF00000u;
-                        bool d = hi < fhi;
-                        if (hi == fhi) {  // one case in 2048: the low bits decide
-                            const uint32_t s2 = WalkStep::A2 * xi + WalkStep::C2;
-                            const uint32_t s3 = WalkStep::A3 * xi + WalkStep::C3;
-                            d = (hi | ((s2 >> 6) & 0x000FFC00u) | ((s3 >> 16) & 0x3FFu)) <= uf;
-                        }
-                        const bool bit = (lane >> i) & 1;
-                        ok = ok && d == bit;
-                        const uint32_t ja = WalkStep::A3 * A, jc = WalkStep::A3 * C + WalkStep::C3;  // the frac draw
-                        if (bit) {  // then its tie draws
-                            const uint32_t ta_i = sa[r0 + i], tc_i = sc[r0 + i];
-                            A = ta_i * ja;
-                            C = ta_i * jc + tc_i;
-                        } else {
-                            A = ja;
-                            C = jc;
-                        }
+                for (int j = 0; j < 32; ++j) {
+                    const bool d = WalkStep::step(x, uf, fhi, sa[j], sc[j]);
+                    pos += d ? 1u + st[j] : 1u;
+                    if (lane == j) {
+                        my_pos = pos;
+                        my_skip = d ? 0 : 1;
                     }
                 }
-                const int w = __ffs(__ballot_sync(FULL, ok)) - 1;  // lanes equal in the k low bits agree
-                x = __shfl_sync(FULL, A * x + C, w);
-                dmask |= ((uint32_t)w & ((1u << k) - 1u)) << r0;
+            } else {
+                for (int j = 0; j < v1 - c0; ++j) {
+                    const bool d = WalkStep::step(x, uf, fhi, sa[j], sc[j]);
+                    pos += d ? 1u + st[j] : 1u;
+                    if (lane == j) {
+                        my_pos = pos;
+                        my_skip = d ? 0 : 1;
+                    }
+                }
             }
-            // each vertex's end position: the chunk start, one frac draw per
-            // vertex so far, the tie draws of the vertices that drew
-            const bool drew = (dmask >> lane) & 1u;
-            uint32_t ties = lane < cnt && drew ? t : 0u;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(FULL, ties, o);
-                if (lane >= o) ties += y;
-            }
-            const uint32_t end = pos + (uint32_t)(lane + 1) + ties;
             if (v < v1) {
-                ndraw[v] = end;
-                skip[v] = drew ? 0 : 1;
+                ndraw[v] = my_pos;
+                skip[v] = my_skip;
             }
-            pos = __shfl_sync(FULL, end, cnt - 1);
         }
         if (!voff && lane == 0) ctr->total_draws = pos;
     }
