@@ -126,36 +126,28 @@ __global__ void k_stats_thread(const int32_t *__restrict__ indices, const int32_
     }
 }
 
-// Warp per vertex for the larger degrees, 32 vertices per warp step: lane i
-// fetches vertex i's label and row bounds, the warp counts each row's
-// internal endpoints in turn, then the 32 results go through add_stats so that
-// vertices of one community add once (large communities would otherwise
-// serialise on their counters).
+// Warp per vertex for the larger degrees; lane 0 adds the vertex's counts.
 __global__ void k_stats_warp(const int32_t *__restrict__ indices, const int32_t *__restrict__ adj,
                              const int32_t *__restrict__ labels, const int32_t *__restrict__ list,
                              int64_t count, int32_t *sizes, int32_t *intv, int32_t *extv, int32_t *vol) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t base = warp * 32; base < count; base += nwarps * 32) {
-        const bool valid = base + lane < count;
-        int32_t ml = 0, mb = 0, me = 0;
-        if (valid) {
-            const int32_t v = list[base + lane];
-            ml = labels[v];
-            mb = indices[v];
-            me = indices[v + 1];
+    for (int64_t idx = warp; idx < count; idx += nwarps) {
+        int32_t v = list[idx];
+        int32_t l = labels[v];
+        int32_t b = indices[v], e = indices[v + 1];
+        int32_t di = 0;
+        for (int32_t j = b + lane; j < e; j += 32) di += (labels[adj[j]] == l);
+#pragma unroll
+        for (int d = 16; d; d >>= 1) di += __shfl_xor_sync(FULL, di, d);
+        if (lane == 0) {
+            int32_t de = (e - b) - di;
+            atomicAdd(sizes + l, 1);
+            atomicAdd(intv + l, di);
+            atomicAdd(extv + l, de);
+            atomicAdd(vol + l, e - b);
         }
-        int32_t my_di = 0;
-        const int cnt = count - base < 32 ? (int)(count - base) : 32;
-        for (int i = 0; i < cnt; ++i) {
-            const int32_t l = __shfl_sync(FULL, ml, i), b = __shfl_sync(FULL, mb, i), e = __shfl_sync(FULL, me, i);
-            int32_t di = 0;
-            for (int32_t j = b + lane; j < e; j += 32) di += (labels[adj[j]] == l);
-            di = __reduce_add_sync(FULL, di);
-            if (lane == i) my_di = di;
-        }
-        add_stats(ml, my_di, (me - mb) - my_di, sizes, intv, extv, vol, valid);
     }
 }
 
