@@ -218,6 +218,21 @@ pcd_status pcd_batch_run(pcd_graph *batch, const pcd_rule *rule, int32_t strateg
                          int32_t rounds, int32_t n_iter, double threshold, int32_t use_cuda_graph,
                          double *scores, int32_t *iterations);
 
+/* Edge list -> graph, on the device, with the semantics of the reference
+ * converter (src/convert.cpp:76-196): loops dropped, both directions,
+ * duplicates removed, vertices renumbered by (degree, id) descending, rows
+ * sorted, vertices without neighbours dropped.  src/dst: num_edges host int32
+ * ids >= 0; num_nodes = -1 takes the largest id + 1 (src/convert.cpp:61).
+ * map (host, may be NULL, room for num_nodes or the largest id + 1): the
+ * original id of each new vertex.  The result is loaded as a graph;
+ * pcd_graph_size / pcd_graph_csr_get read it back (e.g. to write a "PCD"
+ * file).  Replaces the reference's host converter for large inputs. */
+pcd_status pcd_convert_edges(pcd_ctx *ctx, int64_t num_edges, const int32_t *src, const int32_t *dst,
+                             int32_t num_nodes, int32_t *map, pcd_graph **out);
+pcd_status pcd_graph_size(pcd_graph *g, int32_t *n, int32_t *m);
+/* Host arrays of n + 1 and 2m int32. */
+pcd_status pcd_graph_csr_get(pcd_graph *g, int32_t *indices, int32_t *adj);
+
 /* ------------------------------------------------------------------------
  * Serving loop.  No counterpart in the reference (its drivers run one graph
  * per process, src/main.cpp).  Requests -- a graph and a driver schedule --

@@ -21,7 +21,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpcd.so")
 MAIN = os.path.join(HERE, "main-cuda")
-SOURCES = ["api.cu", "partition.cu", "propagate.cu", "merge.cu", "triangles.cu", "batch.cu", "noalloc.cu", "hostside.cpp", "serve.cpp"]
+CONVERT = os.path.join(HERE, "convert-cuda")
+SOURCES = ["api.cu", "partition.cu", "propagate.cu", "merge.cu", "triangles.cu", "batch.cu", "noalloc.cu", "convert.cu", "hostside.cpp", "serve.cpp"]
 HEADERS = ["pcd_device.cuh", "pcd_scan.cuh", "pcd_internal.h", "pcd_types.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -80,12 +81,14 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.run(cmd, check=True)
-    main_src = os.path.join(CSRC, "main_cuda.cpp")
-    if force or _stale(MAIN, [main_src, LIB]):
-        cmd = ["g++", "-O2", "-std=c++17", "-o", MAIN, main_src, "-L", HERE, "-lpcd", "-Wl,-rpath,$ORIGIN"]
-        if verbose:
-            print(" ".join(cmd), flush=True)
-        subprocess.run(cmd, check=True)
+    for exe, src in ((MAIN, "main_cuda.cpp"), (CONVERT, "convert_cuda.cpp")):
+        src = os.path.join(CSRC, src)
+        if force or _stale(exe, [src, LIB]):
+            cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(HERE, "..", "include"), "-o", exe, src, "-L",
+                   HERE, "-lpcd", "-Wl,-rpath,$ORIGIN"]
+            if verbose:
+                print(" ".join(cmd), flush=True)
+            subprocess.run(cmd, check=True)
     return LIB
 
 

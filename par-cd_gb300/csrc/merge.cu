@@ -110,9 +110,8 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const unsigned long l
 
 // Sorts keys/vals (n items, significant bits [0, bits)); ping-pongs between
 // the A and B buffers and returns true if the result ended in B.
-static bool radix_sort(unsigned long long *ka, uint32_t *va, unsigned long long *kb, uint32_t *vb, int64_t n,
-                       int bits, uint32_t *hist, const ScanScratch &sc, int grid, cudaStream_t st,
-                       int *launches) {
+bool radix_sort(unsigned long long *ka, uint32_t *va, unsigned long long *kb, uint32_t *vb, int64_t n, int bits,
+                uint32_t *hist, const ScanScratch &sc, int grid, cudaStream_t st, int *launches) {
     if (n <= 1 || bits <= 0) return false;
     const int64_t chunk = ((n + grid - 1) / grid + RS_THREADS - 1) / RS_THREADS * RS_THREADS;
     const int g = (int)((n + chunk - 1) / chunk);

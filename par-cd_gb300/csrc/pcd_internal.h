@@ -134,6 +134,11 @@ int launch_score(pcd_graph *g, int32_t kind, double lambda, double *d_out, cudaS
 int launch_validate(const int32_t *indices, const int32_t *adj, int32_t n, int32_t m,
                     int32_t *d_flag, cudaStream_t st);
 int launch_bins(pcd_graph *g, cudaStream_t st);  // fills bin_list, bin_off, subs (syncs)
+// Stable LSD radix sort of (uint64 key, uint32 value) pairs on bits [0, bits),
+// 8 bits per pass, ping-ponging between A and B; true if the result is in B.
+// hist: 256 * grid words; sc: scratch for scans of 256 * grid items.
+bool radix_sort(unsigned long long *ka, uint32_t *va, unsigned long long *kb, uint32_t *vb, int64_t n, int bits,
+                uint32_t *hist, const pcd::ScanScratch &sc, int grid, cudaStream_t st, int *launches);
 // hub kernel: shared table slots, distinct labels per part, per-block slice in int32 units
 constexpr int32_t HUB_TABLE_CAP = 16384;  // 192 KiB of table: one 1024-thread block per SM
 constexpr int32_t HUB_PART_LABELS = 6144;

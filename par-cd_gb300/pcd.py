@@ -110,6 +110,9 @@ def _load() -> C.CDLL:
         "pcd_batch_run": ([vp, C.POINTER(_Rule), i32, dbl, i32, i32, dbl, i32, vp, vp], i32),
         "pcd_compress_labels_noalloc": ([vp, i32, vp, vp, vp], i32),
         "pcd_graph_device_bytes": ([vp, C.POINTER(i64)], i32),
+        "pcd_convert_edges": ([vp, i64, vp, vp, i32, vp, C.POINTER(vp)], i32),
+        "pcd_graph_size": ([vp, C.POINTER(i32), C.POINTER(i32)], i32),
+        "pcd_graph_csr_get": ([vp, vp, vp], i32),
         "pcd_estimate_device_bytes": ([i32, i64, i32, i64, i32, i32, i32, i32, C.POINTER(i64)], i32),
         "pcd_device_sm_count": ([vp, C.POINTER(i32)], i32),
         "pcd_serve_start": ([C.POINTER(_ServeConfig), C.POINTER(vp)], i32),
@@ -347,6 +350,13 @@ class Graph:
         w = np.zeros(max(P, 1), np.int32)
         self.ctx._check(LIB.pcd_contract(self.h, P, _ptr(a), _ptr(b), _ptr(w), C.byref(npairs)))
         return a[:P], b[:P], w[:P]
+
+    def csr(self):
+        """The graph's CSR as host arrays (indices[n + 1], adj[2m])."""
+        ind = np.empty(self.n + 1, np.int32)
+        adj = np.empty(max(2 * self.m, 1), np.int32)
+        self.ctx._check(LIB.pcd_graph_csr_get(self.h, _ptr(ind), _ptr(adj)))
+        return ind, adj[: 2 * self.m]
 
     def set_bins(self, max_deg):
         arr = (C.c_int32 * 7)(*[int(x) for x in max_deg])
@@ -667,3 +677,19 @@ class Server:
 
     def __exit__(self, *exc):
         self.stop()
+
+
+def convert_edges(ctx: Context, edges, num_nodes: int = -1):
+    """Edge list -> (Graph, map) on the device with the reference converter's
+    semantics (pcd_convert_edges); map[i] is the original id of vertex i."""
+    e = np.ascontiguousarray(np.asarray(edges).reshape(-1, 2), dtype=np.int32)
+    src = np.ascontiguousarray(e[:, 0])
+    dst = np.ascontiguousarray(e[:, 1])
+    nmax = num_nodes if num_nodes >= 0 else (int(e.max()) + 1 if e.size else 0)
+    mp = np.empty(max(nmax, 1), np.int32)
+    h = C.c_void_p()
+    ctx._check(LIB.pcd_convert_edges(ctx.h, e.shape[0], _ptr(src), _ptr(dst), int(num_nodes), _ptr(mp),
+                                     C.byref(h)))
+    n, m = C.c_int32(), C.c_int32()
+    LIB.pcd_graph_size(h, C.byref(n), C.byref(m))
+    return Graph(ctx, h, n.value, m.value), mp[: n.value].copy()

@@ -59,3 +59,18 @@ def test_main_cuda_matches_oracle(tmp_path, port, args, metric, strategy, rounds
     assert np.array_equal(dump[:, 1], final)
     assert f"iteration {n_iter + 1}:" in r.stdout
     assert f"num. communities: {int(final.max()) + 1}" in r.stdout
+
+
+def test_convert_cuda_rejects_bad_input(tmp_path):
+    import build
+
+    build.build()
+    exe = os.path.join(ROOT, "par-cd_gb300", "convert-cuda")
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 255
+    bad = tmp_path / "bad.txt"
+    bad.write_text("1 2\n3 x\n")
+    r = subprocess.run([exe, str(bad), str(tmp_path / "o.bin")], capture_output=True, text=True)
+    assert r.returncode == 255 and "line 2 is corrupt" in r.stderr
+    r = subprocess.run([exe, str(tmp_path / "missing.txt"), str(tmp_path / "o.bin")], capture_output=True, text=True)
+    assert r.returncode == 255
