@@ -360,6 +360,49 @@ def batched_leg(args, ctx, dev):
     }
 
 
+def convert_leg(args, dev, ind, adj):
+    """The converter on the GPU: the workload's raw R-MAT edge list (loops and
+    duplicates included) from host memory through pcd_convert_edges, timed
+    end to end (H2D copy, sorts, CSR, load as a graph); its CSR must equal the
+    workload's.  CPU: the host restatement of the reference converter on the
+    scale-20 edge list of the same generator."""
+    import numpy as np
+    import torch
+
+    import graphs
+    import pcd
+
+    src, dst = graphs.rmat_edges_torch(args.scale, args.edge_factor, 0.57, 0.19, 0.19, seed=2, device=dev)
+    e = torch.stack([src, dst], 1).to(torch.int32).cpu().numpy()
+    del src, dst
+    torch.cuda.empty_cache()
+    ctx = pcd.Context(0)
+    g, _ = pcd.convert_edges(ctx, e[:1000])  # warm-up
+    g.free()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    g, mp = pcd.convert_edges(ctx, e)
+    sec = time.perf_counter() - t
+    gi, ga = g.csr()
+    same = bool(np.array_equal(gi, ind) and np.array_equal(ga, adj))
+    g.free()
+    ctx.close()
+    out = {"edges_in": int(e.shape[0]), "n": int(gi.shape[0] - 1), "m": int(ga.shape[0] // 2),
+           "seconds": sec, "input_edges_per_s": e.shape[0] / sec, "same_csr_as_workload": same}
+    if not args.no_cpu:
+        src, dst = graphs.rmat_edges_torch(20, args.edge_factor, 0.57, 0.19, 0.19, seed=2, device=dev)
+        e20 = torch.stack([src, dst], 1).cpu().numpy()
+        t = time.perf_counter()
+        graphs.convert_edges(e20, 1 << 20)
+        c = time.perf_counter() - t
+        out["cpu_baseline"] = {"value": e20.shape[0] / c, "unit": "input edges/s", "cores": 1, "kind": "port",
+                               "sample": f"R-MAT s20 edge list ({e20.shape[0]} edges), numpy restatement of the "
+                                         f"reference converter, {c:.1f}s"}
+    assert same, "the GPU converter's CSR differs from the workload's"
+    log(f"[bench] convert: {e.shape[0]} edges in {sec:.2f}s")
+    return out
+
+
 def serve_pool(dev):
     """The served mix's graphs (seed 5): SBMs with log-uniform sizes in
     [1000, 50000] (n/50 blocks, intra-degree 12, inter-degree 2), LFR-style
@@ -515,6 +558,7 @@ def main():
     ap.add_argument("--batch-frac", type=float, default=0.5)
     ap.add_argument("--batch-iters", type=int, default=-1)
     ap.add_argument("--batch-threshold", type=float, default=0.0)
+    ap.add_argument("--convert", type=int, default=1, help="0: skip the converter timing")
     ap.add_argument("--serve-requests", type=int, default=600, help="0: skip the served workload")
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[200.0, 2000.0])
     ap.add_argument("--serve-workers", type=int, default=4)
@@ -684,6 +728,11 @@ def main():
         torch.cuda.empty_cache()
         batched = batched_leg(args, ctx, dev)
 
+    converted = None
+    if args.convert:
+        torch.cuda.empty_cache()
+        converted = convert_leg(args, dev, ind, adj)
+
     served = None
     if args.serve_requests > 0:
         torch.cuda.empty_cache()
@@ -722,6 +771,7 @@ def main():
             "e2e": e2e,
             "batched": batched,
             "served": served,
+            "convert": converted,
             "gpu_launches": int(launches),
             "clocks": clk,
             "phases_ms": {nm: round(ms, 4) for nm, ms in phases.items()},

@@ -265,8 +265,15 @@ def rmat(scale: int, edge_factor: int, a: float, b: float, c: float, seed: int) 
 def rmat_torch(scale: int, edge_factor: int, a: float, b: float, c: float, seed: int,
                device="cuda"):
     """R-MAT generated on a device with torch (input generation for the large
-    benchmark workloads only).  Returns (indices, adj, n, m) as numpy int32 with
+    benchmark workloads only).  Returns (indices, adj, map) as numpy int32 with
     the converter's semantics (degree-sorted, isolated vertices dropped)."""
+    src, dst = rmat_edges_torch(scale, edge_factor, a, b, c, seed, device)
+    return csr_from_edges_torch(src, dst, 1 << scale)
+
+
+def rmat_edges_torch(scale: int, edge_factor: int, a: float, b: float, c: float, seed: int, device="cuda"):
+    """The raw R-MAT edge list of rmat_torch (with loops and duplicates), as
+    two int64 device tensors."""
     import torch
 
     gen = torch.Generator(device=device)
@@ -290,7 +297,7 @@ def rmat_torch(scale: int, edge_factor: int, a: float, b: float, c: float, seed:
     src = perm[src]
     dst = perm[dst]
     del perm
-    return csr_from_edges_torch(src, dst, n)
+    return src, dst
 
 
 def csr_from_edges_torch(src, dst, n):
