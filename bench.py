@@ -18,6 +18,12 @@ Lines printed (rank 0, one JSON line):
   roofline   the sweep's dominant kernel against the measured HBM copy peak
   cpu_baseline  the oracle (C restatement of the reference, OpenMP) on the
              host cores, on the same graph
+  batched    4096 log-normal SBMs through pcd_batch_run vs the single-graph
+             path looped over a sample vs the oracle driver loop on the CPU
+  served     Poisson arrivals (SBM / power-law / R-MAT s22 mix) through the
+             serving loop vs the single-graph path one request at a time:
+             graphs/s and latency percentiles
+  convert    the workload's raw edge list through the GPU converter
 With --impl reference: the reference's CPU path for this sweep (the oracle
 restatement; the reference's own objects cannot run on this host) on all host
 cores, same metric and workload.
