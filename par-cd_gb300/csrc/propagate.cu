@@ -1078,7 +1078,7 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
     __shared__ K s_agg[NW];
     __shared__ uint32_t s_t[NW];
     __shared__ int32_t s_nfin[NW];
-    __shared__ int32_t s_amb, s_curr_freq, s_distinct;
+    __shared__ int32_t s_amb, s_curr_freq;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     K *pos_key = reinterpret_cast<K *>(gscratch + (int64_t)blockIdx.x * gstride);
     int32_t *pos_lab = reinterpret_cast<int32_t *>(pos_key + pos_cap);
@@ -1103,12 +1103,14 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
             if (tid == 0) atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);
             continue;
         }
+        const int32_t parts = min(HUB_MAX_PARTS, max(1, (d + part_labels - 1) / part_labels));
+        for (int32_t i = tid; i < parts; i += BT) s_cur[i] = 0;
         if (tid == 0) {
             s_amb = 0;
             s_curr_freq = 0;
-            s_distinct = 0;
         }
-        // the row's labels by position, gathered once
+        __syncthreads();
+        // the row's labels by position (gathered once) and the part sizes
         for (int32_t p0 = 0; p0 < d; p0 += BT * 4) {
             int32_t l[4];
 #pragma unroll
@@ -1119,53 +1121,91 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int32_t p = p0 + u * BT + tid;
-                if (p < d) pos_lab[p] = a.labels[l[u]];
+                int32_t pt = -1 - lane;
+                if (p < d) {
+                    l[u] = a.labels[l[u]];
+                    pos_lab[p] = l[u];
+                    pt = (int32_t)hub_part(hash_label(l[u]), parts);
+                }
+                const unsigned peers = __match_any_sync(FULL, pt);
+                if (p < d && lane == __ffs(peers) - 1) atomicAdd(&s_cur[pt], __popc(peers));
             }
         }
         __syncthreads();
-        // first the whole row in one table; inserts stop once half of it is
-        // used (rows with more distinct labels go through the parts below)
-        int32_t ts1 = 64;
-        while (ts1 < 2 * d && ts1 < table_cap) ts1 <<= 1;
-        const int32_t limit = ts1 / 2;
-        for (int32_t p0 = 0; p0 < d; p0 += BT) {
+        if (wid == 0) {  // exclusive scan of the part sizes
+            int32_t carry = 0;
+            for (int32_t i0 = 0; i0 < parts; i0 += 32) {
+                const int32_t i = i0 + lane;
+                const int32_t c = i < parts ? s_cur[i] : 0;
+                int32_t inc = c;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int32_t y = __shfl_up_sync(FULL, inc, o);
+                    if (lane >= o) inc += y;
+                }
+                if (i < parts) s_start[i] = carry + inc - c;
+                carry += __shfl_sync(FULL, inc, 31);
+            }
+            if (lane == 0) s_start[parts] = carry;
+        }
+        __syncthreads();
+        for (int32_t i = tid; i < parts; i += BT) s_cur[i] = s_start[i];
+        __syncthreads();
+        for (int32_t p0 = 0; p0 < d; p0 += BT) {  // positions into their part's bucket
             const int32_t p = p0 + tid;
-            const int32_t l = p < d ? pos_lab[p] : -2;
-            const unsigned peers = __match_any_sync(FULL, p < d ? l : -3 - lane);
-            if (p < d && lane == __ffs(peers) - 1 && s_distinct <= limit) {  // lowest lane = first position
-                uint32_t h = hash_label(l) & (uint32_t)(ts1 - 1);
-                int32_t probes = 0;
-                for (; probes < ts1; ++probes) {
-                    const int32_t kk = keys[h];
-                    if (kk == l) break;
-                    if (kk == -1) {
-                        const int32_t old = atomicCAS(&keys[h], -1, l);
-                        if (old == -1) atomicAdd(&s_distinct, 1);
-                        if (old == -1 || old == l) break;
-                    }
-                    h = (h + 1) & (uint32_t)(ts1 - 1);
-                }
-                if (probes < ts1) {
-                    atomicAdd(&cnts[h], __popc(peers));
-                    atomicMin(&first[h], (uint32_t)p);
-                } else {
-                    atomicAdd(&s_distinct, limit + 1);  // table full: take the parts
-                }
-            }
+            const int32_t pt = p < d ? (int32_t)hub_part(hash_label(pos_lab[p]), parts) : -1 - lane;
+            const unsigned peers = __match_any_sync(FULL, pt);
+            int32_t base = 0;
+            if (p < d && lane == __ffs(peers) - 1) base = atomicAdd(&s_cur[pt], __popc(peers));
+            base = __shfl_sync(FULL, base, __ffs(peers) - 1);
+            if (p < d) bucket[base + __popc(peers & lanemask_lt())] = make_int2(p, pos_lab[p]);
         }
         __syncthreads();
-        const bool one_table = s_distinct <= limit;
-        if (one_table) {  // keys of every position from the one table
-            for (int32_t p = tid; p < d; p += BT) {
-                const int32_t l = pos_lab[p];
-                uint32_t h = hash_label(l) & (uint32_t)(ts1 - 1);
+        for (int32_t part = 0; part < parts; ++part) {
+            const int32_t i0 = s_start[part], i1 = s_start[part + 1];
+            int32_t ts = 64;
+            while (ts < 2 * (i1 - i0) && ts < table_cap) ts <<= 1;
+            // histogram of this part's labels
+            for (int32_t j0 = i0; j0 < i1; j0 += BT) {
+                const int32_t j = j0 + tid;
+                const int2 e = j < i1 ? bucket[j] : make_int2(-1, -2);
+                const int32_t p = e.x, l = e.y;
+                const unsigned peers = __match_any_sync(FULL, p >= 0 ? l : -3 - lane);
+                // bucket order is not position order: the group's first position is its minimum
+                const uint32_t pmin = __reduce_min_sync(peers, (uint32_t)p);
+                if (p >= 0 && lane == __ffs(peers) - 1) {
+                    uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
+                    int32_t probes = 0;
+                    for (; probes < ts; ++probes) {
+                        const int32_t kk = keys[h];
+                        if (kk == l) break;
+                        if (kk == -1) {
+                            const int32_t old = atomicCAS(&keys[h], -1, l);
+                            if (old == -1 || old == l) break;
+                        }
+                        h = (h + 1) & (uint32_t)(ts - 1);
+                    }
+                    if (probes < ts) {
+                        atomicAdd(&cnts[h], __popc(peers));
+                        atomicMin(&first[h], pmin);
+                    } else {
+                        atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);  // a part overfilled the table
+                    }
+                }
+            }
+            __syncthreads();
+            // keys of this part's positions
+            for (int32_t j = i0 + tid; j < i1; j += BT) {
+                const int2 e = bucket[j];
+                const int32_t p = e.x, l = e.y;
+                uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
                 int32_t probes = 0;
-                while (probes < ts1 && keys[h] != l) {
-                    h = (h + 1) & (uint32_t)(ts1 - 1);
+                while (probes < ts && keys[h] != l) {
+                    h = (h + 1) & (uint32_t)(ts - 1);
                     ++probes;
                 }
                 K key = PK::ident();
-                if (probes < ts1 && first[h] == (uint32_t)p) {
+                if (probes < ts && first[h] == (uint32_t)p) {
                     const int32_t k = cnts[h];
                     if (l == curr) {
                         s_curr_freq = k;
@@ -1178,118 +1218,12 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                 pos_key[p] = key;
             }
             __syncthreads();
-        }
-        for (int32_t i = tid; i < ts1; i += BT) {
-            keys[i] = -1;
-            cnts[i] = 0;
-            first[i] = 0xffffffffu;
-        }
-        __syncthreads();
-        const int32_t parts =
-            one_table ? 0 : min(HUB_MAX_PARTS, max(1, (d + part_labels - 1) / part_labels));
-        if (parts > 0) {  // part sizes
-            for (int32_t i = tid; i < parts; i += BT) s_cur[i] = 0;
-            __syncthreads();
-            for (int32_t p0 = 0; p0 < d; p0 += BT) {
-                const int32_t p = p0 + tid;
-                const int32_t pt = p < d ? (int32_t)hub_part(hash_label(pos_lab[p]), parts) : -1 - lane;
-                const unsigned peers = __match_any_sync(FULL, pt);
-                if (p < d && lane == __ffs(peers) - 1) atomicAdd(&s_cur[pt], __popc(peers));
+            for (int32_t i = tid; i < ts; i += BT) {
+                keys[i] = -1;
+                cnts[i] = 0;
+                first[i] = 0xffffffffu;
             }
             __syncthreads();
-            if (wid == 0) {  // exclusive scan of the part sizes
-                int32_t carry = 0;
-                for (int32_t i0 = 0; i0 < parts; i0 += 32) {
-                    const int32_t i = i0 + lane;
-                    const int32_t c = i < parts ? s_cur[i] : 0;
-                    int32_t inc = c;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int32_t y = __shfl_up_sync(FULL, inc, o);
-                        if (lane >= o) inc += y;
-                    }
-                    if (i < parts) s_start[i] = carry + inc - c;
-                    carry += __shfl_sync(FULL, inc, 31);
-                }
-                if (lane == 0) s_start[parts] = carry;
-            }
-            __syncthreads();
-            for (int32_t i = tid; i < parts; i += BT) s_cur[i] = s_start[i];
-            __syncthreads();
-            for (int32_t p0 = 0; p0 < d; p0 += BT) {  // positions into their part's bucket
-                const int32_t p = p0 + tid;
-                const int32_t pt = p < d ? (int32_t)hub_part(hash_label(pos_lab[p]), parts) : -1 - lane;
-                const unsigned peers = __match_any_sync(FULL, pt);
-                int32_t base = 0;
-                if (p < d && lane == __ffs(peers) - 1) base = atomicAdd(&s_cur[pt], __popc(peers));
-                base = __shfl_sync(FULL, base, __ffs(peers) - 1);
-                if (p < d) bucket[base + __popc(peers & lanemask_lt())] = make_int2(p, pos_lab[p]);
-            }
-            __syncthreads();
-            for (int32_t part = 0; part < parts; ++part) {
-                const int32_t i0 = s_start[part], i1 = s_start[part + 1];
-                int32_t ts = 64;
-                while (ts < 2 * (i1 - i0) && ts < table_cap) ts <<= 1;
-                // histogram of this part's labels
-                for (int32_t j0 = i0; j0 < i1; j0 += BT) {
-                    const int32_t j = j0 + tid;
-                    const int2 e = j < i1 ? bucket[j] : make_int2(-1, -2);
-                    const int32_t p = e.x, l = e.y;
-                    const unsigned peers = __match_any_sync(FULL, p >= 0 ? l : -3 - lane);
-                    // bucket order is not position order: the group's first position is its minimum
-                    const uint32_t pmin = __reduce_min_sync(peers, (uint32_t)p);
-                    if (p >= 0 && lane == __ffs(peers) - 1) {
-                        uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
-                        int32_t probes = 0;
-                        for (; probes < ts; ++probes) {
-                            const int32_t kk = keys[h];
-                            if (kk == l) break;
-                            if (kk == -1) {
-                                const int32_t old = atomicCAS(&keys[h], -1, l);
-                                if (old == -1 || old == l) break;
-                            }
-                            h = (h + 1) & (uint32_t)(ts - 1);
-                        }
-                        if (probes < ts) {
-                            atomicAdd(&cnts[h], __popc(peers));
-                            atomicMin(&first[h], pmin);
-                        } else {
-                            atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);  // a part overfilled the table
-                        }
-                    }
-                }
-                __syncthreads();
-                // keys of this part's positions
-                for (int32_t j = i0 + tid; j < i1; j += BT) {
-                    const int2 e = bucket[j];
-                    const int32_t p = e.x, l = e.y;
-                    uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
-                    int32_t probes = 0;
-                    while (probes < ts && keys[h] != l) {
-                        h = (h + 1) & (uint32_t)(ts - 1);
-                        ++probes;
-                    }
-                    K key = PK::ident();
-                    if (probes < ts && first[h] == (uint32_t)p) {
-                        const int32_t k = cnts[h];
-                        if (l == curr) {
-                            s_curr_freq = k;
-                        } else {
-                            Tag tag{0, 0};
-                            const typename R::Key raw = vr.join(v, d, l, k, a.cm, tag);
-                            if (R::usable(raw)) key = PK::make(raw, k);
-                        }
-                    }
-                    pos_key[p] = key;
-                }
-                __syncthreads();
-                for (int32_t i = tid; i < ts; i += BT) {
-                    keys[i] = -1;
-                    cnts[i] = 0;
-                    first[i] = 0xffffffffu;
-                }
-                __syncthreads();
-            }
         }
         // ordered pass over the keyed positions, one contiguous range per warp
         const int32_t span = ((d + NW - 1) / NW + 31) & ~31;
