@@ -17,7 +17,7 @@ struct DevCounters {
     int32_t all_found;            // merge: every community matched
     int32_t n_amb_large;          // of those, vertices of degree > 256 (queued from the list's end)
     int32_t check_where;          // bits of failed internal consistency checks (ERR_CHECK)
-    int32_t pad;
+    int32_t hub_next;             // next hub of the sweep's hub queue (blocks take hubs in list order)
 };
 
 enum : int32_t {

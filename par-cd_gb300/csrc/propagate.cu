@@ -1047,17 +1047,17 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
 }
 
 // ---------------------------------------------------------------------------
-// Hubs: one 1024-thread block per vertex (one per SM), tables in shared memory.  A hub's
-// labels are split by hash into P parts of at most part_labels distinct
-// labels; each part is histogrammed in the shared table, its first
-// occurrences are keyed, and the table is cleared, before the next part.
-// Position-indexed arrays in a per-block global slice carry the row between
-// parts: pos_lab[p] (the label at position p, gathered once) and pos_key[p]
-// (the packed key of p if it is a candidate, the identity otherwise; every
-// position is written by the part its label belongs to).  The ordered pass
-// of the one-pass kernel then runs over pos_key: range maxima, carry-ins,
-// ties and the final level.  All global traffic is coalesced and the slices
-// are small enough to stay in L2.
+// Hubs: 1024-thread blocks (one per SM) that take hubs from a queue in list
+// order (largest first), so one very large hub does not leave the others to a
+// fixed share of the blocks.  A hub's labels are split by hash into P parts of
+// at most part_labels distinct labels; each part is histogrammed in the shared
+// table (label, count, first position), then the table is walked once in slot
+// order: each label's packed key is written at its first position and the
+// slot is cleared in the same walk.  Position-indexed arrays in a per-block
+// global slice carry the row between parts: pos_lab[p] (the label at position
+// p, gathered once) and pos_key[p] (the identity, then the packed key at each
+// candidate's first position).  The ordered pass of the one-pass kernel then
+// runs over pos_key: range maxima, carry-ins, ties and the final level.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t hub_part(uint32_t hv, int32_t parts) {
     return (uint32_t)(((unsigned long long)hv * (uint32_t)parts) >> 32);
@@ -1079,6 +1079,7 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
     __shared__ uint32_t s_t[NW];
     __shared__ int32_t s_nfin[NW];
     __shared__ int32_t s_amb, s_curr_freq;
+    __shared__ int32_t s_vi[2];  // by iteration parity: a slot is rewritten only after every thread read it
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     K *pos_key = reinterpret_cast<K *>(gscratch + (int64_t)blockIdx.x * gstride);
     int32_t *pos_lab = reinterpret_cast<int32_t *>(pos_key + pos_cap);
@@ -1090,7 +1091,11 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
         first[i] = 0xffffffffu;
     }
     __syncthreads();
-    for (int64_t vi = blockIdx.x; vi < count; vi += gridDim.x) {
+    for (int it = 0;; ++it) {
+        if (tid == 0) s_vi[it & 1] = atomicAdd(&a.ctr->hub_next, 1);
+        __syncthreads();
+        const int64_t vi = s_vi[it & 1];
+        if (vi >= count) break;
         const int32_t v = list[vi];
         const int32_t b = a.g.indices[v], d = a.g.indices[v + 1] - b;
         const int32_t curr = a.labels[v];
@@ -1125,6 +1130,7 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                 if (p < d) {
                     l[u] = a.labels[l[u]];
                     pos_lab[p] = l[u];
+                    pos_key[p] = PK::ident();
                     pt = (int32_t)hub_part(hash_label(l[u]), parts);
                 }
                 const unsigned peers = __match_any_sync(FULL, pt);
@@ -1194,34 +1200,23 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                 }
             }
             __syncthreads();
-            // keys of this part's positions
-            for (int32_t j = i0 + tid; j < i1; j += BT) {
-                const int2 e = bucket[j];
-                const int32_t p = e.x, l = e.y;
-                uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
-                int32_t probes = 0;
-                while (probes < ts && keys[h] != l) {
-                    h = (h + 1) & (uint32_t)(ts - 1);
-                    ++probes;
-                }
-                K key = PK::ident();
-                if (probes < ts && first[h] == (uint32_t)p) {
-                    const int32_t k = cnts[h];
+            // slot walk: each label's key at its first position; the slot is cleared
+            for (int32_t i = tid; i < ts; i += BT) {
+                const int32_t l = keys[i];
+                if (l != -1) {
+                    const int32_t k = cnts[i];
+                    const uint32_t p = first[i];
                     if (l == curr) {
                         s_curr_freq = k;
                     } else {
                         Tag tag{0, 0};
                         const typename R::Key raw = vr.join(v, d, l, k, a.cm, tag);
-                        if (R::usable(raw)) key = PK::make(raw, k);
+                        if (R::usable(raw)) pos_key[p] = PK::make(raw, k);
                     }
+                    keys[i] = -1;
+                    cnts[i] = 0;
+                    first[i] = 0xffffffffu;
                 }
-                pos_key[p] = key;
-            }
-            __syncthreads();
-            for (int32_t i = tid; i < ts; i += BT) {
-                keys[i] = -1;
-                cnts[i] = 0;
-                first[i] = 0xffffffffu;
             }
             __syncthreads();
         }
@@ -1806,6 +1801,7 @@ __global__ void k_reset_sweep(DevCounters *ctr) {
     ctr->check_where = 0;
     ctr->error = 0;
     ctr->total_draws = 0;
+    ctr->hub_next = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1902,7 +1898,7 @@ static int launch_bins_rule(pcd_graph *g, const SweepArgs &a, const R &rule, cud
         } else if (dm <= 4096) {
             launch_block1<R, 512, 8>(g, a, rule, lst, c, dm, st);
         } else {
-            launch_block1<R, 512, 16>(g, a, rule, lst, c, dm, st);
+            launch_block1<R, 1024, 8>(g, a, rule, lst, c, dm, st);
         }
         ++launches;
         prof_mark(g->ctx, sr.bin == BIN_WARP ? "sweep.warp" : (sr.bin == BIN_BLOCK ? "sweep.block" : "sweep.block_l"),
