@@ -885,19 +885,18 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
             s_amb = 0;
             s_curr_freq = 0;
         }
-        // H: histogram, HU gathers in flight per thread (one round for RPL <= 8)
-        constexpr int HU = RPL < 8 ? RPL : 8;
-        for (int32_t p0 = 0; p0 < d; p0 += BT * HU) {
-            int32_t lab[HU];
+        // H: histogram, four gathers in flight per thread
+        for (int32_t p0 = 0; p0 < d; p0 += BT * 4) {
+            int32_t lab[4];
 #pragma unroll
-            for (int u = 0; u < HU; ++u) {
+            for (int u = 0; u < 4; ++u) {
                 const int32_t p = p0 + u * BT + tid;
                 lab[u] = p < d ? a.g.adj[b + p] : -1;
             }
 #pragma unroll
-            for (int u = 0; u < HU; ++u) lab[u] = lab[u] >= 0 ? a.labels[lab[u]] : -2;
+            for (int u = 0; u < 4; ++u) lab[u] = lab[u] >= 0 ? a.labels[lab[u]] : -2;
 #pragma unroll
-            for (int u = 0; u < HU; ++u) {
+            for (int u = 0; u < 4; ++u) {
                 const int32_t p = p0 + u * BT + tid;
                 const int32_t l = lab[u];
                 const unsigned peers = __match_any_sync(FULL, l);
@@ -1070,7 +1069,7 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                                                          int32_t *gscratch, int64_t gstride, int32_t pos_cap) {
     using PK = PackedKey<R>;
     using K = typename PK::K;
-    constexpr int BT = 1024, NW = 32, HU = 4;
+    constexpr int BT = 1024, NW = 32;
     extern __shared__ int32_t smem[];
     int32_t *keys = smem;
     int32_t *cnts = smem + table_cap;
@@ -1158,25 +1157,14 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
         __syncthreads();
         for (int32_t i = tid; i < parts; i += BT) s_cur[i] = s_start[i];
         __syncthreads();
-        // positions into their part's bucket; every loop below loads HU
-        // entries per thread before it uses them, so that many L2 reads are in flight
-        for (int32_t p0 = 0; p0 < d; p0 += BT * HU) {
-            int32_t l[HU];
-#pragma unroll
-            for (int u = 0; u < HU; ++u) {
-                const int32_t p = p0 + u * BT + tid;
-                l[u] = p < d ? pos_lab[p] : 0;
-            }
-#pragma unroll
-            for (int u = 0; u < HU; ++u) {
-                const int32_t p = p0 + u * BT + tid;
-                const int32_t pt = p < d ? (int32_t)hub_part(hash_label(l[u]), parts) : -1 - lane;
-                const unsigned peers = __match_any_sync(FULL, pt);
-                int32_t base = 0;
-                if (p < d && lane == __ffs(peers) - 1) base = atomicAdd(&s_cur[pt], __popc(peers));
-                base = __shfl_sync(FULL, base, __ffs(peers) - 1);
-                if (p < d) bucket[base + __popc(peers & lanemask_lt())] = make_int2(p, l[u]);
-            }
+        for (int32_t p0 = 0; p0 < d; p0 += BT) {  // positions into their part's bucket
+            const int32_t p = p0 + tid;
+            const int32_t pt = p < d ? (int32_t)hub_part(hash_label(pos_lab[p]), parts) : -1 - lane;
+            const unsigned peers = __match_any_sync(FULL, pt);
+            int32_t base = 0;
+            if (p < d && lane == __ffs(peers) - 1) base = atomicAdd(&s_cur[pt], __popc(peers));
+            base = __shfl_sync(FULL, base, __ffs(peers) - 1);
+            if (p < d) bucket[base + __popc(peers & lanemask_lt())] = make_int2(p, pos_lab[p]);
         }
         __syncthreads();
         for (int32_t part = 0; part < parts; ++part) {
@@ -1184,37 +1172,30 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
             int32_t ts = 64;
             while (ts < 2 * (i1 - i0) && ts < table_cap) ts <<= 1;
             // histogram of this part's labels
-            for (int32_t j0 = i0; j0 < i1; j0 += BT * HU) {
-                int2 ev[HU];
-#pragma unroll
-                for (int u = 0; u < HU; ++u) {
-                    const int32_t j = j0 + u * BT + tid;
-                    ev[u] = j < i1 ? bucket[j] : make_int2(-1, -2);
-                }
-#pragma unroll
-                for (int u = 0; u < HU; ++u) {
-                    const int32_t p = ev[u].x, l = ev[u].y;
-                    const unsigned peers = __match_any_sync(FULL, p >= 0 ? l : -3 - lane);
-                    // bucket order is not position order: the group's first position is its minimum
-                    const uint32_t pmin = __reduce_min_sync(peers, (uint32_t)p);
-                    if (p >= 0 && lane == __ffs(peers) - 1) {
-                        uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
-                        int32_t probes = 0;
-                        for (; probes < ts; ++probes) {
-                            const int32_t kk = keys[h];
-                            if (kk == l) break;
-                            if (kk == -1) {
-                                const int32_t old = atomicCAS(&keys[h], -1, l);
-                                if (old == -1 || old == l) break;
-                            }
-                            h = (h + 1) & (uint32_t)(ts - 1);
+            for (int32_t j0 = i0; j0 < i1; j0 += BT) {
+                const int32_t j = j0 + tid;
+                const int2 e = j < i1 ? bucket[j] : make_int2(-1, -2);
+                const int32_t p = e.x, l = e.y;
+                const unsigned peers = __match_any_sync(FULL, p >= 0 ? l : -3 - lane);
+                // bucket order is not position order: the group's first position is its minimum
+                const uint32_t pmin = __reduce_min_sync(peers, (uint32_t)p);
+                if (p >= 0 && lane == __ffs(peers) - 1) {
+                    uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
+                    int32_t probes = 0;
+                    for (; probes < ts; ++probes) {
+                        const int32_t kk = keys[h];
+                        if (kk == l) break;
+                        if (kk == -1) {
+                            const int32_t old = atomicCAS(&keys[h], -1, l);
+                            if (old == -1 || old == l) break;
                         }
-                        if (probes < ts) {
-                            atomicAdd(&cnts[h], __popc(peers));
-                            atomicMin(&first[h], pmin);
-                        } else {
-                            atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);  // a part overfilled the table
-                        }
+                        h = (h + 1) & (uint32_t)(ts - 1);
+                    }
+                    if (probes < ts) {
+                        atomicAdd(&cnts[h], __popc(peers));
+                        atomicMin(&first[h], pmin);
+                    } else {
+                        atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);  // a part overfilled the table
                     }
                 }
             }
@@ -1243,13 +1224,7 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
         const int32_t span = ((d + NW - 1) / NW + 31) & ~31;
         const int32_t lo = min(d, wid * span), hi = min(d, lo + span);
         K wmax = PK::ident();
-        for (int32_t p0 = lo + lane; p0 < hi; p0 += 32 * HU) {
-            K x[HU];
-#pragma unroll
-            for (int u = 0; u < HU; ++u) x[u] = p0 + 32 * u < hi ? pos_key[p0 + 32 * u] : PK::ident();
-#pragma unroll
-            for (int u = 0; u < HU; ++u) wmax = kmax(wmax, x[u]);
-        }
+        for (int32_t p = lo + lane; p < hi; p += 32) wmax = kmax(wmax, pos_key[p]);
 #pragma unroll
         for (int o = 16; o; o >>= 1) wmax = kmax(wmax, __shfl_xor_sync(FULL, wmax, o));
         if (lane == 0) s_agg[wid] = wmax;
@@ -1264,42 +1239,31 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
         uint32_t t = 0;
         int32_t nfin = 0;
         bool amb = false;
-        // entries already read are overwritten: a group's HU chunks are all
-        // loaded before any of its final-level labels is written
-        int32_t *fin_list = pos_lab + lo;
-        for (int32_t g0 = lo; g0 < hi; g0 += 32 * HU) {
-            K kv[HU];
-            int32_t lv[HU];
-#pragma unroll
-            for (int u = 0; u < HU; ++u) {
-                const int32_t p = g0 + 32 * u + lane;
-                kv[u] = p < hi ? pos_key[p] : PK::ident();
-                lv[u] = p < hi ? pos_lab[p] : -1;
-            }
+        int32_t *fin_list = pos_lab + lo;  // entries already read are overwritten
+        for (int32_t base = lo; base < hi; base += 32) {
+            const int32_t p = base + lane;
+            const K key = p < hi ? pos_key[p] : PK::ident();
+            const bool cand = key != PK::ident();
+            const int32_t l = cand ? pos_lab[p] : -1;
             __syncwarp();
+            const bool fin = cand && PK::level(key) == lfin;
+            const unsigned fm = __ballot_sync(FULL, fin);
+            if (fin) fin_list[nfin + __popc(fm & lanemask_lt())] = l;
+            nfin += __popc(fm);
+            if (!__any_sync(FULL, cand && PK::level(key) >= PK::level(carry))) continue;
+            K inc = key;
 #pragma unroll
-            for (int u = 0; u < HU; ++u) {
-                const K key = kv[u];
-                const bool cand = key != PK::ident();
-                const bool fin = cand && PK::level(key) == lfin;
-                const unsigned fm = __ballot_sync(FULL, fin);
-                if (fin) fin_list[nfin + __popc(fm & lanemask_lt())] = lv[u];
-                nfin += __popc(fm);
-                if (!__any_sync(FULL, cand && PK::level(key) >= PK::level(carry))) continue;
-                K inc = key;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const K y = __shfl_up_sync(FULL, inc, o);
-                    if (lane >= o) inc = kmax(inc, y);
-                }
-                K ex = __shfl_up_sync(FULL, inc, 1);
-                if (lane == 0) ex = PK::ident();
-                const K pre = kmax(carry, ex);
-                const bool tie = cand && PK::level(key) == PK::level(pre);
-                if (tie && PK::tie_ambiguous(key, pre)) amb = true;
-                t += __popc(__ballot_sync(FULL, tie));
-                carry = kmax(carry, __shfl_sync(FULL, inc, 31));
+            for (int o = 1; o < 32; o <<= 1) {
+                const K y = __shfl_up_sync(FULL, inc, o);
+                if (lane >= o) inc = kmax(inc, y);
             }
+            K ex = __shfl_up_sync(FULL, inc, 1);
+            if (lane == 0) ex = PK::ident();
+            const K pre = kmax(carry, ex);
+            const bool tie = cand && PK::level(key) == PK::level(pre);
+            if (tie && PK::tie_ambiguous(key, pre)) amb = true;
+            t += __popc(__ballot_sync(FULL, tie));
+            carry = kmax(carry, __shfl_sync(FULL, inc, 31));
         }
         amb = __any_sync(FULL, amb);
         if (lane == 0) {
