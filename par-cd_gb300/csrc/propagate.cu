@@ -326,21 +326,29 @@ __global__ void __launch_bounds__(256) k_prop_thread(SweepArgs a, R rule, const 
     }
 }
 
+// Shared memory of one warp of k_prop_warp: the label table (int32, 2 WCAP
+// slots; the scoring pass reuses it for the tie list), first-occurrence
+// labels (int32), counts (uint16, <= WCAP) and slot ordinals (uint8, < WCAP).
+template <int WCAP>
+constexpr size_t warp_bytes() {
+    static_assert(WCAP <= 256, "ordinals are stored in 8 bits");
+    return 8 * WCAP + 4 * WCAP + 2 * WCAP + 2 * WCAP;
+}
+
 template <class R, int WCAP>
 __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const int32_t *__restrict__ list,
                                                    int64_t count, const int32_t *count_dev) {
     constexpr int TS = 2 * WCAP;
-    constexpr int PER_WARP = 2 * TS + 4 * WCAP;
     extern __shared__ int32_t smem[];
     using Key = typename R::Key;
     using E = Elem<Key>;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int32_t *keys = smem + wid * PER_WARP;
-    int32_t *ords = keys + TS;
-    int32_t *clab = ords + TS;
-    int32_t *ccnt = clab + WCAP;
-    int32_t *cvol = ccnt + WCAP;
-    int32_t *ties = cvol + WCAP;
+    unsigned char *wbase = reinterpret_cast<unsigned char *>(smem) + wid * warp_bytes<WCAP>();
+    int32_t *keys = reinterpret_cast<int32_t *>(wbase);
+    int32_t *ties = keys;  // the table is dead once the histogram is done
+    int32_t *clab = keys + TS;
+    uint16_t *ccnt = reinterpret_cast<uint16_t *>(clab + WCAP);
+    uint8_t *ords = reinterpret_cast<uint8_t *>(ccnt + WCAP);
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     if (count_dev) count = *count_dev;
@@ -385,12 +393,12 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
             const unsigned newmask = __ballot_sync(FULL, isnew);
             if (isnew) {
                 int32_t ord = nc + __popc(newmask & lanemask_lt());
-                ords[h] = ord;
+                ords[h] = (uint8_t)ord;
                 clab[ord] = l;
-                ccnt[ord] = __popc(peers);
+                ccnt[ord] = (uint16_t)__popc(peers);
             }
             __syncwarp();
-            if (leader && !isnew) ccnt[ords[h]] += __popc(peers);
+            if (leader && !isnew) ccnt[ords[h]] += (uint16_t)__popc(peers);
             nc += __popc(newmask);
             __syncwarp();
         }
@@ -1832,7 +1840,7 @@ static void launch_group(pcd_graph *g, const SweepArgs &a, const R &rule, int bi
 template <class R, int WCAP>
 static void launch_warp(pcd_graph *g, const SweepArgs &a, const R &rule, const int32_t *list, int64_t c,
                         cudaStream_t st) {
-    const size_t smem = 8ull * (2 * 2 * WCAP + 4 * WCAP) * sizeof(int32_t);
+    const size_t smem = 8 * warp_bytes<WCAP>();
     cudaFuncSetAttribute(k_prop_warp<R, WCAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_prop_warp<R, WCAP>, 256, smem);
@@ -1951,7 +1959,7 @@ int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32
         RuleModF64 rf;
         rf.m = g->m;
         rf.bv = bv;
-        const size_t smem = 8ull * (2 * 2 * WARP_CAP + 4 * WARP_CAP) * sizeof(int32_t);
+        const size_t smem = 8 * warp_bytes<WARP_CAP>();
         cudaFuncSetAttribute(k_prop_warp<RuleModF64, WARP_CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
         k_prop_warp<RuleModF64, WARP_CAP><<<g->ctx->num_sms * 8, 256, smem, st>>>(a, rf, g->amb, 0,
