@@ -332,6 +332,34 @@ pcd_status pcd_singleton_partition(pcd_rand *s, int32_t n, int32_t *labels);
 pcd_status pcd_clustering_partition(int32_t n, const int32_t *indices, const int32_t *adj,
                                     const int32_t *tri, int32_t *labels);
 
+/* create_clustering_partition (src/framework.cpp:27-59) on the device: the
+ * graph's labels become the same partition as pcd_clustering_partition
+ * (vertices by decreasing tri / (deg (deg - 1)), the product in 32-bit int,
+ * then decreasing degree, then id; each unlabelled vertex opens a community
+ * and claims its unlabelled neighbours).  Computes the triangles if they are
+ * not yet known.  Labels are 0..k-1 in the order the communities open;
+ * *num_labels (may be NULL) receives k.  Synchronises. */
+pcd_status pcd_clustering_partition_device(pcd_graph *g, int32_t *num_labels);
+
+/* FindConnectedRefinement::refine (src/refinement.cpp:291-322): the graph's
+ * labels become, for every vertex, the smallest vertex id in its connected
+ * component (the fixed point the reference's min-label rounds reach); the
+ * current labels are not read.  Asynchronous unless num_components is
+ * non-NULL, which receives the number of components and synchronises. */
+pcd_status pcd_find_connected(pcd_graph *g, int32_t *num_components);
+
+/* norm_mutual_info (src/common.cpp:75-125) of the confusion counts of count
+ * label pairs (a[i], b[i]), normalised by n vertices: compare_communities(g,
+ * a, b) (src/common.cpp:163-173) is count = n = g.n; the ground-truth file
+ * form (src/common.cpp:127-160) passes one (community line, label) pair per
+ * listed vertex and n = g.n.  Labels must be >= 0.  FP64; the sums run in a
+ * fixed order that differs from the reference's map walk, so the value
+ * agrees to rounding.  pcd_nmi_device takes device arrays, pcd_nmi host
+ * arrays.  Synchronise. */
+pcd_status pcd_nmi_device(pcd_ctx *ctx, int64_t count, const int32_t *a, const int32_t *b, int32_t n,
+                          double *nmi);
+pcd_status pcd_nmi(pcd_ctx *ctx, int64_t count, const int32_t *a, const int32_t *b, int32_t n, double *nmi);
+
 #ifdef __cplusplus
 }
 #endif

@@ -153,6 +153,19 @@ class Port:
         self.lib.pcdo_clustering_partition(C.byref(self._g), lab.ctypes.data_as(C.c_void_p))
         return lab
 
+    def find_connected(self) -> np.ndarray:
+        lab = np.zeros(self.n, np.int32)
+        self.lib.pcdo_find_connected(C.byref(self._g), lab.ctypes.data_as(C.c_void_p))
+        return lab
+
+    def nmi(self, a: np.ndarray, b: np.ndarray, n: int | None = None) -> float:
+        a = np.ascontiguousarray(a, dtype=np.int32)
+        b = np.ascontiguousarray(b, dtype=np.int32)
+        f = self.lib.pcdo_norm_mutual_info
+        f.restype = C.c_double
+        return float(f(C.c_int64(a.shape[0]), a.ctypes.data_as(C.c_void_p), b.ctypes.data_as(C.c_void_p),
+                       C.c_int32(self.n if n is None else n)))
+
     def compress(self, labels: np.ndarray):
         lab = np.ascontiguousarray(labels, dtype=np.int32).copy()
         k = self.lib.pcdo_compress_labels(C.c_int32(lab.shape[0]), lab.ctypes.data_as(C.c_void_p))
@@ -304,6 +317,26 @@ class Reference:
         lab = np.zeros(self.n, np.int32)
         self.lib.ref_clustering(C.c_void_p(self.h), lab.ctypes.data_as(C.c_void_p))
         return lab
+
+    def find_connected(self, threads=1):
+        lab = np.zeros(self.n, np.int32)
+        start = np.arange(self.n, dtype=np.int32)  # the refinement ignores the partition
+        self.lib.ref_find_connected(C.c_void_p(self.h), start.ctypes.data_as(C.c_void_p), C.c_int(threads),
+                                    lab.ctypes.data_as(C.c_void_p))
+        return lab
+
+    def nmi_file(self, labels, path):
+        lab = np.ascontiguousarray(labels, dtype=np.int32).copy()
+        f = self.lib.ref_compare_file
+        f.restype = C.c_double
+        return float(f(C.c_void_p(self.h), lab.ctypes.data_as(C.c_void_p), str(path).encode()))
+
+    def nmi(self, a, b):
+        a = np.ascontiguousarray(a, dtype=np.int32).copy()
+        b = np.ascontiguousarray(b, dtype=np.int32).copy()
+        f = self.lib.ref_compare
+        f.restype = C.c_double
+        return float(f(C.c_void_p(self.h), a.ctypes.data_as(C.c_void_p), b.ctypes.data_as(C.c_void_p)))
 
     def compress(self, labels):
         lab = np.ascontiguousarray(labels, dtype=np.int32).copy()

@@ -213,6 +213,80 @@ void pcdo_clustering_partition(const pcdo_graph *g, int32_t *labels) {
     free(pairs);
 }
 
+/* refinement.cpp:291-322: tags start as vertex ids; each round every vertex
+ * takes the minimum of its own and its neighbours' tags (read from the
+ * previous round) until no tag changes. */
+void pcdo_find_connected(const pcdo_graph *g, int32_t *labels) {
+    int32_t n = g->n;
+    int32_t *tags = (int32_t *)malloc(sizeof(int32_t) * (n ? n : 1));
+    int32_t *next = (int32_t *)malloc(sizeof(int32_t) * (n ? n : 1));
+    for (int32_t i = 0; i < n; i++) tags[i] = i;
+    int done = 0;
+    while (!done) {
+        done = 1;
+        for (int32_t v = 0; v < n; v++) {
+            int32_t t = tags[v];
+            for (int32_t e = g->indices[v]; e < g->indices[v + 1]; e++)
+                if (tags[g->adj[e]] < t) t = tags[g->adj[e]];
+            next[v] = t;
+            if (tags[v] != t) done = 0;
+        }
+        int32_t *tmp = tags;
+        tags = next;
+        next = tmp;
+    }
+    memcpy(labels, tags, sizeof(int32_t) * (size_t)n);
+    free(tags);
+    free(next);
+}
+
+typedef struct {
+    int32_t i, j;
+} nmi_pair;
+
+static int nmi_pair_cmp(const void *a, const void *b) {
+    const nmi_pair *x = (const nmi_pair *)a, *y = (const nmi_pair *)b;
+    if (x->i != y->i) return x->i < y->i ? -1 : 1;
+    return x->j < y->j ? -1 : (x->j > y->j);
+}
+
+/* common.cpp:75-125 with the map of common.cpp:163-173: the distinct pairs
+ * in (i, j) order with their counts; sums in that order, i then j for den. */
+double pcdo_norm_mutual_info(int64_t count, const int32_t *a, const int32_t *b, int32_t n) {
+    nmi_pair *pr = (nmi_pair *)malloc(sizeof(nmi_pair) * (size_t)(count ? count : 1));
+    int32_t ca = 0, cb = 0;
+    for (int64_t k = 0; k < count; k++) {
+        pr[k].i = a[k];
+        pr[k].j = b[k];
+        if (a[k] + 1 > ca) ca = a[k] + 1;
+        if (b[k] + 1 > cb) cb = b[k] + 1;
+    }
+    qsort(pr, (size_t)count, sizeof(nmi_pair), nmi_pair_cmp);
+    int32_t *ni = (int32_t *)calloc((size_t)(ca ? ca : 1), sizeof(int32_t));
+    int32_t *nj = (int32_t *)calloc((size_t)(cb ? cb : 1), sizeof(int32_t));
+    for (int64_t k = 0; k < count; k++) {
+        ni[pr[k].i] += 1;
+        nj[pr[k].j] += 1;
+    }
+    double nom = 0.0, den = 0.0;
+    for (int64_t k = 0; k < count;) {
+        int64_t e = k + 1;
+        while (e < count && pr[e].i == pr[k].i && pr[e].j == pr[k].j) e++;
+        int32_t val = (int32_t)(e - k);
+        int32_t i = pr[k].i, j = pr[k].j;
+        nom += val * log(((double)val * n) / imul_wrap(ni[i], nj[j]));
+        k = e;
+    }
+    for (int32_t i = 0; i < ca; i++)
+        if (ni[i] != 0) den += ni[i] * log(ni[i] / ((double)n));
+    for (int32_t j = 0; j < cb; j++)
+        if (nj[j] != 0) den += nj[j] * log(nj[j] / ((double)n));
+    free(pr);
+    free(ni);
+    free(nj);
+    return -2 * nom / den;
+}
+
 /* framework.cpp:146-170: first-occurrence renumbering; every NEW_LABEL
  * vertex gets a fresh id. */
 int32_t pcdo_compress_labels(int32_t n, int32_t *labels) {

@@ -54,6 +54,11 @@ int32_t pcdo_rand_r(uint32_t *seed);
 /* framework.cpp */
 void pcdo_singleton_partition(const pcdo_graph *g, pcdo_rand_state *rs, int32_t *labels);
 void pcdo_clustering_partition(const pcdo_graph *g, int32_t *labels);
+/* FindConnectedRefinement::refine (refinement.cpp:291-322) */
+void pcdo_find_connected(const pcdo_graph *g, int32_t *labels);
+/* norm_mutual_info over the (a[i], b[i]) confusion map (common.cpp:75-125,
+ * 163-173); n is g.n.  Labels >= 0. */
+double pcdo_norm_mutual_info(int64_t count, const int32_t *a, const int32_t *b, int32_t n);
 int32_t pcdo_compress_labels(int32_t n, int32_t *labels);
 int32_t pcdo_collect_statistics(const pcdo_graph *g, const int32_t *labels, int32_t *sizes,
                                 int32_t *int_volume, int32_t *ext_volume);

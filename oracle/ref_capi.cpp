@@ -14,11 +14,15 @@
 //   ref_count_triangles -> Graph::count_triangles     src/graph.cpp:107-175
 //   ref_singleton / ref_clustering -> framework.cpp:14-24 / 27-59
 //   ref_gain_*          -> Rule::score_join/leave/merge (rules.cpp)
+//   ref_find_connected  -> FindConnectedRefinement    src/refinement.cpp:291-322
+//   ref_compare         -> compare_communities(g,a,b) src/common.cpp:75-125,163-173
+//   ref_compare_file    -> compare_communities(g,l,f) src/common.cpp:127-160
 // glibc rand() is the process-global stream the reference draws its seeds
 // from; ref_srand / ref_rand expose it.
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 
 #include "graph.hpp"
 #include "common.hpp"
@@ -138,6 +142,24 @@ void ref_refine_merge(void *h, int rule, double lambda, const int *labels, int r
     mr.refine(*g, *p, *r, new_labels);
     delete p;
     delete r;
+}
+
+void ref_find_connected(void *h, const int *labels, int threads, int *new_labels) {
+    const Graph *g = ((RefGraph *)h)->g;
+    Rule *r = make_rule(0, 0.0);
+    Partition *p = make_partition(g, labels, threads);
+    FindConnectedRefinement fc(threads);
+    fc.refine(*g, *p, *r, new_labels);
+    delete p;
+    delete r;
+}
+
+double ref_compare(void *h, int *a, int *b) {
+    return compare_communities(*((RefGraph *)h)->g, a, b);
+}
+
+double ref_compare_file(void *h, int *labels, const char *path) {
+    return compare_communities(*((RefGraph *)h)->g, labels, std::string(path));
 }
 
 // Single gain evaluations on a partition (for rule-level unit checks).

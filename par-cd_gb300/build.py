@@ -22,7 +22,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpcd.so")
 MAIN = os.path.join(HERE, "main-cuda")
 CONVERT = os.path.join(HERE, "convert-cuda")
-SOURCES = ["api.cu", "partition.cu", "propagate.cu", "merge.cu", "triangles.cu", "batch.cu", "noalloc.cu", "convert.cu", "hostside.cpp", "serve.cpp"]
+SOURCES = ["api.cu", "partition.cu", "propagate.cu", "merge.cu", "triangles.cu", "batch.cu", "noalloc.cu", "convert.cu", "components.cu", "initial.cu", "nmi.cu", "hostside.cpp", "serve.cpp"]
 HEADERS = ["pcd_device.cuh", "pcd_scan.cuh", "pcd_internal.h", "pcd_types.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -126,6 +126,10 @@ def _load() -> C.CDLL:
         "pcd_rand_skip": ([C.POINTER(_Rand), i64], None),
         "pcd_singleton_partition": ([C.POINTER(_Rand), i32, vp], i32),
         "pcd_clustering_partition": ([i32, vp, vp, vp, vp], i32),
+        "pcd_clustering_partition_device": ([vp, C.POINTER(i32)], i32),
+        "pcd_find_connected": ([vp, C.POINTER(i32)], i32),
+        "pcd_nmi_device": ([vp, i64, vp, vp, i32, C.POINTER(dbl)], i32),
+        "pcd_nmi": ([vp, i64, vp, vp, i32, C.POINTER(dbl)], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -393,6 +397,19 @@ class MergingRefinement:
         g.ctx._check(LIB.pcd_merge(g.h, C.byref(rule._c()), self.rounds, C.c_uint32(seed & 0xFFFFFFFF)))
 
 
+class FindConnectedRefinement:
+    """FindConnectedRefinement (src/refinement.cpp:291-322): every vertex's
+    label becomes the smallest vertex id of its connected component."""
+
+    def __init__(self, num_threads: int = 1):
+        self.num_threads = num_threads  # the reference's OpenMP width; unused here
+
+    def refine(self, g: Graph, rule: Rule | None = None, seed: int = 0) -> int:
+        k = C.c_int32()
+        g.ctx._check(LIB.pcd_find_connected(g.h, C.byref(k)))
+        return int(k.value)
+
+
 class GlibcRand:
     """The reference's rand() stream (glibc, default seed 1)."""
 
@@ -420,6 +437,61 @@ def create_clustering_partition(g: Graph) -> np.ndarray:
     lab = np.zeros(g.n, np.int32)
     g.ctx._check(LIB.pcd_clustering_partition(g.n, _ptr(g._indices), _ptr(g._adj), _ptr(tri), _ptr(lab)))
     return lab
+
+
+def create_clustering_partition_device(g: Graph) -> int:
+    """create_clustering_partition (src/framework.cpp:27-59) computed on the
+    device into the graph's labels; returns the number of communities."""
+    k = C.c_int32()
+    g.ctx._check(LIB.pcd_clustering_partition_device(g.h, C.byref(k)))
+    return int(k.value)
+
+
+def nmi(ctx: Context, a, b, n: int | None = None) -> float:
+    """norm_mutual_info (src/common.cpp:75-125) of the label pairs (a[i],
+    b[i]), normalised by n (default len(a)).  a and b: host arrays, or CUDA
+    tensors / objects with data_ptr() (device arrays, not copied)."""
+    out = C.c_double()
+    if hasattr(a, "data_ptr"):
+        count = int(a.numel())
+        ctx._check(LIB.pcd_nmi_device(ctx.h, count, C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()),
+                                      count if n is None else n, C.byref(out)))
+    else:
+        x, y = _i32(a), _i32(b)
+        if x.shape != y.shape:
+            raise ValueError("labelings differ in length")
+        count = int(x.shape[0])
+        ctx._check(LIB.pcd_nmi(ctx.h, count, _ptr(x), _ptr(y), count if n is None else n, C.byref(out)))
+    return float(out.value)
+
+
+def compare_communities(g: Graph, a, b) -> float:
+    """compare_communities(g, a, b) (src/common.cpp:163-173)."""
+    return nmi(g.ctx, a, b, g.n)
+
+
+def compare_communities_file(g: Graph, labels, path: str) -> float:
+    """compare_communities(g, labels, filename) (src/common.cpp:127-160): one
+    ground-truth community per line (vertex ids separated by white space);
+    empty lines and lines starting with '#' are skipped, and a line is read
+    up to its first token that is not an integer.  Vertex ids index
+    labels."""
+    lab = _i32(labels)
+    comm, va, vb = 0, [], []
+    with open(path) as f:
+        for line in f:
+            line = line.rstrip("\n")
+            if not line or line[0] == "#":
+                continue
+            comm += 1
+            for tok in line.split():
+                try:
+                    v = int(tok)
+                except ValueError:
+                    break
+                va.append(comm)
+                vb.append(int(lab[v]))
+    return nmi(g.ctx, np.asarray(va, np.int32), np.asarray(vb, np.int32), g.n)
 
 
 @dataclass

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
-for p in (os.path.join(ROOT, "par-cd_gb300"), os.path.join(ROOT, "oracle")):
+for p in (os.path.join(ROOT, "par-cd_gb300"), os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests", "golden")):
     if p not in sys.path:
         sys.path.insert(0, p)
 
@@ -41,6 +41,14 @@ def golden():
         return json.load(f)
 
 
+@pytest.fixture(scope="session")
+def golden_extras():
+    import json
+
+    with open(os.path.join(ROOT, "tests", "golden", "golden_extras.json")) as f:
+        return json.load(f)
+
+
 _GRAPHS = {}
 
 
@@ -51,7 +59,12 @@ def golden_graph(name):
         import graphs
         import make_golden
 
-        _GRAPHS[name] = make_golden.make_graph(name)[1]
+        if name == "forest":
+            import make_golden_extras
+
+            _GRAPHS[name] = graphs.convert_edges(make_golden_extras.forest_edges())
+        else:
+            _GRAPHS[name] = make_golden.make_graph(name)[1]
     return _GRAPHS[name]
 
 

@@ -168,3 +168,33 @@ def test_reference_shipped_flags_match_strict_except_cpm(golden):
         if case["metric"].startswith("cpm"):
             continue  # contraction-dependent: fast-math may fuse k - lambda * size
         assert same, (case["graph"], case["metric"], case["strategy"])
+
+
+def test_oracle_extras_golden(port, golden_extras):
+    """Initial partition, connected components and NMI of the restatement
+    against the reference's outputs in tests/golden/golden_extras.json."""
+    import graphs
+    import make_golden_extras as mge
+
+    for name, rec in golden_extras["graphs"].items():
+        g = golden_graph(name)
+        if name == "forest":
+            assert hashlib.sha256(graphs.to_bytes(g)).hexdigest() == golden_extras["forest_pcd_sha256"]
+        port.load(g.indices, g.adj)
+        port.count_triangles()
+        clus = port.clustering()
+        comp = port.find_connected()
+        assert sha(clus) == rec["clustering_sha256"], name
+        assert sha(comp) == rec["components_sha256"], name
+        assert np.unique(comp).shape[0] == rec["components"]
+        s1, s2 = mge.synth_labels(g.n)
+        # the restatement walks the confusion map in the reference's order: bit-identical
+        assert repr(port.nmi(clus, comp)) == rec["nmi_clustering_components"]
+        assert repr(port.nmi(clus, s1)) == rec["nmi_clustering_synth"]
+        assert repr(port.nmi(s1, s2)) == rec["nmi_synth"]
+    for name, rec in golden_extras["hand"].items():
+        g = graphs.convert_edges(np.array(__import__("make_golden").HAND[name]))
+        port.load(g.indices, g.adj)
+        port.count_triangles()
+        assert port.clustering().tolist() == rec["clustering"], name
+        assert port.find_connected().tolist() == rec["components"], name
