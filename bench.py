@@ -5,9 +5,10 @@ Workload (N=1): R-MAT scale 24, edge factor 16, quadrants (.57, .19, .19, .05),
 seed 2, random vertex permutation, loops/duplicates/isolated vertices removed
 and vertices renumbered by decreasing degree as the reference converter does.
 One step = one synchronous label-propagation sweep with the Modularity rule,
-frac 1.0, from the singleton partition (the reference's first sweep: compress
-+ statistics are done before the timed sweep of every step, from the same
-start partition and the same rand_r seed).
+frac 1.0; the timed steps cycle through the first five sweeps of the
+reference's -s 0 schedule, each restored from a device copy of its start
+partition and run with that sweep's rand_r seed (compress + statistics of
+the start partition are done before the timed sweep).
 
 Lines printed (rank 0, one JSON line):
   value      refine-sweep edges/s, inputs resident in HBM, CUDA events on the
@@ -24,6 +25,8 @@ Lines printed (rank 0, one JSON line):
              serving loop vs the single-graph path one request at a time:
              graphs/s and latency percentiles
   convert    the workload's raw edge list through the GPU converter
+  extras     connected components and NMI on the workload graph, the
+             triangle-based initial partition on R-MAT scale 22
 With --impl reference: the reference's CPU path for this sweep (the oracle
 restatement; the reference's own objects cannot run on this host) on all host
 cores, same metric and workload.
@@ -409,6 +412,78 @@ def convert_leg(args, dev, ind, adj):
     return out
 
 
+def extras_leg(args, dev, ind, adj):
+    """The rows beside the sweep, on the GPU: FindConnectedRefinement
+    (pcd_find_connected) and the NMI of its labels against a synthetic
+    labeling (pcd_nmi_device) on the workload graph; the triangle-based
+    initial partition (pcd_clustering_partition_device, triangles counted
+    first and timed apart) on the R-MAT scale-22 graph of the same generator.
+    Wall time of each call (each synchronises), after one warm-up call.  CPU:
+    the oracle's restatements of the same functions on the scale-18 graph."""
+    import numpy as np
+    import torch
+
+    import graphs
+    import pcd
+
+    def timed(f):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        r = f()
+        return r, time.perf_counter() - t
+
+    ctx = pcd.Context(0)
+    out = {}
+    G = pcd.Graph.from_csr(ctx, ind, adj)
+    fc = pcd.FindConnectedRefinement()
+    fc.refine(G)
+    k, sec = timed(lambda: fc.refine(G))
+    n = G.n
+    out["find_connected"] = {"graph": f"rmat-s{args.scale}", "components": k, "ms": 1000 * sec,
+                             "edges_per_s": G.m / sec}
+    comp = torch.from_numpy(G.labels).to(dev)
+    synth = ((torch.arange(n, device=dev, dtype=torch.int64) * 7919) % 9973).to(torch.int32)
+    pcd.nmi(ctx, comp, synth, n)
+    v, sec = timed(lambda: pcd.nmi(ctx, comp, synth, n))
+    out["nmi"] = {"graph": f"rmat-s{args.scale}", "pairs": n, "value": v, "ms": 1000 * sec,
+                  "pairs_per_s": n / sec}
+    G.free()
+    del comp, synth
+    i22, a22, _ = graphs.rmat_torch(22, args.edge_factor, 0.57, 0.19, 0.19, seed=2, device=dev)
+    torch.cuda.empty_cache()
+    G = pcd.Graph.from_csr(ctx, i22, a22)
+    _, tsec = timed(lambda: G.count_triangles())
+    pcd.create_clustering_partition_device(G)
+    k, sec = timed(lambda: pcd.create_clustering_partition_device(G))
+    out["clustering_partition"] = {"graph": "rmat-s22", "n": G.n, "m": G.m, "communities": k,
+                                   "ms": 1000 * sec, "triangles_ms": 1000 * tsec, "vertices_per_s": G.n / sec}
+    G.free()
+    ctx.close()
+    if not args.no_cpu:
+        import oracle
+
+        i18, a18, _ = graphs.rmat_torch(18, args.edge_factor, 0.57, 0.19, 0.19, seed=2, device=dev)
+        port = oracle.Port().load(i18, a18)
+        port.count_triangles()
+        t = time.perf_counter()
+        port.clustering()
+        c1 = time.perf_counter() - t
+        t = time.perf_counter()
+        lab = port.find_connected()
+        c2 = time.perf_counter() - t
+        n18 = i18.shape[0] - 1
+        syn = ((np.arange(n18, dtype=np.int64) * 7919) % 9973).astype(np.int32)
+        t = time.perf_counter()
+        port.nmi(lab, syn)
+        c3 = time.perf_counter() - t
+        out["cpu_baseline"] = {"kind": "port", "cores": 1, "sample": f"R-MAT s18 (n {n18}, m {a18.shape[0] // 2})",
+                               "clustering_partition_vertices_per_s": n18 / c1,
+                               "find_connected_edges_per_s": (a18.shape[0] // 2) / c2,
+                               "nmi_pairs_per_s": n18 / c3}
+    log(f"[bench] extras: {json.dumps(out)}")
+    return out
+
+
 def serve_pool(dev):
     """The served mix's graphs (seed 5): SBMs with log-uniform sizes in
     [1000, 50000] (n/50 blocks, intra-degree 12, inter-degree 2), LFR-style
@@ -565,6 +640,8 @@ def main():
     ap.add_argument("--batch-iters", type=int, default=-1)
     ap.add_argument("--batch-threshold", type=float, default=0.0)
     ap.add_argument("--convert", type=int, default=1, help="0: skip the converter timing")
+    ap.add_argument("--extras", type=int, default=1,
+                    help="0: skip the components / NMI / initial-partition timings")
     ap.add_argument("--serve-requests", type=int, default=600, help="0: skip the served workload")
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[200.0, 2000.0])
     ap.add_argument("--serve-workers", type=int, default=4)
@@ -739,6 +816,11 @@ def main():
         torch.cuda.empty_cache()
         converted = convert_leg(args, dev, ind, adj)
 
+    extras = None
+    if args.extras:
+        torch.cuda.empty_cache()
+        extras = extras_leg(args, dev, ind, adj)
+
     served = None
     if args.serve_requests > 0:
         torch.cuda.empty_cache()
@@ -778,6 +860,7 @@ def main():
             "batched": batched,
             "served": served,
             "convert": converted,
+            "extras": extras,
             "gpu_launches": int(launches),
             "clocks": clk,
             "phases_ms": {nm: round(ms, 4) for nm, ms in phases.items()},

@@ -6,8 +6,10 @@
 * pcd_find_connected == FindConnectedRefinement::refine
   (src/refinement.cpp:291-322), bit-exact labels;
 * pcd_nmi / pcd_nmi_device == compare_communities + norm_mutual_info
-  (src/common.cpp:75-173) within 1e-12 relative (FP64, the GPU sums in a
-  different order and its log may differ from glibc's by an ulp).
+  (src/common.cpp:75-173) within 1e-12 relative, or within the reference's
+  own summation error where that is larger (it adds N near-equal terms in
+  sequence; the GPU adds them in a tree, and its log may differ from glibc's
+  by an ulp).
 """
 import hashlib
 
@@ -25,11 +27,29 @@ def sha(a):
     return hashlib.sha256(np.ascontiguousarray(a, dtype="<i4").tobytes()).hexdigest()
 
 
-def close(x, want):
+def close(x, want, ref_err=0.0):
+    """|x - want| <= 1e-12 relative, or within the reference's own summation
+    error bound ref_err (nmi_scale) where that is larger."""
     want = float(want)
     if want != want:
         return x != x  # NaN where the reference's arithmetic gives NaN
-    return abs(x - want) <= NMI_RTOL * max(abs(want), 1e-300) or (x == want)
+    return abs(x - want) <= max(NMI_RTOL * abs(want), ref_err) or (x == want)
+
+
+def nmi_scale(a, b, n):
+    """Bound of the reference's own rounding: it adds its N distinct-pair
+    terms one after another, so its nom carries up to N * 2^-53 * sum |term|
+    of error (the sum of many near-equal terms drifts that way), while the
+    GPU adds them in a tree.  Returns N * 2^-53 * 2 * sum |term| / |den|."""
+    a = np.asarray(a, np.int64)
+    b = np.asarray(b, np.int64)
+    ni = np.bincount(a).astype(np.float64)
+    nj = np.bincount(b).astype(np.float64)
+    key, val = np.unique(a * (int(b.max()) + 1) + b, return_counts=True)
+    i, j = key // (int(b.max()) + 1), key % (int(b.max()) + 1)
+    terms = val * np.log(val * float(n) / (ni[i] * nj[j]))
+    den = np.sum(ni[ni > 0] * np.log(ni[ni > 0] / n)) + np.sum(nj[nj > 0] * np.log(nj[nj > 0] / n))
+    return float(terms.shape[0] * 2.0**-53 * 2 * np.sum(np.abs(terms)) / abs(den))
 
 
 @pytest.mark.parametrize("name", ["sbm10k", "rmat12", "pl20k", "forest"])
@@ -98,7 +118,7 @@ def test_larger_graphs_against_oracle(ctx, port, scale):
     assert np.array_equal(comp, port.find_connected())
     want = port.nmi(clus, comp)
     got = pcd.compare_communities(G, clus, comp)
-    assert close(got, want)
+    assert close(got, want, nmi_scale(clus, comp, g.n))
     dev = pcd.nmi(ctx, torch.from_numpy(clus).cuda(), torch.from_numpy(comp).cuda(), g.n)
     assert dev == got  # same kernels, same order
     G.free()
