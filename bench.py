@@ -414,8 +414,8 @@ def convert_leg(args, dev, ind, adj):
 
 def extras_leg(args, dev, ind, adj):
     """The rows beside the sweep, on the GPU: FindConnectedRefinement
-    (pcd_find_connected) and the NMI of its labels against a synthetic
-    labeling (pcd_nmi_device) on the workload graph; the triangle-based
+    (pcd_find_connected) on the workload graph, the NMI (pcd_nmi_device) of
+    two synthetic labelings of its vertices; the triangle-based
     initial partition (pcd_clustering_partition_device, triangles counted
     first and timed apart) on the R-MAT scale-22 graph of the same generator.
     Wall time of each call (each synchronises), after one warm-up call.  CPU:
@@ -441,14 +441,17 @@ def extras_leg(args, dev, ind, adj):
     n = G.n
     out["find_connected"] = {"graph": f"rmat-s{args.scale}", "components": k, "ms": 1000 * sec,
                              "edges_per_s": G.m / sec}
-    comp = torch.from_numpy(G.labels).to(dev)
-    synth = ((torch.arange(n, device=dev, dtype=torch.int64) * 7919) % 9973).to(torch.int32)
-    pcd.nmi(ctx, comp, synth, n)
-    v, sec = timed(lambda: pcd.nmi(ctx, comp, synth, n))
+    # two synthetic labelings of the workload's vertices (the components'
+    # giant part would overflow the reference's int product ni * nj)
+    vid = torch.arange(n, device=dev, dtype=torch.int64)
+    la = ((vid * 7919) % 9973).to(torch.int32)
+    lb = (vid // 997).to(torch.int32)
+    pcd.nmi(ctx, la, lb, n)
+    v, sec = timed(lambda: pcd.nmi(ctx, la, lb, n))
     out["nmi"] = {"graph": f"rmat-s{args.scale}", "pairs": n, "value": v, "ms": 1000 * sec,
                   "pairs_per_s": n / sec}
     G.free()
-    del comp, synth
+    del vid, la, lb
     i22, a22, _ = graphs.rmat_torch(22, args.edge_factor, 0.57, 0.19, 0.19, seed=2, device=dev)
     torch.cuda.empty_cache()
     G = pcd.Graph.from_csr(ctx, i22, a22)
@@ -469,12 +472,12 @@ def extras_leg(args, dev, ind, adj):
         port.clustering()
         c1 = time.perf_counter() - t
         t = time.perf_counter()
-        lab = port.find_connected()
+        port.find_connected()
         c2 = time.perf_counter() - t
         n18 = i18.shape[0] - 1
-        syn = ((np.arange(n18, dtype=np.int64) * 7919) % 9973).astype(np.int32)
+        vid = np.arange(n18, dtype=np.int64)
         t = time.perf_counter()
-        port.nmi(lab, syn)
+        port.nmi(((vid * 7919) % 9973).astype(np.int32), (vid // 997).astype(np.int32))
         c3 = time.perf_counter() - t
         out["cpu_baseline"] = {"kind": "port", "cores": 1, "sample": f"R-MAT s18 (n {n18}, m {a18.shape[0] // 2})",
                                "clustering_partition_vertices_per_s": n18 / c1,

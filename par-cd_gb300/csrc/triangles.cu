@@ -6,9 +6,14 @@
 //     single-threaded call does (src/main.cpp:195), so it is bit-exact;
 //   * WCCRule::calculate (src/rules.cpp:150-235): the same counts restricted
 //     to triangles inside one community, then the per-vertex WCC terms.
-// Each undirected edge (v, u), u < v, is handled once by the warp that owns v:
-// lanes take different u and intersect the two sorted rows, walking the
-// shorter row and binary-searching the longer one.
+// The reference's orientation: a triangle w < u < v is found once, from the
+// edge (v, u) of v's row prefix (neighbours below v), by intersecting v's
+// neighbours below u with u's neighbours below u; the edge counts live at
+// each edge's position in its higher endpoint's row.  On the device a warp
+// owns v and its lanes take different u; a lane walks the shorter of the two
+// lists and binary-searches the longer.  A second pass turns the edge counts
+// into tri / tri_deg.  The edge counts use the tie buffer (>= 2m ints), which
+// no sweep holds while triangles are counted or WCC is scored.
 #include "pcd_device.cuh"
 #include "pcd_internal.h"
 
@@ -26,38 +31,72 @@ __device__ __forceinline__ int32_t lower_bound_i32(const int32_t *__restrict__ a
     return lo;
 }
 
-// |N(v) cap N(u)|, optionally only common neighbours w with labels[w] == l.
-__device__ int32_t intersect(const int32_t *__restrict__ indices, const int32_t *__restrict__ adj, int32_t v,
-                             int32_t u, const int32_t *__restrict__ labels, int32_t l) {
-    int32_t bv = indices[v], ev = indices[v + 1], bu = indices[u], eu = indices[u + 1];
-    if (ev - bv > eu - bu) {
-        int32_t t;
-        t = bv; bv = bu; bu = t;
-        t = ev; ev = eu; eu = t;
-    }
-    int32_t c = 0, pos = bu;
-    for (int32_t j = bv; j < ev && pos < eu; ++j) {
-        int32_t w = adj[j];
-        pos = lower_bound_i32(adj, pos, eu, w);
-        if (pos < eu && adj[pos] == w && (!labels || labels[w] == l)) ++c;
-    }
-    return c;
-}
-
-__global__ void k_triangles(const int32_t *__restrict__ indices, const int32_t *__restrict__ adj, int32_t n,
-                            const int32_t *__restrict__ labels, int32_t *tri, int32_t *tri_deg) {
+// Edge counts of the triangles closed through the prefix edges of each v
+// (labels non-null: only triangles whose three vertices share a label).
+__global__ void __launch_bounds__(256) k_tri_edges(const int32_t *__restrict__ indices,
+                                                   const int32_t *__restrict__ adj, int32_t n,
+                                                   const int32_t *__restrict__ labels, int32_t *et) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t v = warp; v < n; v += nwarps) {
-        const int32_t b = indices[v], e = indices[v + 1];
+    for (int64_t vv = warp; vv < n; vv += nwarps) {
+        const int32_t v = (int32_t)vv;
+        const int32_t bv = indices[v], ev = indices[v + 1];
         const int32_t l = labels ? labels[v] : 0;
+        for (int32_t j0 = bv; j0 < ev; j0 += 32) {
+            const int32_t r = j0 + lane;
+            const int32_t u = r < ev ? adj[r] : INT32_MAX;
+            if (!__any_sync(FULL, u < v)) break;  // rows are sorted: the prefix has ended
+            if (u >= v || (labels && labels[u] != l)) continue;
+            const int32_t bu = indices[u], eu = lower_bound_i32(adj, bu, indices[u + 1], u);
+            // A = v's neighbours below u = [bv, r); B = u's neighbours below u = [bu, eu)
+            int32_t c = 0;
+            if (r - bv <= eu - bu) {
+                int32_t y = bu;
+                for (int32_t x = bv; x < r && y < eu; ++x) {
+                    const int32_t w = adj[x];
+                    y = lower_bound_i32(adj, y, eu, w);
+                    if (y < eu && adj[y] == w && (!labels || labels[w] == l)) {
+                        atomicAdd(et + x, 1);
+                        atomicAdd(et + y, 1);
+                        ++c;
+                    }
+                }
+            } else {
+                int32_t x = bv;
+                for (int32_t y = bu; y < eu && x < r; ++y) {
+                    const int32_t w = adj[y];
+                    x = lower_bound_i32(adj, x, r, w);
+                    if (x < r && adj[x] == w && (!labels || labels[w] == l)) {
+                        atomicAdd(et + x, 1);
+                        atomicAdd(et + y, 1);
+                        ++c;
+                    }
+                }
+            }
+            if (c) atomicAdd(et + r, c);
+        }
+    }
+}
+
+// tri[v] / tri_deg[v] from the edge counts at the prefix positions.
+__global__ void __launch_bounds__(256) k_tri_vertices(const int32_t *__restrict__ indices,
+                                                      const int32_t *__restrict__ adj, int32_t n,
+                                                      const int32_t *__restrict__ et, int32_t *tri,
+                                                      int32_t *tri_deg) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t vv = warp; vv < n; vv += nwarps) {
+        const int32_t v = (int32_t)vv;
+        const int32_t bv = indices[v], ev = indices[v + 1];
         int32_t my_t = 0, my_td = 0;
-        for (int32_t j = b + lane; j < e; j += 32) {
-            const int32_t u = adj[j];
-            if (u >= v) continue;  // rows are sorted: u < v is a prefix
-            if (labels && labels[u] != l) continue;
-            const int32_t c = intersect(indices, adj, (int32_t)v, u, labels, l);
+        for (int32_t j0 = bv; j0 < ev; j0 += 32) {
+            const int32_t r = j0 + lane;
+            const int32_t u = r < ev ? adj[r] : INT32_MAX;
+            if (!__any_sync(FULL, u < v)) break;
+            if (u >= v) continue;
+            const int32_t c = et[r];
             if (c > 0) {
                 my_t += c;
                 my_td += 1;
@@ -72,6 +111,20 @@ __global__ void k_triangles(const int32_t *__restrict__ indices, const int32_t *
             atomicAdd(tri_deg + v, my_td);
         }
     }
+}
+
+static void launch_tri_counts(pcd_graph *g, const int32_t *labels, int32_t *tri, int32_t *tri_deg,
+                              cudaStream_t st) {
+    int32_t *et = g->tiebuf;  // >= 2m ints
+    cudaMemsetAsync(et, 0, sizeof(int32_t) * (size_t)g->nnz, st);
+    cudaMemsetAsync(tri, 0, sizeof(int32_t) * (size_t)g->n, st);
+    cudaMemsetAsync(tri_deg, 0, sizeof(int32_t) * (size_t)g->n, st);
+    int64_t blocks = ((int64_t)g->n * 32 + 255) / 256;
+    const int64_t cap = (int64_t)g->ctx->num_sms * 16;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    k_tri_edges<<<(unsigned)blocks, 256, 0, st>>>(g->indices, g->adj, g->n, labels, et);
+    k_tri_vertices<<<(unsigned)blocks, 256, 0, st>>>(g->indices, g->adj, g->n, et, tri, tri_deg);
 }
 
 // clustering_coef = sum over v of (tri / (deg (deg - 1.0))) / n, in vertex
@@ -107,20 +160,13 @@ __global__ void k_clustering_coef(const int32_t *__restrict__ indices, const int
 }
 
 int launch_triangles(pcd_graph *g, cudaStream_t st) {
-    cudaMemsetAsync(g->tri, 0, sizeof(int32_t) * (size_t)g->n, st);
-    cudaMemsetAsync(g->tri_deg, 0, sizeof(int32_t) * (size_t)g->n, st);
-    int64_t warps = g->n;
-    unsigned blocks = (unsigned)((warps * 32 + 255) / 256);
-    unsigned cap = (unsigned)g->ctx->num_sms * 16;
-    if (blocks > cap) blocks = cap;
-    if (blocks < 1) blocks = 1;
-    k_triangles<<<blocks, 256, 0, st>>>(g->indices, g->adj, g->n, nullptr, g->tri, g->tri_deg);
+    launch_tri_counts(g, nullptr, g->tri, g->tri_deg, st);
     if (g->batch)
         k_clustering_coef<<<(g->batch->G + 7) / 8, 256, 0, st>>>(g->indices, g->tri, g->n, g->batch->voff,
                                                                   g->batch->G, g->batch->gcc);
     else
         k_clustering_coef<<<1, 32, 0, st>>>(g->indices, g->tri, g->n, nullptr, 1, g->d_score);
-    return 2;
+    return 3;
 }
 
 // ---------------------------------------------------------------------------
@@ -183,18 +229,11 @@ int launch_wcc_score(pcd_graph *g, double *d_out, cudaStream_t st) {
     // intra-community counts reuse the propagation scratch: ndraw and first
     int32_t *it = reinterpret_cast<int32_t *>(g->ndraw);
     int32_t *itd = g->first;
-    cudaMemsetAsync(it, 0, sizeof(int32_t) * (size_t)g->n, st);
-    cudaMemsetAsync(itd, 0, sizeof(int32_t) * (size_t)g->n, st);
-    int64_t warps = g->n;
-    unsigned blocks = (unsigned)((warps * 32 + 255) / 256);
-    unsigned cap = (unsigned)g->ctx->num_sms * 16;
-    if (blocks > cap) blocks = cap;
-    if (blocks < 1) blocks = 1;
-    k_triangles<<<blocks, 256, 0, st>>>(g->indices, g->adj, g->n, g->labels, it, itd);
+    launch_tri_counts(g, g->labels, it, itd, st);
     BatchState *B = g->batch;
     k_wcc_graph<<<B ? B->G : 1, WCC_THREADS, 0, st>>>(g->n, B ? B->voff : nullptr, g->labels, g->sizes, g->tri,
                                                       g->tri_deg, it, itd, B ? B->gscore : d_out);
-    return 2;
+    return 3;
 }
 
 }  // namespace pcd
