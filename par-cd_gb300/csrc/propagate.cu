@@ -141,100 +141,6 @@ __device__ __forceinline__ long long alloc_ties_warp(const SweepArgs &a, int32_t
 }
 
 // ---------------------------------------------------------------------------
-// G lanes per vertex (deg <= G, G in {4, 8, 16, 32}): the whole row sits in
-// registers, one neighbour per lane in row order.  Lanes holding the same
-// label are merged with match_any; the lowest lane of each set is the label's
-// first occurrence and carries its count.  The ordered running maximum is a
-// segmented warp scan over the group.
-// ---------------------------------------------------------------------------
-template <class R, int G>
-__global__ void __launch_bounds__(256) k_prop_group(SweepArgs a, R rule, const int32_t *__restrict__ list,
-                                                    int64_t count) {
-    using Key = typename R::Key;
-    using E = Elem<Key>;
-    constexpr int VPW = 32 / G;
-    const int lane = threadIdx.x & 31, gl = lane & (G - 1), gid = lane / G;
-    const unsigned gmask = G == 32 ? FULL : (((1u << G) - 1u) << (gid * G));
-    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t base = warp * VPW; base < count; base += nwarps * VPW) {
-        const int64_t idx = base + gid;
-        const bool has_v = idx < count;
-        const int32_t v = has_v ? list[idx] : 0;
-        const int32_t b = has_v ? a.g.indices[v] : 0;
-        const int32_t d = has_v ? a.g.indices[v + 1] - b : 0;
-        const int32_t curr = has_v ? a.labels[v] : -1;
-        const R vr = has_v ? rule.at(v) : rule;
-        const bool valid = gl < d;
-        const int32_t lab = valid ? a.labels[a.g.adj[b + gl]] : -1;
-        const unsigned long long mk =
-            valid ? (((unsigned long long)(unsigned)gid << 32) | (unsigned)lab) : (~0ull << 32) | (unsigned)lane;
-        const unsigned peers = __match_any_sync(FULL, mk);
-        const bool first = valid && lane == __ffs(peers) - 1;
-        const int32_t k = __popc(peers);
-        const bool is_curr = first && lab == curr;
-        bool sc = first && !is_curr;
-        Tag tag{0, 0};
-        Key key = R::identity();
-        if (sc) {
-            key = vr.join(v, d, lab, k, a.cm, tag);
-            if (!R::usable(key)) {
-                sc = false;
-                key = R::identity();
-            }
-        }
-        const E x{key, sc ? gl : -2};
-        const E inc = warp_scan_max<R, G>(x, gl);
-        E ex = shfl_up_any(inc, 1, G);
-        if (gl == 0) ex = E{R::identity(), -2};
-        const E init{R::initial(), -1};
-        const E pre = combine<R>(init, ex);
-        const E fin = combine<R>(init, shfl_any(inc, G - 1, G));
-        const bool tie = sc && R::eq(key, pre.key);
-        // tag of the holder each tie compared against (a lane of this group)
-        const Tag htag{__shfl_sync(FULL, tag.k, pre.ord >= 0 ? pre.ord : gl, G),
-                       __shfl_sync(FULL, tag.V, pre.ord >= 0 ? pre.ord : gl, G)};
-        const bool amb_tie = tie && R::ambiguous_tie(tag, htag, pre.ord >= 0);
-        const bool inrun = tie && pre.ord == fin.ord;
-        const unsigned tm = __ballot_sync(FULL, tie) & gmask;
-        const unsigned rm = __ballot_sync(FULL, inrun) & gmask;
-        const unsigned cm = __ballot_sync(FULL, is_curr) & gmask;
-        bool amb = (__ballot_sync(FULL, amb_tie) & gmask) != 0;
-        const int32_t ck = __shfl_sync(FULL, k, cm ? __ffs(cm) - 1 : lane);
-        const int32_t curr_freq = cm ? ck : 0;
-        const int32_t holder = __shfl_sync(FULL, lab, fin.ord >= 0 ? fin.ord : gl, G);
-        const int32_t r = __popc(rm);
-        int32_t dec = DEC_STAY;
-        if (has_v) {
-            amb |= vr.vertex_ambiguous(d);
-            if (!amb) dec = vr.decide(fin.key, fin.ord >= 0, v, d, curr, curr_freq, a.cm);
-            if (dec == DEC_AMBIGUOUS) amb = true;
-        }
-        const bool leader = has_v && gl == 0;
-        const bool rec = has_v && !amb && dec == DEC_MOVE && r > 0;  // the same in every lane of the group
-        const long long off = rec ? (long long)b + v : -1;
-        if (off >= 0 && inrun) a.tiebuf[off + 1 + __popc(rm & lanemask_lt())] = lab;
-        if (leader) {
-            if (amb) {
-                push_ambiguous(a, v, d);
-            } else {
-                a.ndraw[v] = (uint32_t)__popc(tm);
-                write_decision(a, v, dec, holder, curr);
-                record_ties(a, v, b, rec, r, holder);
-            }
-        }
-    }
-}
-
-// ---------------------------------------------------------------------------
-// warp per vertex (deg <= WCAP): adjacency in chunks of 32 in order; lanes
-// holding the same label are merged with match_any and the lowest lane (the
-// first occurrence) inserts into the warp's shared hash; new labels get
-// consecutive ordinals in lane order, so ordinals are first-occurrence order.
-// Then an ordered warp scan of the gains with the running maximum carried
-// across chunks.
-// ---------------------------------------------------------------------------
-// ---------------------------------------------------------------------------
 // One thread per vertex (deg <= MAXD): the reference's candidate loop run as
 // it is written, on a row held in registers.  Counting is a pass over the
 // pairs i < j of the row (an equal later label adds to the earlier one's
@@ -326,6 +232,42 @@ __global__ void __launch_bounds__(256) k_prop_thread(SweepArgs a, R rule, const 
     }
 }
 
+template <class R>
+struct PackedKey {
+    using K = double;
+    __device__ static K ident() { return -__longlong_as_double(0x7ff0000000000000LL); }
+    __device__ static K init() { return 0.0; }
+    __device__ static K make(typename R::Key raw, int32_t) { return raw; }
+    __device__ static double level(K x) { return x; }
+    __device__ static bool tie_ambiguous(K, K) { return false; }
+    __device__ static typename R::Key raw_level(K x) { return x; }
+};
+
+template <>
+struct PackedKey<RuleModInt> {
+    using K = long long;
+    __device__ static K ident() { return LLONG_MIN; }
+    __device__ static K init() { return 0; }
+    __device__ static K make(long long n, int32_t k) { return (long long)((unsigned long long)n << 14) | k; }
+    __device__ static long long level(K x) { return x >> 14; }
+    __device__ static bool tie_ambiguous(K c, K pre) { return ((c ^ pre) & 0x3FFF) != 0; }
+    __device__ static long long raw_level(K x) { return x >> 14; }
+};
+
+template <class K>
+__device__ __forceinline__ K kmax(K a, K b) {
+    return a > b ? a : b;
+}
+
+// ---------------------------------------------------------------------------
+// warp per vertex (deg <= WCAP): adjacency in chunks of 32 in order; lanes
+// holding the same label are merged with match_any and the lowest lane (the
+// first occurrence) inserts into the warp's shared hash; new labels get
+// consecutive ordinals in lane order, so ordinals are first-occurrence order.
+// The candidates are then scored in ordinal order with packed keys, as in the
+// one-pass block kernel: their maximum first, then one ordered pass from the
+// initial 0.0 for the ties with the running maximum and the final level.
+// ---------------------------------------------------------------------------
 // Shared memory of one warp of k_prop_warp: the label table (int32, 2 WCAP
 // slots; the scoring pass reuses it for the tie list), first-occurrence
 // labels (int32), counts (uint16, <= WCAP) and slot ordinals (uint8, < WCAP).
@@ -402,60 +344,72 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
             nc += __popc(newmask);
             __syncwarp();
         }
-        // ordered scoring
-        E carry{R::initial(), -1};
-        Tag ctag{0, 0};
-        uint32_t t = 0;
-        int32_t r = 0, my_curr = 0;
-        bool amb = false;
-        for (int32_t base = 0; base < nc; base += 32) {
-            const int32_t i = base + lane;
-            const bool valid = i < nc;
-            const int32_t l = valid ? clab[i] : -1;
-            const int32_t k = valid ? ccnt[i] : 0;
-            const bool is_curr = valid && l == curr;
-            if (is_curr) my_curr = k;
-            bool sc = valid && !is_curr;
-            Tag tag{0, 0};
-            Key key = R::identity();
-            if (sc) {
-                key = vr.join(v, d, l, k, a.cm, tag);
-                if (!R::usable(key)) {
-                    sc = false;
-                    key = R::identity();
+        // scoring over the candidates in first-occurrence order, with packed
+        // keys as in the one-pass block kernel: A the keys (registers) and their
+        // maximum, B the ordered pass from the initial 0.0 (ties with the running
+        // maximum, FP64 ambiguity, the final level's labels in order)
+        using PK = PackedKey<R>;
+        using K = typename PK::K;
+        constexpr int CH = WCAP / 32;
+        K key[CH];
+        int32_t my_curr = 0;
+        K wmax = PK::ident();
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+            const int32_t i = 32 * c + lane;
+            key[c] = PK::ident();
+            if (i < nc) {
+                const int32_t l = clab[i], k = ccnt[i];
+                if (l == curr) {
+                    my_curr = k;
+                } else {
+                    Tag tag{0, 0};
+                    const Key raw = vr.join(v, d, l, k, a.cm, tag);
+                    if (R::usable(raw)) key[c] = PK::make(raw, k);
                 }
             }
-            if (!__any_sync(FULL, sc && !R::gt(carry.key, key))) continue;  // nothing reaches the maximum
-            const E inc = warp_scan_max<R>(E{key, sc ? i : -2}, lane);
-            E ex = shfl_up_any(inc, 1);
-            if (lane == 0) ex = E{R::identity(), -2};
-            const E pre = combine<R>(carry, ex);
-            const bool tie = sc && R::eq(key, pre.key);
-            // the holder a tie met: the carried holder or a lane of this chunk
-            const bool in_chunk = pre.ord >= base;
-            const int src = in_chunk ? pre.ord - base : lane;
-            const Tag lt{__shfl_sync(FULL, tag.k, src), __shfl_sync(FULL, tag.V, src)};
-            const Tag htag = in_chunk ? lt : ctag;
-            if (tie && R::ambiguous_tie(tag, htag, pre.ord >= 0)) amb = true;
-            t += __popc(__ballot_sync(FULL, tie));
-            const E nxt = combine<R>(carry, shfl_any(inc, 31));
-            if (nxt.ord != carry.ord) {
-                r = 0;
-                const int hs = nxt.ord - base;  // a new holder is always in this chunk
-                ctag = Tag{__shfl_sync(FULL, tag.k, hs), __shfl_sync(FULL, tag.V, hs)};
+            wmax = kmax(wmax, key[c]);
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) wmax = kmax(wmax, __shfl_xor_sync(FULL, wmax, o));
+        const K mreal = wmax;
+        const auto lfin = PK::level(kmax(PK::init(), mreal));
+        K carry = PK::init();
+        uint32_t t = 0;
+        int32_t nfin = 0;
+        bool amb = false;
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+            if (32 * c >= nc) break;
+            const int32_t i = 32 * c + lane;
+            const bool cand = key[c] != PK::ident();
+            const bool fin = cand && PK::level(key[c]) == lfin;
+            const unsigned fm = __ballot_sync(FULL, fin);
+            if (fin) ties[nfin + __popc(fm & lanemask_lt())] = clab[i];
+            nfin += __popc(fm);
+            if (!__any_sync(FULL, cand && PK::level(key[c]) >= PK::level(carry))) continue;
+            K inc = key[c];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const K y = __shfl_up_sync(FULL, inc, o);
+                if (lane >= o) inc = kmax(inc, y);
             }
-            const bool inrun = tie && pre.ord == nxt.ord;
-            const unsigned run = __ballot_sync(FULL, inrun);
-            if (inrun) ties[r + __popc(run & lanemask_lt())] = l;
-            r += __popc(run);
-            carry = nxt;
+            K ex = __shfl_up_sync(FULL, inc, 1);
+            if (lane == 0) ex = PK::ident();
+            const K pre = kmax(carry, ex);
+            const bool tie = cand && PK::level(key[c]) == PK::level(pre);
+            if (tie && PK::tie_ambiguous(key[c], pre)) amb = true;
+            t += __popc(__ballot_sync(FULL, tie));
+            carry = kmax(carry, __shfl_sync(FULL, inc, 31));
         }
         __syncwarp();
         amb = __any_sync(FULL, amb);
         const int32_t curr_freq = __reduce_add_sync(FULL, my_curr);
-        const bool has = carry.ord >= 0;
-        const int32_t holder = has ? clab[carry.ord] : -1;
-        int32_t dec = amb ? DEC_AMBIGUOUS : vr.decide(carry.key, has, v, d, curr, curr_freq, a.cm);
+        const bool has = mreal != PK::ident() && PK::level(mreal) > PK::level(PK::init());
+        const int32_t holder = has ? ties[0] : -1;
+        const int32_t r = has ? nfin - 1 : 0;
+        int32_t dec = DEC_AMBIGUOUS;
+        if (!amb) dec = vr.decide(has ? PK::raw_level(mreal) : R::initial(), has, v, d, curr, curr_freq, a.cm);
         if (dec == DEC_AMBIGUOUS) {
             if (lane == 0) push_ambiguous(a, v, d);
             continue;
@@ -468,7 +422,7 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
             record_ties(a, v, b, rec, r, holder);
         }
         if (off >= 0)
-            for (int32_t j = lane; j < r; j += 32) a.tiebuf[off + 1 + j] = ties[j];
+            for (int32_t j = lane; j < r; j += 32) a.tiebuf[off + 1 + j] = ties[1 + j];
         __syncwarp();
     }
 }
@@ -808,33 +762,6 @@ __global__ void __launch_bounds__(BT) k_prop_block(SweepArgs a, R rule, const in
 //     initial 0.0 packs as k = 0, which no real candidate has.
 //   FP64 rules: the gain itself (NaN gains are not candidates).
 // ---------------------------------------------------------------------------
-template <class R>
-struct PackedKey {
-    using K = double;
-    __device__ static K ident() { return -__longlong_as_double(0x7ff0000000000000LL); }
-    __device__ static K init() { return 0.0; }
-    __device__ static K make(typename R::Key raw, int32_t) { return raw; }
-    __device__ static double level(K x) { return x; }
-    __device__ static bool tie_ambiguous(K, K) { return false; }
-    __device__ static typename R::Key raw_level(K x) { return x; }
-};
-
-template <>
-struct PackedKey<RuleModInt> {
-    using K = long long;
-    __device__ static K ident() { return LLONG_MIN; }
-    __device__ static K init() { return 0; }
-    __device__ static K make(long long n, int32_t k) { return (long long)((unsigned long long)n << 14) | k; }
-    __device__ static long long level(K x) { return x >> 14; }
-    __device__ static bool tie_ambiguous(K c, K pre) { return ((c ^ pre) & 0x3FFF) != 0; }
-    __device__ static long long raw_level(K x) { return x >> 14; }
-};
-
-template <class K>
-__device__ __forceinline__ K kmax(K a, K b) {
-    return a > b ? a : b;
-}
-
 // ---------------------------------------------------------------------------
 // block per vertex, one keyed pass (degrees up to NW * 32 * RPL).
 //   H  histogram: labels into the shared table (label, count, first position by
@@ -1319,267 +1246,6 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
 }
 
 // ---------------------------------------------------------------------------
-// hubs: one 512-thread block per vertex with the table in a per-block HBM
-// slice.  Random HBM traffic is what costs here, so after the histogram the
-// table is walked once in slot order: each candidate is written to
-// position-indexed arrays (label, count) at its first position and its slot
-// is cleared in the same coalesced sweep.  The ordered passes then read the
-// position arrays sequentially.  Slice layout: keys, counts, first positions
-// (fb_slots each), labels and counts by position (max degree each).
-// ---------------------------------------------------------------------------
-template <class R, int U>
-__global__ void __launch_bounds__(512) k_prop_hub(SweepArgs a, R rule, const int32_t *__restrict__ list,
-                                                  int64_t count, int32_t slots, int32_t *gscratch, int64_t gstride) {
-    using Key = typename R::Key;
-    using E = Elem<Key>;
-    constexpr int BT = 512, NW = BT / 32;
-    __shared__ BlockScratch<R> s;
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    int32_t *keys = gscratch + (int64_t)blockIdx.x * gstride;
-    int32_t *cnts = keys + slots;
-    uint32_t *fpos = reinterpret_cast<uint32_t *>(cnts + slots);
-    int32_t *posL = cnts + 2 * slots;
-    for (int64_t vi = blockIdx.x; vi < count; vi += gridDim.x) {
-        const int32_t v = list[vi];
-        const int32_t b = a.g.indices[v], e = a.g.indices[v + 1], d = e - b;
-        const int32_t curr = a.labels[v];
-        const R vr = rule.at(v);
-        if (vr.vertex_ambiguous(d)) {
-            if (tid == 0) push_ambiguous(a, v, d);
-            continue;
-        }
-        int32_t ts = 64;
-        while (ts < 2 * d) ts <<= 1;
-        if (ts > slots) {
-            if (tid == 0) atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);
-            continue;
-        }
-        int32_t *posC = posL + d;
-        for (int32_t p = tid; p < d; p += BT) posL[p] = -1;
-        if (tid == 0) {
-            s.t = 0;
-            s.amb = 0;
-            s.curr_freq = 0;
-        }
-        __syncthreads();
-        for (int32_t p0 = 0; p0 < d; p0 += BT * U) {
-            int32_t lab[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int32_t p = p0 + u * BT + tid;
-                lab[u] = p < d ? a.g.adj[b + p] : -1;
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) lab[u] = lab[u] >= 0 ? a.labels[lab[u]] : -2;
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int32_t p = p0 + u * BT + tid;
-                const int32_t l = lab[u];
-                const unsigned peers = __match_any_sync(FULL, l);
-                if (p < d && lane == __ffs(peers) - 1) {
-                    uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
-                    for (;;) {
-                        int32_t kk = keys[h];
-                        if (kk == l) break;
-                        if (kk == -1) {
-                            int32_t old = atomicCAS(&keys[h], -1, l);
-                            if (old == -1 || old == l) break;
-                        }
-                        h = (h + 1) & (uint32_t)(ts - 1);
-                    }
-                    atomicAdd(&cnts[h], __popc(peers));
-                    atomicMin(&fpos[h], (uint32_t)p);
-                }
-            }
-        }
-        __syncthreads();
-        for (int32_t i = tid; i < ts; i += BT) {
-            const int32_t kk = keys[i];
-            if (kk != -1) {
-                const uint32_t fp = fpos[i];
-                posL[fp] = kk;
-                posC[fp] = cnts[i];
-                keys[i] = -1;
-                cnts[i] = 0;
-                fpos[i] = 0xffffffffu;
-            }
-        }
-        __syncthreads();
-        const int32_t span = ((d + NW - 1) / NW + 32 * U - 1) / (32 * U) * (32 * U);
-        const int32_t lo = min(d, wid * span), hi = min(d, lo + span);
-        {  // pass A
-            E carry{R::identity(), -2};
-            Tag ctag{0, 0};
-            int32_t clabel = -1;
-            for (int32_t base0 = lo; base0 < hi; base0 += 32 * U) {
-                int32_t l[U], k[U];
-                Key key[U];
-                Tag tag[U];
-                bool sc[U];
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const int32_t p = base0 + 32 * u + lane;
-                    l[u] = p < hi ? posL[p] : -1;
-                    k[u] = p < hi ? posC[p] : 0;
-                }
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    if (l[u] >= 0 && l[u] == curr) s.curr_freq = k[u];
-                    sc[u] = l[u] >= 0 && l[u] != curr;
-                    tag[u] = Tag{0, 0};
-                    key[u] = R::identity();
-                    if (sc[u]) {
-                        key[u] = vr.join(v, d, l[u], k[u], a.cm, tag[u]);
-                        if (!R::usable(key[u])) {
-                            sc[u] = false;
-                            key[u] = R::identity();
-                        }
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    if (!__any_sync(FULL, sc[u] && R::gt(key[u], carry.key))) continue;
-                    const Key wm = warp_max_key<R>(key[u]);
-                    const int fl = __ffs(__ballot_sync(FULL, sc[u] && R::eq(key[u], wm))) - 1;
-                    carry = E{wm, base0 + 32 * u + fl};
-                    ctag = Tag{__shfl_sync(FULL, tag[u].k, fl), __shfl_sync(FULL, tag[u].V, fl)};
-                    clabel = __shfl_sync(FULL, l[u], fl);
-                }
-            }
-            if (lane == 0) {
-                s.warp_tot[wid] = carry;
-                s.carry_tag[wid] = ctag;
-                s.warp_label[wid] = clabel;
-            }
-        }
-        __syncthreads();
-        if (wid == 0) {
-            const E wt = lane < NW ? s.warp_tot[lane] : E{R::identity(), -2};
-            const Tag wtag = lane < NW ? s.carry_tag[lane] : Tag{0, 0};
-            const E wi = warp_scan_max<R>(wt, lane);
-            E we = shfl_up_any(wi, 1);
-            if (lane == 0) we = E{R::identity(), -2};
-            const E init{R::initial(), -1};
-            const E cin = combine<R>(init, we);
-            const E fin = combine<R>(init, shfl_any(wi, 31));
-            int src = lane, fsrc = 0;
-            for (int w2 = 0; w2 < NW; ++w2) {
-                const int32_t o = __shfl_sync(FULL, wt.ord, w2);
-                if (cin.ord >= 0 && o == cin.ord) src = w2;
-                if (fin.ord >= 0 && o == fin.ord) fsrc = w2;
-            }
-            const Tag ct{__shfl_sync(FULL, wtag.k, src), __shfl_sync(FULL, wtag.V, src)};
-            const int32_t wl = lane < NW ? s.warp_label[lane] : -1;
-            const int32_t fl = __shfl_sync(FULL, wl, fsrc);
-            __syncwarp();
-            if (lane < NW) {
-                s.carry_in[lane] = cin;
-                s.carry_tag[lane] = ct;
-            }
-            if (lane == 0) {
-                s.fin = fin;
-                s.fin_label = fin.ord >= 0 ? fl : -1;
-            }
-        }
-        __syncthreads();
-        {  // pass B
-            E carry = s.carry_in[wid];
-            Tag ctag = s.carry_tag[wid];
-            const E fin = s.fin;
-            uint32_t t = 0;
-            int32_t nt = 0;
-            bool amb = false;
-            for (int32_t base0 = lo; base0 < hi; base0 += 32 * U) {
-                int32_t l[U], k[U];
-                Key key[U];
-                Tag tag[U];
-                bool sc[U];
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const int32_t p = base0 + 32 * u + lane;
-                    l[u] = p < hi ? posL[p] : -1;
-                    k[u] = p < hi ? posC[p] : 0;
-                }
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    sc[u] = l[u] >= 0 && l[u] != curr;
-                    tag[u] = Tag{0, 0};
-                    key[u] = R::identity();
-                    if (sc[u]) {
-                        key[u] = vr.join(v, d, l[u], k[u], a.cm, tag[u]);
-                        if (!R::usable(key[u])) {
-                            sc[u] = false;
-                            key[u] = R::identity();
-                        }
-                    }
-                }
-                __syncwarp();
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    if (!__any_sync(FULL, sc[u] && !R::gt(carry.key, key[u]))) continue;
-                    const int32_t base = base0 + 32 * u;
-                    const E inc = warp_scan_max<R>(E{key[u], sc[u] ? base + lane : -2}, lane);
-                    E ex = shfl_up_any(inc, 1);
-                    if (lane == 0) ex = E{R::identity(), -2};
-                    const E pre = combine<R>(carry, ex);
-                    const bool tie = sc[u] && R::eq(key[u], pre.key);
-                    const bool in_chunk = pre.ord >= base;
-                    const int src = in_chunk ? pre.ord - base : lane;
-                    const Tag lt{__shfl_sync(FULL, tag[u].k, src), __shfl_sync(FULL, tag[u].V, src)};
-                    const Tag htag = in_chunk ? lt : ctag;
-                    if (tie && R::ambiguous_tie(tag[u], htag, pre.ord >= 0)) amb = true;
-                    t += __popc(__ballot_sync(FULL, tie));
-                    const E nxt = combine<R>(carry, shfl_any(inc, 31));
-                    if (nxt.ord != carry.ord) {
-                        const int hs = nxt.ord - base;
-                        ctag = Tag{__shfl_sync(FULL, tag[u].k, hs), __shfl_sync(FULL, tag[u].V, hs)};
-                    }
-                    const bool inrun = tie && pre.ord == fin.ord;
-                    const unsigned run = __ballot_sync(FULL, inrun);
-                    if (inrun) posL[lo + nt + __popc(run & lanemask_lt())] = l[u];
-                    nt += __popc(run);
-                    carry = nxt;
-                }
-            }
-            amb = __any_sync(FULL, amb);
-            if (lane == 0) {
-                s.warp_ties[wid] = nt;
-                if (t) atomicAdd(&s.t, t);
-                if (amb) s.amb = 1;
-            }
-        }
-        __syncthreads();
-        if (tid == 0) {
-            const E c = s.fin;
-            int32_t r = 0;
-            for (int w = 0; w < NW; ++w) {
-                s.tie_off[w] = r;
-                r += s.warp_ties[w];
-            }
-            s.r = r;
-            s.off = -1;
-            const int32_t dec = s.amb ? DEC_AMBIGUOUS : vr.decide(c.key, c.ord >= 0, v, d, curr, s.curr_freq, a.cm);
-            if (dec == DEC_AMBIGUOUS) {
-                push_ambiguous(a, v, d);
-            } else {
-                a.ndraw[v] = s.t;
-                write_decision(a, v, dec, s.fin_label, curr);
-                s.off = record_ties(a, v, b, dec == DEC_MOVE && r > 0, r, s.fin_label);
-            }
-        }
-        __syncthreads();
-        {
-            const long long off = s.off;
-            if (off >= 0) {
-                const int32_t nt = s.warp_ties[wid], o = s.tie_off[wid];
-                for (int32_t j = lane; j < nt; j += 32) a.tiebuf[off + 1 + o + j] = posL[lo + j];
-            }
-        }
-        __syncthreads();
-    }
-}
-
-// ---------------------------------------------------------------------------
 // stream positions
 // ---------------------------------------------------------------------------
 struct DrawLoad {
@@ -1816,24 +1482,10 @@ __global__ void k_reset_sweep(DevCounters *ctr) {
 // host launcher
 // ---------------------------------------------------------------------------
 constexpr int WARP_CAP = 256;
-constexpr int BLOCK_CAP = 2048;    // table 4096, 256 threads
-constexpr int BLOCK_L_CAP = 8192;  // table 16384, 1024 threads
 
 static inline unsigned cap_grid(int64_t want, int64_t cap) {
     if (want < 1) want = 1;
     return (unsigned)(want < cap ? want : cap);
-}
-
-template <class R, int G>
-static void launch_group(pcd_graph *g, const SweepArgs &a, const R &rule, int bin, const char *name,
-                         cudaStream_t st, int *launches) {
-    const int64_t c = g->bin_off[bin + 1] - g->bin_off[bin];
-    if (c <= 0) return;
-    const int64_t warps = (c + (32 / G) - 1) / (32 / G);
-    k_prop_group<R, G><<<cap_grid((warps + 7) / 8, (int64_t)g->ctx->num_sms * 16), 256, 0, st>>>(
-        a, rule, g->bin_list + g->bin_off[bin], c);
-    ++*launches;
-    prof_mark(g->ctx, name, st);
 }
 
 // Warp per vertex for degrees up to WCAP: shared tables of 8 warps per block.
@@ -1877,7 +1529,6 @@ static void launch_thread(pcd_graph *g, const SweepArgs &a, const R &rule, int b
 
 template <class R>
 static int launch_bins_rule(pcd_graph *g, const SweepArgs &a, const R &rule, cudaStream_t st) {
-    const int sms = g->ctx->num_sms;
     int launches = 0;
     const int32_t *L = g->bin_list;
     int64_t c;
@@ -1897,12 +1548,20 @@ static int launch_bins_rule(pcd_graph *g, const SweepArgs &a, const R &rule, cud
                 launch_warp<R, 128>(g, a, rule, lst, c, st);
             else
                 launch_warp<R, WARP_CAP>(g, a, rule, lst, c, st);
-        } else if (dm <= 512) {
+        } else if (dm <= 512) {  // positions per lane (RPL) fitted to the sub-range's largest degree
             launch_block1<R, 256, 2>(g, a, rule, lst, c, dm, st);
+        } else if (dm <= 768) {
+            launch_block1<R, 256, 3>(g, a, rule, lst, c, dm, st);
         } else if (dm <= 1024) {
             launch_block1<R, 256, 4>(g, a, rule, lst, c, dm, st);
+        } else if (dm <= 1536) {
+            launch_block1<R, 256, 6>(g, a, rule, lst, c, dm, st);
         } else if (dm <= 2048) {
             launch_block1<R, 256, 8>(g, a, rule, lst, c, dm, st);
+        } else if (dm <= 2560) {
+            launch_block1<R, 512, 5>(g, a, rule, lst, c, dm, st);
+        } else if (dm <= 3072) {
+            launch_block1<R, 512, 6>(g, a, rule, lst, c, dm, st);
         } else if (dm <= 4096) {
             launch_block1<R, 512, 8>(g, a, rule, lst, c, dm, st);
         } else {

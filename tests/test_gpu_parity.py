@@ -305,3 +305,37 @@ def test_fp64_recheck_lists_match_oracle(ctx, port, shape):
         assert bad.size == 0, f"trial {trial}: {bad.size} vertices differ, first {bad[:6]}"
     G.free()
     assert rechecked > 0, "no vertex took the FP64 re-evaluation path"
+
+
+def _planted_degree_graph(D, hubs=8, seed=0):
+    """Random base graph (average degree ~10) plus `hubs` vertices with exactly
+    D neighbours each, so the degree sub-range holding D has largest degree D
+    and the kernel variant sized for it runs."""
+    import graphs
+
+    n = max(6000, 2 * D)
+    rng = np.random.default_rng(seed + D)
+    base = rng.integers(0, n, size=(5 * n, 2))
+    extra = [(n + h, int(u)) for h in range(hubs) for u in rng.choice(n, size=D, replace=False)]
+    return graphs.convert_edges(np.concatenate([base, np.array(extra)]))
+
+
+@pytest.mark.parametrize("D", [600, 900, 1200, 1800, 2300, 2900, 3500, 5000, 9000])
+def test_block_variants_by_degree_match_oracle(ctx, port, D):
+    """Each shared-table variant (positions per lane fitted to the sub-range's
+    largest degree) and the hub kernel, on graphs whose largest degrees are
+    planted: Modularity and CPM sweeps against the oracle."""
+    import oracle
+    import pcd
+
+    g = _planted_degree_graph(D)
+    assert int(np.diff(g.indices).max()) == D
+    for metric in ("mod", "cpm-0.05"):
+        G = pcd.Graph.from_csr(ctx, g.indices, g.adj)
+        got = []
+        pcd.run(G, pcd.parse_metric(metric), 0, 1.0, 1, 4, keep_raw=True, callback=got.append)
+        G.free()
+        _, _, want = oracle.run_schedule(port, g.indices, g.adj, metric, 0, 1.0, 1, 4)
+        for a, b in zip(got, want):
+            bad = np.nonzero(a.raw != b.raw)[0]
+            assert bad.size == 0, f"D={D} {metric} sweep {a.it}: {bad.size} differ"
