@@ -25,6 +25,8 @@
 #include <unordered_map>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "pcd.h"
 
 namespace pcd {
@@ -258,12 +260,29 @@ void pcd_server::worker_main() {
         if (ctx) pcd_destroy(ctx);
         return;
     }
+    // small batches run on a high-priority stream: whenever blocks of a long
+    // run's kernels retire, the scheduler starts the small batch's blocks first
+    int lo_prio = 0, hi_prio = 0;
+    cudaStream_t s_hi = nullptr, s_lo = nullptr;
+    if (cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&s_hi, cudaStreamNonBlocking, hi_prio) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&s_lo, cudaStreamNonBlocking, lo_prio) != cudaSuccess) {
+        cudaGetLastError();  // no priorities: every batch stays on the context's own stream
+        if (s_hi) cudaStreamDestroy(s_hi);
+        s_hi = s_lo = nullptr;
+    }
+    cudaStream_t cur = nullptr;
     for (;;) {
         std::vector<std::shared_ptr<Request>> batch;
         int64_t bytes = 0;
         if (!take_batch(batch, bytes)) break;
+        cudaStream_t want = s_hi ? (batch.front()->cls == 0 ? s_hi : s_lo) : nullptr;
+        if (want != cur && pcd_set_stream(ctx, want) == PCD_OK) cur = want;
         run_batch(ctx, batch, bytes);
     }
+    pcd_set_stream(ctx, nullptr);
+    if (s_hi) cudaStreamDestroy(s_hi);
+    if (s_lo) cudaStreamDestroy(s_lo);
     pcd_destroy(ctx);
 }
 
