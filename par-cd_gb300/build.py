@@ -61,7 +61,7 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
         if s.endswith(".cpp"):
             cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "include")
             cmd = ["g++", "-c", s, "-o", o, "-O2", "-fPIC", "-std=c++17", "-pthread", "-ffp-contract=off",
-                   "-fno-fast-math", "-I", os.path.join(HERE, "..", "include"), "-I", cuda_inc]
+                   "-fno-fast-math", "-I", os.path.join(HERE, "..", "include"), "-I", cuda_inc, "-I", CSRC]
         else:
             cmd = [nvcc(), "-c", s, "-o", o] + flags(extra)
         if verbose:

@@ -26,6 +26,10 @@ struct pcd_ctx {
     std::vector<const char *> prof_names;
     size_t prof_used = 0;
     pcd::DevCounters *h_ctr = nullptr;  // pinned copy of a graph's counters (shared by its graphs)
+    // multiplies the resident-block caps of the sweep grids: above 1 the warp,
+    // block and thread classes launch more blocks than fit at once, so blocks
+    // retire (and free SMs for other streams' work) throughout the kernel
+    int32_t grid_scale = 1;
 };
 
 // Per-graph state of a batch: many graphs refined as one disjoint union whose

@@ -1496,7 +1496,8 @@ static void launch_warp(pcd_graph *g, const SweepArgs &a, const R &rule, const i
     cudaFuncSetAttribute(k_prop_warp<R, WCAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_prop_warp<R, WCAP>, 256, smem);
-    k_prop_warp<R, WCAP><<<cap_grid((c + 7) / 8, (int64_t)g->ctx->num_sms * std::max(1, per_sm)), 256, smem, st>>>(
+    k_prop_warp<R, WCAP><<<cap_grid((c + 7) / 8, (int64_t)g->ctx->num_sms * std::max(1, per_sm) * g->ctx->grid_scale),
+                           256, smem, st>>>(
         a, rule, list, c, nullptr);
 }
 
@@ -1512,7 +1513,8 @@ static void launch_block1(pcd_graph *g, const SweepArgs &a, const R &rule, const
     cudaFuncSetAttribute(k_prop_block1<R, BT, RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_prop_block1<R, BT, RPL>, BT, smem);
-    k_prop_block1<R, BT, RPL><<<cap_grid(c, (int64_t)g->ctx->num_sms * std::max(1, per_sm)), BT, smem, st>>>(
+    k_prop_block1<R, BT, RPL><<<cap_grid(c, (int64_t)g->ctx->num_sms * std::max(1, per_sm) * g->ctx->grid_scale), BT,
+                                smem, st>>>(
         a, rule, list, c, cap);
 }
 
@@ -1521,7 +1523,7 @@ static void launch_thread(pcd_graph *g, const SweepArgs &a, const R &rule, int b
                           cudaStream_t st, int *launches) {
     const int64_t c = g->bin_off[bin + 1] - g->bin_off[bin];
     if (c <= 0) return;
-    k_prop_thread<R, MAXD><<<cap_grid((c + 255) / 256, (int64_t)g->ctx->num_sms * 16), 256, 0, st>>>(
+    k_prop_thread<R, MAXD><<<cap_grid((c + 255) / 256, (int64_t)g->ctx->num_sms * 16 * g->ctx->grid_scale), 256, 0, st>>>(
         a, rule, g->bin_list + g->bin_off[bin], c);
     ++*launches;
     prof_mark(g->ctx, name, st);

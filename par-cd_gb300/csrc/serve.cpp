@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include "pcd.h"
+#include "pcd_internal.h"
 
 namespace pcd {
 pcd_status keep_pool_memory(int32_t device, int64_t bytes);  // api.cu
@@ -278,6 +279,7 @@ void pcd_server::worker_main() {
         if (!take_batch(batch, bytes)) break;
         cudaStream_t want = s_hi ? (batch.front()->cls == 0 ? s_hi : s_lo) : nullptr;
         if (want != cur && pcd_set_stream(ctx, want) == PCD_OK) cur = want;
+        ctx->grid_scale = batch.front()->cls == 0 ? 1 : 8;  // long runs release SMs block by block
         run_batch(ctx, batch, bytes);
     }
     pcd_set_stream(ctx, nullptr);
