@@ -189,11 +189,8 @@ pcd_status pcd_init(pcd_ctx **out, int32_t device) {
     pcd_status s = check_cuda(ctx, cudaSetDevice(device), "cudaSetDevice");
     if (s == PCD_OK) s = check_cuda(ctx, cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking),
                                     "cudaStreamCreate");
-    if (s == PCD_OK) s = check_cuda(ctx, cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking), "side stream");
     if (s == PCD_OK)
         s = check_cuda(ctx, cudaMallocHost((void **)&ctx->h_ctr, sizeof(DevCounters)), "cudaMallocHost");
-    if (s == PCD_OK) s = check_cuda(ctx, cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming), "event");
-    if (s == PCD_OK) s = check_cuda(ctx, cudaEventCreateWithFlags(&ctx->join, cudaEventDisableTiming), "event");
     if (s == PCD_OK) {
         ctx->stream = ctx->own_stream;
         int sms = 0;
@@ -203,6 +200,19 @@ pcd_status pcd_init(pcd_ctx **out, int32_t device) {
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
         ctx->smem_optin = (size_t)optin;
         upload_jump_table(ctx->stream);
+        // graphs are loaded and freed stream-ordered: let the device's default
+        // pool keep up to a quarter of the device's memory after frees, so the
+        // next graph reuses mapped memory instead of mapping it again
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+            cudaMemPool_t pool;
+            uint64_t cur = 0;
+            if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess &&
+                cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &cur) == cudaSuccess &&
+                cur < total_b / 4)
+                keep_pool_memory(device, (int64_t)(total_b / 4));
+        }
+        cudaGetLastError();
         s = check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "pcd_init");
     }
     if (s != PCD_OK) {
@@ -236,12 +246,6 @@ pcd_status pcd_destroy(pcd_ctx *ctx) {
     if (!ctx) return PCD_ERR_INVALID_ARGUMENT;
     while (!ctx->graphs.empty()) pcd_graph_free(ctx->graphs.back());
     for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
-    if (ctx->fork) cudaEventDestroy(ctx->fork);
-    if (ctx->join) cudaEventDestroy(ctx->join);
-    if (ctx->side) {
-        cudaStreamSynchronize(ctx->side);
-        cudaStreamDestroy(ctx->side);
-    }
     if (ctx->own_stream) {
         cudaStreamSynchronize(ctx->own_stream);
         cudaStreamDestroy(ctx->own_stream);
@@ -382,6 +386,15 @@ static pcd_status graph_setup(pcd_ctx *ctx, pcd_graph *g) {
     return PCD_OK;
 }
 
+__global__ void k_label_range(const int32_t *__restrict__ labels, int32_t n, int32_t *bad) {
+    int32_t b = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t l = labels[i];
+        b |= (l < -1) | (l >= n);
+    }
+    if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+}
+
 __global__ void k_iota(int32_t *p, int32_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         p[i] = (int32_t)i;
@@ -509,13 +522,19 @@ pcd_status pcd_graph_get_bins(pcd_graph *g, int32_t max_deg[7], int64_t counts[8
 pcd_status pcd_labels_set(pcd_graph *g, const int32_t *labels) {
     if (!g || (!labels && g->n)) return PCD_ERR_INVALID_ARGUMENT;
     pcd_ctx *ctx = g->ctx;
-    for (int32_t v = 0; v < g->n; ++v)
-        if (labels[v] < -1 || labels[v] >= g->n)
-            return set_error(ctx, PCD_ERR_INVALID_ARGUMENT, "label out of range [-1, n)");
     CK(cudaMemcpyAsync(g->labels, labels, sizeof(int32_t) * (size_t)g->n, cudaMemcpyHostToDevice, ctx->stream),
        "labels_set");
-    CK(cudaStreamSynchronize(ctx->stream), "labels_set");
     g->compressed = false;
+    // range check on the device (NEW_LABEL = -1 allowed), reported here
+    int32_t *bad = static_cast<int32_t *>(g->small);
+    CK(cudaMemsetAsync(bad, 0, sizeof(int32_t), ctx->stream), "labels_set");
+    if (g->n > 0)
+        k_label_range<<<std::max(1, std::min<int>((g->n + 255) / 256, ctx->num_sms * 8)), 256, 0, ctx->stream>>>(
+            g->labels, g->n, bad);
+    int32_t h_bad = 0;
+    CK(cudaMemcpyAsync(&h_bad, bad, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream), "labels_set");
+    CK(cudaStreamSynchronize(ctx->stream), "labels_set");
+    if (h_bad) return set_error(ctx, PCD_ERR_INVALID_ARGUMENT, "label out of range [-1, n)");
     return PCD_OK;
 }
 

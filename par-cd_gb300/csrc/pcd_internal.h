@@ -14,8 +14,6 @@ struct pcd_ctx {
     int32_t device = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;  // own_stream or the caller's
-    cudaStream_t side = nullptr;    // hubs run here, concurrently with the other degree classes
-    cudaEvent_t fork = nullptr, join = nullptr;
     int32_t num_sms = 0;
     size_t smem_optin = 0;
     std::string last_error;
