@@ -151,6 +151,43 @@ __global__ void k_stats_warp(const int32_t *__restrict__ indices, const int32_t 
     }
 }
 
+// Block per vertex for rows above 2048 neighbours (the largest rows would
+// otherwise keep one warp busy for the whole pass): 512 threads with four
+// label gathers in flight each, one set of atomics per vertex.
+__global__ void __launch_bounds__(512) k_stats_block(const int32_t *__restrict__ indices,
+                                                     const int32_t *__restrict__ adj,
+                                                     const int32_t *__restrict__ labels,
+                                                     const int32_t *__restrict__ list, int64_t count, int32_t *sizes,
+                                                     int32_t *intv, int32_t *extv, int32_t *vol) {
+    __shared__ int32_t part[16];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int64_t idx = blockIdx.x; idx < count; idx += gridDim.x) {
+        const int32_t v = list[idx];
+        const int32_t l = labels[v];
+        const int32_t b = indices[v], e = indices[v + 1];
+        int32_t di = 0;
+        for (int32_t j0 = b + (int32_t)threadIdx.x; j0 < e; j0 += 4 * 512) {
+            int32_t u[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) u[k] = j0 + k * 512 < e ? adj[j0 + k * 512] : -1;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) di += u[k] >= 0 && labels[u[k]] == l;
+        }
+        di = __reduce_add_sync(FULL, di);
+        if (lane == 0) part[wid] = di;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int32_t t = 0;
+            for (int w = 0; w < 16; ++w) t += part[w];
+            atomicAdd(sizes + l, 1);
+            atomicAdd(intv + l, t);
+            atomicAdd(extv + l, (e - b) - t);
+            atomicAdd(vol + l, e - b);
+        }
+        __syncthreads();
+    }
+}
+
 int launch_stats(pcd_graph *g, cudaStream_t st) {
     int launches = 0;
     size_t bytes = sizeof(int32_t) * (size_t)(g->n > 0 ? g->n : 1);
@@ -165,11 +202,18 @@ int launch_stats(pcd_graph *g, cudaStream_t st) {
                                                            g->intv, g->extv, g->vol);
         ++launches;
     }
-    int64_t nw = g->bin_off[NBINS] - g->bin_off[BIN_WARP];
+    int64_t nw = g->bin_off[BIN_BLOCK_L] - g->bin_off[BIN_WARP];
     if (nw > 0) {
         k_stats_warp<<<grid_for(nw * 32, 256), 256, 0, st>>>(g->indices, g->adj, g->labels,
                                                              g->bin_list + g->bin_off[BIN_WARP], nw, g->sizes,
                                                              g->intv, g->extv, g->vol);
+        ++launches;
+    }
+    int64_t nb = g->bin_off[NBINS] - g->bin_off[BIN_BLOCK_L];
+    if (nb > 0) {
+        const unsigned blocks = (unsigned)std::min<int64_t>(nb, (int64_t)g->ctx->num_sms * 4);
+        k_stats_block<<<blocks, 512, 0, st>>>(g->indices, g->adj, g->labels, g->bin_list + g->bin_off[BIN_BLOCK_L], nb,
+                                             g->sizes, g->intv, g->extv, g->vol);
         ++launches;
     }
     return launches;
