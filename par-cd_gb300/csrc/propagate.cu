@@ -1308,43 +1308,32 @@ struct WalkStep {
 };
 
 // The walk only branches at vertices with ties: a vertex without ties makes
-// one call whether or not it passes the frac test.  Per chunk of 32
-// vertices the warp walks the vertices with ties in order (the calls of the
-// vertices between them are jumped over with the map of k calls, k < 32),
-// then every other lane evaluates its own frac test from the state of the
-// last vertex with ties before it.
+// one call whether or not it passes the frac test, so on the sequential
+// chain it is one LCG step (three steps of the generator folded into one
+// affine map); its frac test is evaluated afterwards, in its own lane, from
+// the state it saw.  A vertex with ties takes the full step (its frac draw,
+// then the jump over its tie draws when it draws).
 __global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gseed, const int32_t *voff, int32_t G,
                                               int32_t f, int32_t n, uint32_t *ndraw, int32_t *skip,
                                               DevCounters *ctr) {
-    __shared__ uint32_t sh[4][5][32];
+    __shared__ uint32_t sh[4][3][32];
     __shared__ uint32_t jA[32], jC[32];
-    __shared__ uint32_t kA[33], kC[33];  // map of k calls, k = 0..32
     if (threadIdx.x < 32) {
         jA[threadIdx.x] = c_jump.a[threadIdx.x];
         jC[threadIdx.x] = c_jump.c[threadIdx.x];
-    }
-    if (threadIdx.x == 0) {
-        uint32_t a = 1u, c = 0u;
-        for (int k = 0; k <= 32; ++k) {
-            kA[k] = a;
-            kC[k] = c;
-            c = WalkStep::A3 * c + WalkStep::C3;
-            a = WalkStep::A3 * a;
-        }
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const uint32_t uf = (uint32_t)f, fhi = uf & 0x7FF00000u;
-    uint32_t *st = sh[wib][0], *sa = sh[wib][1], *sc = sh[wib][2], *xa = sh[wib][3], *pa = sh[wib][4];
+    uint32_t *st = sh[wib][0], *sa = sh[wib][1], *sc = sh[wib][2];
     for (int64_t g = warp; g < G; g += nw) {
         const int32_t v0 = voff ? voff[g] : 0, v1 = voff ? voff[g + 1] : n;
         uint32_t x = voff ? gseed[g] : seed, pos = 0;
         uint32_t t_next = v0 + lane < v1 ? ndraw[v0 + lane] : 0u;
         for (int32_t c0 = v0; c0 < v1; c0 += 32) {
             const int32_t v = c0 + lane;
-            const bool valid = v < v1;
             const uint32_t t = t_next;
             // the next chunk's counts are loaded while this chunk is walked
             t_next = v + 32 < v1 ? ndraw[v + 32] : 0u;
@@ -1360,50 +1349,43 @@ __global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gse
             sa[lane] = ta;
             sc[lane] = tc;
             __syncwarp();
-            const unsigned vm = __ballot_sync(FULL, valid);
-            const unsigned bm = __ballot_sync(FULL, valid && t > 0u);
-            // the vertices with ties, in order (the same steps in every lane)
-            uint32_t xs = x, ps = pos;
-            int prev = -1;
-            for (unsigned rest = bm; rest; rest &= rest - 1) {
-                const int j = __ffs(rest) - 1;
-                const int gap = j - prev - 1;  // vertices without ties in between: one call each
-                xs = kA[gap] * xs + kC[gap];
-                ps += (uint32_t)gap;
-                const bool d = WalkStep::step(xs, uf, fhi, sa[j], sc[j]);
-                ps += d ? 1u + st[j] : 1u;
-                if (lane == j) {
-                    xa[j] = xs;  // the state and position after vertex j
-                    pa[j] = ps;
+            const unsigned bm = __ballot_sync(FULL, v < v1 && t > 0u);
+            const int cnt = min(32, v1 - c0);
+            uint32_t my_x = 0, my_pos = 0;
+            bool my_d = false;
+            if (cnt == 32) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    if (lane == j) my_x = x;
+                    if ((bm >> j) & 1u) {
+                        const bool d = WalkStep::step(x, uf, fhi, sa[j], sc[j]);
+                        pos += d ? 1u + st[j] : 1u;
+                        if (lane == j) my_d = d;
+                    } else {
+                        x = WalkStep::A3 * x + WalkStep::C3;
+                        pos += 1u;
+                    }
+                    if (lane == j) my_pos = pos;
                 }
-                prev = j;
+            } else {
+                for (int j = 0; j < cnt; ++j) {
+                    if (lane == j) my_x = x;
+                    if ((bm >> j) & 1u) {
+                        const bool d = WalkStep::step(x, uf, fhi, sa[j], sc[j]);
+                        pos += d ? 1u + st[j] : 1u;
+                        if (lane == j) my_d = d;
+                    } else {
+                        x = WalkStep::A3 * x + WalkStep::C3;
+                        pos += 1u;
+                    }
+                    if (lane == j) my_pos = pos;
+                }
             }
-            __syncwarp();
-            // every lane: its frac test from the state after the last vertex
-            // with ties before it, k calls later (for a vertex with ties this
-            // repeats the test of the loop above)
-            const bool has_ties = (bm >> lane) & 1u;
-            const unsigned before = bm & lanemask_lt();
-            const int p = before ? 31 - __clz(before) : -1;
-            const uint32_t xb = p >= 0 ? xa[p] : x, pb = p >= 0 ? pa[p] : pos;
-            const int k = lane - p - 1;
-            uint32_t xv = kA[k] * xb + kC[k];
-            const bool dv = WalkStep::step(xv, uf, fhi, sa[lane], sc[lane]);
-            const int32_t my_skip = dv ? 0 : 1;
-            const uint32_t my_pos = has_ties ? pa[lane] : pb + (uint32_t)k + 1u;
-            // the chunk's end: after its last valid vertex
-            const int last = 31 - __clz(vm);
-            const unsigned bl = bm & (last == 31 ? FULL : ((2u << last) - 1u));
-            const int pl = bl ? 31 - __clz(bl) : -1;
-            const int m = last - pl;  // vertices without ties after the last one with ties
-            const uint32_t xe = pl >= 0 ? xa[pl] : x, pe = pl >= 0 ? pa[pl] : pos;
-            x = kA[m] * xe + kC[m];
-            pos = pe + (uint32_t)m;
-            if (valid) {
+            if (v < v1) {
+                if (!((bm >> lane) & 1u)) my_d = WalkStep::step(my_x, uf, fhi, 1u, 0u);  // its frac test
                 ndraw[v] = my_pos;
-                skip[v] = my_skip;
+                skip[v] = my_d ? 0 : 1;
             }
-            __syncwarp();
         }
         if (!voff && lane == 0) ctr->total_draws = pos;
     }
