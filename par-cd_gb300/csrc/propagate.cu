@@ -1308,32 +1308,51 @@ struct WalkStep {
 };
 
 // The walk only branches at vertices with ties: a vertex without ties makes
-// one call whether or not it passes the frac test, so on the sequential
-// chain it is one LCG step (three steps of the generator folded into one
-// affine map); its frac test is evaluated afterwards, in its own lane, from
-// the state it saw.  A vertex with ties takes the full step (its frac draw,
-// then the jump over its tie draws when it draws).
+// one call whether or not it passes the frac test.  Per chunk of 32
+// vertices, two exact ways, picked by how many of them have ties:
+//   few: the vertices with ties are walked in order (the calls of the
+//        vertices between them are jumped over with the map of k calls),
+//        then every lane evaluates its own frac test from the state after
+//        the last vertex with ties before it;
+//   many: the chain runs over all 32 vertices, one LCG step (three steps of
+//        the generator folded into one affine map) for a vertex without
+//        ties, the full step (frac draw, then the jump over its tie draws
+//        when it draws) for one with ties; the frac tests of the vertices
+//        without ties are evaluated afterwards in their own lanes.
+constexpr int WALK_SPARSE = 4;  // at most this many vertices with ties: walk only those
+
 __global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gseed, const int32_t *voff, int32_t G,
                                               int32_t f, int32_t n, uint32_t *ndraw, int32_t *skip,
                                               DevCounters *ctr) {
-    __shared__ uint32_t sh[4][3][32];
+    __shared__ uint32_t sh[4][5][32];
     __shared__ uint32_t jA[32], jC[32];
+    __shared__ uint32_t kA[33], kC[33];  // map of k calls, k = 0..32
     if (threadIdx.x < 32) {
         jA[threadIdx.x] = c_jump.a[threadIdx.x];
         jC[threadIdx.x] = c_jump.c[threadIdx.x];
+    }
+    if (threadIdx.x == 0) {
+        uint32_t a = 1u, c = 0u;
+        for (int k = 0; k <= 32; ++k) {
+            kA[k] = a;
+            kC[k] = c;
+            c = WalkStep::A3 * c + WalkStep::C3;
+            a = WalkStep::A3 * a;
+        }
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const uint32_t uf = (uint32_t)f, fhi = uf & 0x7FF00000u;
-    uint32_t *st = sh[wib][0], *sa = sh[wib][1], *sc = sh[wib][2];
+    uint32_t *st = sh[wib][0], *sa = sh[wib][1], *sc = sh[wib][2], *xa = sh[wib][3], *pa = sh[wib][4];
     for (int64_t g = warp; g < G; g += nw) {
         const int32_t v0 = voff ? voff[g] : 0, v1 = voff ? voff[g + 1] : n;
         uint32_t x = voff ? gseed[g] : seed, pos = 0;
         uint32_t t_next = v0 + lane < v1 ? ndraw[v0 + lane] : 0u;
         for (int32_t c0 = v0; c0 < v1; c0 += 32) {
             const int32_t v = c0 + lane;
+            const bool valid = v < v1;
             const uint32_t t = t_next;
             // the next chunk's counts are loaded while this chunk is walked
             t_next = v + 32 < v1 ? ndraw[v + 32] : 0u;
@@ -1349,11 +1368,45 @@ __global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gse
             sa[lane] = ta;
             sc[lane] = tc;
             __syncwarp();
-            const unsigned bm = __ballot_sync(FULL, v < v1 && t > 0u);
+            const unsigned bm = __ballot_sync(FULL, valid && t > 0u);
+            const bool has_ties = (bm >> lane) & 1u;
             const int cnt = min(32, v1 - c0);
-            uint32_t my_x = 0, my_pos = 0;
+            uint32_t my_x = 0, my_pos = 0;  // the state before its frac draw, its end position
             bool my_d = false;
-            if (cnt == 32) {
+            if (__popc(bm) <= WALK_SPARSE) {
+                uint32_t xs = x, ps = pos;
+                int prev = -1;
+                for (unsigned rest = bm; rest; rest &= rest - 1) {
+                    const int j = __ffs(rest) - 1;
+                    const int gap = j - prev - 1;  // vertices without ties in between: one call each
+                    xs = kA[gap] * xs + kC[gap];
+                    ps += (uint32_t)gap;
+                    const bool d = WalkStep::step(xs, uf, fhi, sa[j], sc[j]);
+                    ps += d ? 1u + st[j] : 1u;
+                    if (lane == j) {
+                        xa[j] = xs;  // the state and position after vertex j
+                        pa[j] = ps;
+                        my_d = d;
+                    }
+                    prev = j;
+                }
+                __syncwarp();
+                const unsigned before = bm & lanemask_lt();
+                const int p = before ? 31 - __clz(before) : -1;
+                const uint32_t xb = p >= 0 ? xa[p] : x, pb = p >= 0 ? pa[p] : pos;
+                const int k = lane - p - 1;
+                my_x = kA[k] * xb + kC[k];
+                my_pos = has_ties ? pa[lane] : pb + (uint32_t)k + 1u;
+                // the chunk's end: after its last vertex
+                const int last = cnt - 1;
+                const unsigned bl = bm & (last == 31 ? FULL : ((2u << last) - 1u));
+                const int pl = bl ? 31 - __clz(bl) : -1;
+                const int m = last - pl;
+                const uint32_t xe = pl >= 0 ? xa[pl] : x, pe = pl >= 0 ? pa[pl] : pos;
+                x = kA[m] * xe + kC[m];
+                pos = pe + (uint32_t)m;
+                __syncwarp();
+            } else if (cnt == 32) {
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
                     if (lane == j) my_x = x;
@@ -1381,8 +1434,8 @@ __global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gse
                     if (lane == j) my_pos = pos;
                 }
             }
-            if (v < v1) {
-                if (!((bm >> lane) & 1u)) my_d = WalkStep::step(my_x, uf, fhi, 1u, 0u);  // its frac test
+            if (valid) {
+                if (!has_ties) my_d = WalkStep::step(my_x, uf, fhi, 1u, 0u);  // its frac test
                 ndraw[v] = my_pos;
                 skip[v] = my_d ? 0 : 1;
             }
