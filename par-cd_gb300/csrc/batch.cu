@@ -348,15 +348,25 @@ pcd_status pcd_batch_run(pcd_graph *g, const pcd_rule *rule, int32_t strategy, d
     if (rule->kind == PCD_RULE_WCC)
         return set_error(ctx, PCD_ERR_UNSUPPORTED, "batched runs start from singletons; WCC needs -i 1");
     cudaStream_t st = ctx->stream;
-    // each graph's seed stream: the reference driver draws n_g values for the
-    // singleton partition, then one per refinement call
+    // each graph's seed stream: the reference driver seeds rand() with 1,
+    // draws n_g values for the singleton partition, then one per refinement
+    // call.  Every graph reads the same stream, so it is drawn once, up to
+    // the largest graph plus the iteration cap: graph g's seed of iteration
+    // it is value n_g + it.
     const int32_t cap = n_iter >= 0 ? std::max(n_iter, 1) : 1000;
-    std::vector<uint32_t> table((size_t)cap * G);
-    for (int32_t gi = 0; gi < G; ++gi) {
+    int32_t max_n = 0;
+    for (int32_t gi = 0; gi < G; ++gi)
+        max_n = std::max(max_n, B->h_voff[(size_t)gi + 1] - B->h_voff[(size_t)gi]);
+    std::vector<uint32_t> stream((size_t)max_n + (size_t)cap);
+    {
         pcd_rand r;
         pcd_rand_seed(&r, 1);
-        pcd_rand_skip(&r, B->h_voff[(size_t)gi + 1] - B->h_voff[(size_t)gi]);
-        for (int32_t it = 0; it < cap; ++it) table[(size_t)it * G + gi] = (uint32_t)pcd_rand_next(&r);
+        for (auto &x : stream) x = (uint32_t)pcd_rand_next(&r);
+    }
+    std::vector<uint32_t> table((size_t)cap * G);
+    for (int32_t gi = 0; gi < G; ++gi) {
+        const size_t ng = (size_t)(B->h_voff[(size_t)gi + 1] - B->h_voff[(size_t)gi]);
+        for (int32_t it = 0; it < cap; ++it) table[(size_t)it * G + gi] = stream[ng + (size_t)it];
     }
     if (B->seed_iters < cap) {
         if (B->seed_table) cudaFreeAsync(B->seed_table, st);
