@@ -406,7 +406,7 @@ pcd_status pcd_batch_run(pcd_graph *g, const pcd_rule *rule, int32_t strategy, d
     cudaGraphExec_t exec = nullptr;
     const int32_t max_it = n_iter >= 0 ? n_iter : cap - 1;
     pcd_status s = PCD_OK;
-    int32_t done_count = 0;
+    int32_t done_count = 0, done_at_bins = 0;
     int32_t *d_count = B->iter + 2;
     for (int32_t it = 0; it <= max_it && s == PCD_OK; ++it) {
         const bool is_prop = strategy == 0 || (strategy == 2 && it % 2 == 0);
@@ -456,9 +456,21 @@ pcd_status pcd_batch_run(pcd_graph *g, const pcd_rule *rule, int32_t strategy, d
             cudaMemcpyAsync(&done_count, d_count, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
             s = check_cuda(ctx, cudaStreamSynchronize(st), "batch iteration");
             if (done_count == G) break;
+            // finished graphs keep their labels: once an eighth more of them have
+            // finished, the degree classes are rebuilt over the others, so the
+            // sweeps and statistics skip them (a captured iteration is re-captured)
+            if (s == PCD_OK && done_count - done_at_bins >= std::max(1, G / 8)) {
+                launch_bins(g, st, true);
+                done_at_bins = done_count;
+                if (exec) {
+                    cudaGraphExecDestroy(exec);
+                    exec = nullptr;
+                }
+            }
         }
     }
     if (exec) cudaGraphExecDestroy(exec);
+    if (done_at_bins > 0) launch_bins(g, st);  // every vertex back in its class
     ctx->prof_on = prof;
     g->compressed = true;
     g->labels_vertex_space = false;

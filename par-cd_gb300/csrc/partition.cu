@@ -406,9 +406,10 @@ struct SubFlag {
     const int32_t *indices;
     BinConfig cfg;
     int32_t bin, lo, hi;
+    const int32_t *vgid, *gdone;  // batch, active graphs only: vertices of finished graphs are left out
     __device__ bool in(int64_t v) const {
         const int32_t d = indices[v + 1] - indices[v];
-        return d > lo && d <= hi && bin_of(d, cfg) == bin;
+        return d > lo && d <= hi && bin_of(d, cfg) == bin && (!gdone || !gdone[vgid[v]]);
     }
     __device__ uint32_t operator()(int64_t v) const { return in(v) ? 1u : 0u; }
 };
@@ -428,11 +429,13 @@ struct SubBounds {
 };
 
 // the largest degree in each sub-range (sizes the shared tables of its launch)
-__global__ void k_sub_maxdeg(const int32_t *__restrict__ indices, int32_t n, SubBounds sb, int32_t *out) {
+__global__ void k_sub_maxdeg(const int32_t *__restrict__ indices, int32_t n, SubBounds sb, int32_t *out,
+                             const int32_t *__restrict__ vgid, const int32_t *__restrict__ gdone) {
     __shared__ int32_t sm[MAX_SUBS];
     if (threadIdx.x < MAX_SUBS) sm[threadIdx.x] = 0;
     __syncthreads();
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        if (gdone && gdone[vgid[v]]) continue;
         const int32_t d = indices[v + 1] - indices[v];
         for (int s = 0; s < sb.count; ++s)
             if (d > sb.lo[s] && d <= sb.hi[s]) {
@@ -447,8 +450,10 @@ __global__ void k_sub_maxdeg(const int32_t *__restrict__ indices, int32_t n, Sub
 // Classes, and inside the warp and block classes sub-ranges at powers of two
 // (warp: 64, 128; block: 512, 1024; large block: 4096), each a stable
 // compaction of the vertices with that degree range.
-int launch_bins(pcd_graph *g, cudaStream_t st) {
+int launch_bins(pcd_graph *g, cudaStream_t st, bool active_only) {
     int launches = 0;
+    const int32_t *vgid = active_only && g->batch ? g->batch->vgid : nullptr;
+    const int32_t *gdone = active_only && g->batch ? g->batch->gdone : nullptr;
     std::vector<pcd_graph::SubRange> subs;
     for (int b = 0; b < NBINS; ++b) {
         const int32_t lo = b == 0 ? -1 : g->bins.max_deg[b - 1];
@@ -473,7 +478,7 @@ int launch_bins(pcd_graph *g, cudaStream_t st) {
     }
     int32_t *d_max = reinterpret_cast<int32_t *>(g->small);
     cudaMemsetAsync(d_max, 0, MAX_SUBS * sizeof(int32_t), st);
-    k_sub_maxdeg<<<grid_for(g->n, 256), 256, 0, st>>>(g->indices, g->n, sb, d_max);
+    k_sub_maxdeg<<<grid_for(g->n, 256), 256, 0, st>>>(g->indices, g->n, sb, d_max, vgid, gdone);
     int32_t h_max[MAX_SUBS] = {0};
     cudaMemcpyAsync(h_max, d_max, MAX_SUBS * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
     ++launches;
@@ -481,7 +486,7 @@ int launch_bins(pcd_graph *g, cudaStream_t st) {
     for (int b = 0; b < NBINS; ++b) g->bin_maxdeg[b] = 0;
     for (size_t s = 0; s < subs.size(); ++s) {
         auto &r = subs[s];
-        const SubFlag f{g->indices, g->bins, r.bin, r.lo, r.hi};
+        const SubFlag f{g->indices, g->bins, r.bin, r.lo, r.hi, vgid, gdone};
         launches += scan_exclusive(f, SubStore{f, g->bin_list + off}, g->n, g->scan, st);
         uint32_t cnt = 0;
         cudaMemcpyAsync(&cnt, g->scan_total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);

@@ -135,7 +135,9 @@ int launch_stats(pcd_graph *g, cudaStream_t st);
 int launch_score(pcd_graph *g, int32_t kind, double lambda, double *d_out, cudaStream_t st);
 int launch_validate(const int32_t *indices, const int32_t *adj, int32_t n, int32_t m,
                     int32_t *d_flag, cudaStream_t st);
-int launch_bins(pcd_graph *g, cudaStream_t st);  // fills bin_list, bin_off, subs (syncs)
+// fills bin_list, bin_off, subs (syncs); active_only (batches): vertices of
+// graphs whose schedule has finished are left out of every class
+int launch_bins(pcd_graph *g, cudaStream_t st, bool active_only = false);
 // Stable LSD radix sort of (uint64 key, uint32 value) pairs on bits [0, bits),
 // 8 bits per pass, ping-ponging between A and B; true if the result is in B.
 // hist: 256 * grid words; sc: scratch for scans of 256 * grid items.

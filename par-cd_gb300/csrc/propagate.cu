@@ -1323,7 +1323,7 @@ constexpr int WALK_SPARSE = 4;  // at most this many vertices with ties: walk on
 
 __global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gseed, const int32_t *voff, int32_t G,
                                               int32_t f, int32_t n, uint32_t *ndraw, int32_t *skip,
-                                              DevCounters *ctr) {
+                                              DevCounters *ctr, const int32_t *gdone) {
     __shared__ uint32_t sh[4][5][32];
     __shared__ uint32_t jA[32], jC[32];
     __shared__ uint32_t kA[33], kC[33];  // map of k calls, k = 0..32
@@ -1347,6 +1347,7 @@ __global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gse
     const uint32_t uf = (uint32_t)f, fhi = uf & 0x7FF00000u;
     uint32_t *st = sh[wib][0], *sa = sh[wib][1], *sc = sh[wib][2], *xa = sh[wib][3], *pa = sh[wib][4];
     for (int64_t g = warp; g < G; g += nw) {
+        if (gdone && gdone[g]) continue;  // a finished graph keeps its labels: nothing to walk
         const int32_t v0 = voff ? voff[g] : 0, v1 = voff ? voff[g + 1] : n;
         uint32_t x = voff ? gseed[g] : seed, pos = 0;
         uint32_t t_next = v0 + lane < v1 ? ndraw[v0 + lane] : 0u;
@@ -1725,7 +1726,7 @@ int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32
     } else {
         const int32_t G = B ? B->G : 1;
         k_walk<<<(unsigned)((G + 3) / 4), 128, 0, st>>>(seed, B ? B->gseed : nullptr, B ? B->voff : nullptr, G, f,
-                                                         g->n, g->ndraw, g->first, g->ctr);
+                                                         g->n, g->ndraw, g->first, g->ctr, B ? B->gdone : nullptr);
         if (B) cudaMemsetAsync(B->gbase, 0, sizeof(uint32_t) * B->G, st);
         skip = g->first;
         ++launches;
