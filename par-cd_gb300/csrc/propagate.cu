@@ -1350,13 +1350,23 @@ __global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gse
         if (gdone && gdone[g]) continue;  // a finished graph keeps its labels: nothing to walk
         const int32_t v0 = voff ? voff[g] : 0, v1 = voff ? voff[g + 1] : n;
         uint32_t x = voff ? gseed[g] : seed, pos = 0;
-        uint32_t t_next = v0 + lane < v1 ? ndraw[v0 + lane] : 0u;
+        // tie counts of the next WQ chunks in flight: each chunk's load is
+        // issued WQ chunks before the chain reaches it (ndraw is overwritten
+        // only at the chunk being walked)
+        constexpr int WQ = 8;
+        uint32_t tq[WQ];
+#pragma unroll
+        for (int q = 0; q < WQ; ++q) {
+            const int32_t u = v0 + 32 * q + lane;
+            tq[q] = u < v1 ? ndraw[u] : 0u;
+        }
         for (int32_t c0 = v0; c0 < v1; c0 += 32) {
             const int32_t v = c0 + lane;
             const bool valid = v < v1;
-            const uint32_t t = t_next;
-            // the next chunk's counts are loaded while this chunk is walked
-            t_next = v + 32 < v1 ? ndraw[v + 32] : 0u;
+            const uint32_t t = tq[0];
+#pragma unroll
+            for (int q = 0; q < WQ - 1; ++q) tq[q] = tq[q + 1];
+            tq[WQ - 1] = v + 32 * WQ < v1 ? ndraw[v + 32 * WQ] : 0u;
             uint32_t ta = 1u, tc = 0u;
 #pragma unroll 1
             for (uint32_t rem = t, i = 0; rem; ++i, rem >>= 1)
