@@ -1305,6 +1305,29 @@ struct WalkStep {
         x = draws ? ta * s3 + tc : s3;
         return draws;
     }
+    // One vertex on the sequential chain, without branches: both outcomes of
+    // the frac test are formed and selected (a vertex without ties has
+    // t = 0 and the identity tie map, so its outcome moves neither the
+    // state nor the position); lane `mine` keeps the state it saw, its end
+    // position and its outcome.
+    __device__ __forceinline__ static void chain(uint32_t &x, uint32_t &pos, uint32_t f, uint32_t fhi, uint32_t ta,
+                                                 uint32_t tc, uint32_t t, bool mine, uint32_t &my_x,
+                                                 uint32_t &my_pos, bool &my_d) {
+        if (mine) my_x = x;
+        const uint32_t s1 = (16u * A1) * x + 16u * C1;
+        const uint32_t s2 = A2 * x + C2;
+        const uint32_t s3 = A3 * x + C3;
+        const uint32_t hi = s1 & 0x7FF00000u;
+        const uint32_t val = hi | ((s2 >> 6) & 0x000FFC00u) | ((s3 >> 16) & 0x3FFu);
+        const bool d = hi != fhi ? hi < fhi : val <= f;
+        const uint32_t xd = ta * s3 + tc;
+        x = d ? xd : s3;
+        pos += d ? 1u + t : 1u;
+        if (mine) {
+            my_pos = pos;
+            my_d = d;
+        }
+    }
 };
 
 // The walk only branches at vertices with ties: a vertex without ties makes
@@ -1384,7 +1407,8 @@ __global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gse
             const int cnt = min(32, v1 - c0);
             uint32_t my_x = 0, my_pos = 0;  // the state before its frac draw, its end position
             bool my_d = false;
-            if (__popc(bm) <= WALK_SPARSE) {
+            const bool sparse = __popc(bm) <= WALK_SPARSE;
+            if (sparse) {
                 uint32_t xs = x, ps = pos;
                 int prev = -1;
                 for (unsigned rest = bm; rest; rest &= rest - 1) {
@@ -1419,34 +1443,14 @@ __global__ void __launch_bounds__(128) k_walk(uint32_t seed, const uint32_t *gse
                 __syncwarp();
             } else if (cnt == 32) {
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    if (lane == j) my_x = x;
-                    if ((bm >> j) & 1u) {
-                        const bool d = WalkStep::step(x, uf, fhi, sa[j], sc[j]);
-                        pos += d ? 1u + st[j] : 1u;
-                        if (lane == j) my_d = d;
-                    } else {
-                        x = WalkStep::A3 * x + WalkStep::C3;
-                        pos += 1u;
-                    }
-                    if (lane == j) my_pos = pos;
-                }
+                for (int j = 0; j < 32; ++j) WalkStep::chain(x, pos, uf, fhi, sa[j], sc[j], st[j], lane == j, my_x,
+                                                             my_pos, my_d);
             } else {
-                for (int j = 0; j < cnt; ++j) {
-                    if (lane == j) my_x = x;
-                    if ((bm >> j) & 1u) {
-                        const bool d = WalkStep::step(x, uf, fhi, sa[j], sc[j]);
-                        pos += d ? 1u + st[j] : 1u;
-                        if (lane == j) my_d = d;
-                    } else {
-                        x = WalkStep::A3 * x + WalkStep::C3;
-                        pos += 1u;
-                    }
-                    if (lane == j) my_pos = pos;
-                }
+                for (int j = 0; j < cnt; ++j)
+                    WalkStep::chain(x, pos, uf, fhi, sa[j], sc[j], st[j], lane == j, my_x, my_pos, my_d);
             }
             if (valid) {
-                if (!has_ties) my_d = WalkStep::step(my_x, uf, fhi, 1u, 0u);  // its frac test
+                if (sparse && !has_ties) my_d = WalkStep::step(my_x, uf, fhi, 1u, 0u);  // its frac test
                 ndraw[v] = my_pos;
                 skip[v] = my_d ? 0 : 1;
             }
