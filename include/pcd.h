@@ -59,7 +59,7 @@ typedef struct pcd_graph pcd_graph;
  * the next synchronising call, or pcd_synchronize). */
 typedef struct pcd_sweep_info {
     int64_t draws;         /* rand_r calls the sweep consumed */
-    int32_t fallback;      /* vertices re-evaluated in FP64 (see DESIGN) */
+    int32_t fallback;      /* vertices re-evaluated in FP64 (the exact integer key could not order them) */
     int32_t resolved;      /* vertices / communities whose tie list was replayed */
     int32_t kernels;       /* kernel launches issued by the call */
     int32_t merge_pairs;   /* contracted (a, b) pairs (merge only) */

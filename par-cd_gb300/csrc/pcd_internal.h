@@ -89,7 +89,8 @@ struct pcd_graph {
     int32_t *fb_scratch = nullptr;
     int64_t fb_slots = 0;    // power of two >= 2 * max_deg
     int32_t fb_blocks = 0;
-    // hub tables: the same layout, one slice per hub block
+    // hub kernel: one slice per hub block (hub_stride(max_deg) ints: packed
+    // keys, labels and (position, label) buckets of the row being refined)
     int32_t *hub_scratch = nullptr;
     int32_t hub_blocks = 0;
     size_t hub_bytes = 0;

@@ -213,7 +213,7 @@ def test_edge_cases(ctx, port):
 
 BIN_LAYOUTS = [
     [4, 8, 16, 32, 256, 2048, 8192],   # default
-    [0, 0, 0, 0, 0, 0, 0],             # everything in HBM-table blocks
+    [0, 0, 0, 0, 0, 0, 0],             # everything in the hub class (parts over per-block slices)
     [0, 0, 0, 0, 0, 0, 8192],          # everything in 1024-thread shared-table blocks
     [0, 0, 0, 0, 0, 2048, 2048],       # 256-thread blocks (+ HBM beyond)
     [0, 0, 0, 0, 256, 256, 256],       # warps (+ HBM beyond)
