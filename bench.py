@@ -115,6 +115,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(dist, x: float, device) -> float:
+    """The job's time is its slowest rank's: max of x over the ranks (x itself
+    without a process group)."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def make_workload(args, device):
     import graphs
 
@@ -660,8 +672,10 @@ def main():
     if world > 1:
         import torch.distributed as dist
 
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        # NCCL between GPUs; gloo where there is no GPU (the reference arm on host cores)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
 
     if args.impl == "reference":
         rc = run_reference_arm(args, rank, world)
@@ -743,10 +757,7 @@ def main():
     sweep_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
     launches = G.info().kernels_total - k_before
     total_ms = sum(sweep_ms)
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(dist, total_ms, dev)
     ms_per_step = total_ms / args.steps
     value = world * m * args.steps / (total_ms / 1e3)
     assert np.array_equal(G.labels, results[last]), "sweep result changed between identical steps"
@@ -798,10 +809,7 @@ def main():
         for _ in range(args.e2e_steps):
             e2e_step()
         sec = time.perf_counter() - t0
-        if dist:
-            t = torch.tensor([sec], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            sec = float(t.item())
+        sec = max_over_ranks(dist, sec, dev)
         e2e = {"value": world * m * args.e2e_steps / sec, "unit": "edges/s",
                "h2d_bytes_per_step": int(4 * (n + 1) + 8 * m + 4 * n), "d2h_bytes_per_step": int(4 * n),
                "ms_per_step": 1000.0 * sec / args.e2e_steps,
