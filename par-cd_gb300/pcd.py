@@ -470,12 +470,13 @@ def compare_communities(g: Graph, a, b) -> float:
     return nmi(g.ctx, a, b, g.n)
 
 
-def compare_communities_file(g: Graph, labels, path: str) -> float:
-    """compare_communities(g, labels, filename) (src/common.cpp:127-160): one
-    ground-truth community per line (vertex ids separated by white space);
-    empty lines and lines starting with '#' are skipped, and a line is read
-    up to its first token that is not an integer.  Vertex ids index
-    labels."""
+def truth_file_pairs(labels, path: str):
+    """The confusion pairs compare_communities(g, labels, filename) builds
+    (src/common.cpp:127-160): one ground-truth community per line (vertex
+    ids separated by white space), numbered from 1; empty lines and lines
+    starting with '#' are skipped, and a line is read up to its first token
+    that is not an integer.  Returns (community, labels[v]) as two int32
+    arrays."""
     lab = _i32(labels)
     comm, va, vb = 0, [], []
     with open(path) as f:
@@ -491,7 +492,14 @@ def compare_communities_file(g: Graph, labels, path: str) -> float:
                     break
                 va.append(comm)
                 vb.append(int(lab[v]))
-    return nmi(g.ctx, np.asarray(va, np.int32), np.asarray(vb, np.int32), g.n)
+    return np.asarray(va, np.int32), np.asarray(vb, np.int32)
+
+
+def compare_communities_file(g: Graph, labels, path: str) -> float:
+    """compare_communities(g, labels, filename) (src/common.cpp:127-160) on
+    the device: the pairs of truth_file_pairs, normalised by g.n."""
+    a, b = truth_file_pairs(labels, path)
+    return nmi(g.ctx, a, b, g.n)
 
 
 @dataclass

@@ -198,3 +198,23 @@ def test_oracle_extras_golden(port, golden_extras):
         port.count_triangles()
         assert port.clustering().tolist() == rec["clustering"], name
         assert port.find_connected().tolist() == rec["components"], name
+
+
+def test_truth_file_pairs_match_reference_reader(port, golden_extras, tmp_path):
+    """The host reader of ground-truth files (pcd.truth_file_pairs) builds the
+    reference's confusion pairs: with the restatement's NMI (bit-identical to
+    the reference's for the same pairs) it reproduces the value the
+    reference computed from the same file (comment and empty lines
+    included)."""
+    import make_golden_extras as mge
+    import pcd
+
+    g = golden_graph("sbm10k")
+    port.load(g.indices, g.adj)
+    port.count_triangles()
+    clus = port.clustering()
+    path = tmp_path / "truth.txt"
+    mge.truth_file(g, 100, str(path))
+    a, b = pcd.truth_file_pairs(clus, str(path))
+    assert a.min() == 1 and a.shape[0] == g.n
+    assert repr(port.nmi(a, b, g.n)) == golden_extras["graphs"]["sbm10k"]["nmi_truth_file_clustering"]
