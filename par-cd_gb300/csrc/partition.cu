@@ -363,69 +363,34 @@ int launch_score(pcd_graph *g, int32_t kind, double lambda, double *d_out, cudaS
 // CSR validation: offsets monotone and spanning [0, 2m], neighbours in range,
 // rows strictly increasing (sorted, no duplicates), no loops.
 // ---------------------------------------------------------------------------
-// CSR validation, flags: 1 span (indices[0] != 0 or indices[n] != 2m),
-// 2 offsets (a row outside [0, 2m] or ending before it starts), 4 rows (a
-// neighbour out of range, a loop, or a row not strictly increasing).
-// Offsets are checked vertex-parallel; entries edge-parallel in chunks of
-// VALIDATE_CHUNK, each thread finding the row of its first entry by binary
-// search, so a long row is spread over many threads.
-constexpr int VALIDATE_CHUNK = 16;
-
-__global__ void k_validate_rows(const int32_t *__restrict__ indices, int32_t n, int32_t m, int32_t *flag) {
-    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (tid == 0 && (indices[0] != 0 || (int64_t)indices[n] != 2 * (int64_t)m)) atomicOr(flag, 1);
-    int32_t bad = 0;
-    for (int64_t v = tid; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t b = indices[v], e = indices[v + 1];
-        bad |= b > e || b < 0 || (int64_t)e > 2 * (int64_t)m;
+__global__ void k_validate(const int32_t *__restrict__ indices, const int32_t *__restrict__ adj, int32_t n,
+                           int32_t m, int32_t *flag) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    if (warp == 0 && lane == 0) {
+        if (indices[0] != 0 || (int64_t)indices[n] != 2 * (int64_t)m) atomicOr(flag, 1);
     }
-    if (__any_sync(FULL, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 2);
-}
-
-__global__ void k_validate_entries(const int32_t *__restrict__ indices, const int32_t *__restrict__ adj,
-                                   int32_t n, int64_t nnz, int32_t *flag) {
-    const int64_t nchunks = (nnz + VALIDATE_CHUNK - 1) / VALIDATE_CHUNK;
-    int32_t bad = 0;
-    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nchunks;
-         c += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t j0 = c * VALIDATE_CHUNK, j1 = min(nnz, j0 + VALIDATE_CHUNK);
-        // row of entry j0: the last v with indices[v] <= j0 (offsets that are
-        // not monotone are flagged by k_validate_rows; every read here stays
-        // inside indices[0..n] whatever they hold)
-        int32_t lo = 0, hi = n - 1;
-        while (lo < hi) {
-            const int32_t mid = lo + (hi - lo + 1) / 2;
-            if (indices[mid] <= j0)
-                lo = mid;
-            else
-                hi = mid - 1;
+    for (int64_t v = warp; v < n; v += nwarps) {
+        int32_t b = indices[v], e = indices[v + 1];
+        if (b > e || b < 0 || (int64_t)e > 2 * (int64_t)m) {
+            if (lane == 0) atomicOr(flag, 2);
+            continue;
         }
-        int32_t v = lo;
-        int64_t vb = indices[v], ve = indices[v + 1];
-        int32_t prev = j0 > vb && j0 > 0 ? adj[j0 - 1] : INT32_MIN;
-        for (int64_t j = j0; j < j1; ++j) {
-            while (j >= ve && v < n - 1) {
-                ++v;
-                vb = ve;
-                ve = indices[v + 1];
-                prev = INT32_MIN;
-            }
-            const int32_t u = adj[j];
-            bad |= u < 0 || u >= n || u == v || (j > vb && prev >= u);
-            prev = u;
+        bool bad = false;
+        for (int32_t j = b + lane; j < e; j += 32) {
+            int32_t u = adj[j];
+            bad |= (u < 0 || u >= n || u == (int32_t)v);
+            if (j > b) bad |= (adj[j - 1] >= u);
         }
+        if (__any_sync(FULL, bad) && lane == 0) atomicOr(flag, 4);
     }
-    if (__any_sync(FULL, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 4);
 }
 
 int launch_validate(const int32_t *indices, const int32_t *adj, int32_t n, int32_t m, int32_t *d_flag,
                     cudaStream_t st) {
-    k_validate_rows<<<grid_for(n, 256), 256, 0, st>>>(indices, n, m, d_flag);
-    const int64_t nnz = 2 * (int64_t)m;
-    if (nnz > 0 && n > 0)
-        k_validate_entries<<<grid_for((nnz + VALIDATE_CHUNK - 1) / VALIDATE_CHUNK, 256), 256, 0, st>>>(
-            indices, adj, n, nnz, d_flag);
-    return 2;
+    k_validate<<<grid_for((int64_t)n * 32, 256), 256, 0, st>>>(indices, adj, n, m, d_flag);
+    return 1;
 }
 
 // ---------------------------------------------------------------------------
