@@ -474,10 +474,14 @@ def truth_file_pairs(labels, path: str):
     """The confusion pairs compare_communities(g, labels, filename) builds
     (src/common.cpp:127-160): one ground-truth community per line (vertex
     ids separated by white space), numbered from 1; empty lines and lines
-    starting with '#' are skipped, and a line is read up to its first token
-    that is not an integer.  Returns (community, labels[v]) as two int32
-    arrays."""
+    starting with '#' are skipped, and a line is read as a stream of integers
+    until the first character that cannot continue one (so "12abc" yields 12
+    and ends the line).  Vertex ids must lie in [0, n).  Returns (community,
+    labels[v]) as two int32 arrays."""
+    import re
+
     lab = _i32(labels)
+    num = re.compile(r"[+-]?\d+")
     comm, va, vb = 0, [], []
     with open(path) as f:
         for line in f:
@@ -486,12 +490,13 @@ def truth_file_pairs(labels, path: str):
                 continue
             comm += 1
             for tok in line.split():
-                try:
-                    v = int(tok)
-                except ValueError:
+                mt = num.match(tok)
+                if not mt:
                     break
                 va.append(comm)
-                vb.append(int(lab[v]))
+                vb.append(int(lab[int(mt.group())]))
+                if mt.end() < len(tok):
+                    break
     return np.asarray(va, np.int32), np.asarray(vb, np.int32)
 
 

@@ -218,3 +218,27 @@ def test_truth_file_pairs_match_reference_reader(port, golden_extras, tmp_path):
     a, b = pcd.truth_file_pairs(clus, str(path))
     assert a.min() == 1 and a.shape[0] == g.n
     assert repr(port.nmi(a, b, g.n)) == golden_extras["graphs"]["sbm10k"]["nmi_truth_file_clustering"]
+
+
+@needs_ref
+def test_truth_file_reader_edge_cases_match_reference(port, tmp_path):
+    """Lines the reference's stream reader treats specially: comments, empty
+    lines, a token with trailing characters (read up to them, then the line
+    ends), a non-numeric token, repeated vertices, a leading '+'."""
+    import graphs
+    import oracle
+    import pcd
+
+    ref = oracle.Reference("strict")
+    g = graphs.convert_edges(graphs.sbm(10, 30, 0.3, 0.01, seed=8))
+    ref.load(g.indices, g.adj)
+    port.load(g.indices, g.adj)
+    rng = np.random.default_rng(3)
+    labels = rng.integers(0, 7, g.n).astype(np.int32)
+    text = ("# header\n\n0 1 2 3\n4 5 6x 7 8\n9 10 abc 11\n+12 13 13 14\n\n# c\n"
+            + " ".join(str(v) for v in range(15, g.n)) + "\n20 21\t22\n")
+    path = tmp_path / "truth.txt"
+    path.write_text(text)
+    a, b = pcd.truth_file_pairs(labels, str(path))
+    want = ref.nmi_file(labels, str(path))
+    assert repr(port.nmi(a, b, g.n)) == repr(want)
