@@ -210,18 +210,17 @@ int main(int argc, char **argv) {
     pcd_rand_seed(&rnd, 1);
     std::cout << "creating initial partitioning..." << std::endl;
     timer.start();
-    std::vector<int32_t> tri;
     if (initial == 1 || rule.kind == PCD_RULE_WCC) {
         timer.start();
-        tri.resize((size_t)n);
-        CHECK(pcd_triangles(g, tri.data(), nullptr, nullptr));
+        CHECK(pcd_triangles(g, nullptr, nullptr, nullptr));
         std::cout << "count triangles: " << timer.end() << std::endl;
     }
-    if (initial == 0)
+    if (initial == 0) {
         CHECK(pcd_singleton_partition(&rnd, n, labels.data()));
-    else
-        CHECK(pcd_clustering_partition(n, hg.indices.data(), hg.adj.data(), tri.data(), labels.data()));
-    CHECK(pcd_labels_set(g, labels.data()));
+        CHECK(pcd_labels_set(g, labels.data()));
+    } else {
+        CHECK(pcd_clustering_partition_device(g, nullptr));  // create_clustering_partition's labels
+    }
     const double time_initial = timer.end();
 
     double prev_score = 0.0, score = 0.0;
