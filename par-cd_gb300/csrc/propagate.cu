@@ -283,7 +283,6 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
     constexpr int TS = 2 * WCAP;
     extern __shared__ int32_t smem[];
     using Key = typename R::Key;
-    using E = Elem<Key>;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     unsigned char *wbase = reinterpret_cast<unsigned char *>(smem) + wid * warp_bytes<WCAP>();
     int32_t *keys = reinterpret_cast<int32_t *>(wbase);
