@@ -242,3 +242,32 @@ def test_truth_file_reader_edge_cases_match_reference(port, tmp_path):
     a, b = pcd.truth_file_pairs(labels, str(path))
     want = ref.nmi_file(labels, str(path))
     assert repr(port.nmi(a, b, g.n)) == repr(want)
+
+
+@needs_ref
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_extras_side_by_side_with_reference(port, seed):
+    """Start partition, components and NMI of the restatement against the
+    reference's own objects on seeded graphs with several components."""
+    import graphs
+    import oracle
+
+    ref = oracle.Reference("strict")
+    rng = np.random.default_rng(seed)
+    parts, off = [], 0
+    for k in range(4):
+        e = np.asarray(graphs.rmat(9 + k % 2, 6, 0.57, 0.19, 0.19, seed=100 * seed + k), np.int64)
+        parts.append(e + off)
+        off += 1 << (9 + k % 2)
+    g = graphs.convert_edges(np.concatenate(parts))
+    ref.load(g.indices, g.adj)
+    port.load(g.indices, g.adj)
+    ref.count_triangles()
+    port.count_triangles()
+    assert np.array_equal(port.clustering(), ref.clustering())
+    comp = ref.find_connected()
+    assert np.array_equal(port.find_connected(), comp)
+    a = rng.integers(0, 50, g.n).astype(np.int32)
+    b = (a + rng.integers(0, 3, g.n)).astype(np.int32) % 40
+    for x, y in ((a, b), (a, comp), (comp, comp)):
+        assert repr(port.nmi(x, y)) == repr(ref.nmi(x, y))
