@@ -71,7 +71,10 @@ const char *pcd_status_string(pcd_status s);
 const char *pcd_last_error(const pcd_ctx *ctx);
 
 /* cuda_init (src/framework-cuda.cu:59-73, declared src/framework-cuda.cuh:14).
- * Selects `device`, creates the context's stream, uploads constant tables. */
+ * Selects `device`, creates the context's stream, uploads constant tables,
+ * and lets the device's default memory pool keep up to a quarter of the
+ * device's memory after frees (graphs are allocated stream-ordered from it;
+ * kept memory makes the next load cheap; trim the pool to return it). */
 pcd_status pcd_init(pcd_ctx **ctx, int32_t device);
 /* cuda_deinit (src/framework-cuda.cu:75-78).  Frees every graph of the ctx. */
 pcd_status pcd_destroy(pcd_ctx *ctx);
