@@ -1,4 +1,4 @@
-"""ctypes front-ends for the CPU checkers of the refine / merge / score path.
+"""ctypes front-ends for the CPU oracles of the refine / merge / score path.
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
 bench.py's CPU-baseline leg; never by the product.

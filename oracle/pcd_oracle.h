@@ -1,6 +1,6 @@
 /* CPU restatement of the reference's refine / merge / score path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker the GPU path is
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle the GPU path is
  * compared against (tests/, __graft_entry__.smoke) and the timed CPU baseline
  * (bench.py's cpu_baseline leg and its reference arm).  The product never
  * links, loads or calls it.

@@ -1,5 +1,5 @@
 """Shared test setup: import paths, the `gpu` marker, seeded graphs and the
-checkers (oracle/ is test infrastructure; only tests, smoke() and bench.py's
+oracles (oracle/ is test infrastructure; only tests, smoke() and bench.py's
 CPU-baseline leg use it)."""
 import os
 import sys
