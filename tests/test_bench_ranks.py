@@ -1,4 +1,6 @@
-"""CPU: the multi-rank path of bench.py with the gloo backend (world size 2).
+"""CPU: bench.py's host-side rules -- the multi-rank path with the gloo
+backend (world size 2), the reference schedule's seeds and the per-class
+algorithmic bytes.
 
 The sweep has no exchange step, so ranks run independent replicas; what the
 ranks share is the timing rule (the job's time is the slowest rank's) and
@@ -63,3 +65,39 @@ def test_reference_arm_two_ranks_prints_one_line():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["value"] == d["value"] and d["cpu_baseline"]["kind"] in ("port", "reference")
+
+
+def test_schedule_seeds_are_the_reference_drivers():
+    """The bench replays the reference schedule's sweeps: the seed of sweep i
+    is the (n + i + 1)-th value of glibc rand() after srand(1) (the singleton
+    partition draws n first, src/framework.cpp:14-24; each refinement draws
+    one, src/refinement.cpp:123-124)."""
+    import ctypes
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    libc = ctypes.CDLL("libc.so.6")
+    libc.rand.restype = ctypes.c_int
+    for n in (0, 1, 1000, 123457):
+        libc.srand(ctypes.c_uint(1))
+        for _ in range(n):
+            libc.rand()
+        assert bench.schedule_seeds(n, 5) == [libc.rand() for _ in range(5)]
+
+
+def test_bins_bytes_sum_to_the_sweep_formula():
+    """Per-class algorithmic bytes (8 per endpoint + 12 per vertex) add up to
+    the sweep's 16m + 12n (+4 for the last row offset, counted once)."""
+    import numpy as np
+
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "par-cd_gb300"))
+    import bench
+    import graphs
+
+    g = graphs.convert_edges(graphs.rmat(12, 16, 0.57, 0.19, 0.19, seed=2))
+    bb = bench.bins_bytes(g.indices)
+    assert sum(bb.values()) + 4 == 16 * g.m + 12 * g.n + 4
+    assert set(bb) == {"sweep.g4", "sweep.g8", "sweep.g16", "sweep.g32", "sweep.warp", "sweep.block",
+                       "sweep.block_l", "sweep.hub"}
