@@ -88,3 +88,30 @@ def test_host_initial_partitions_match_oracle(port):
         st = pcd.LIB.pcd_clustering_partition(g.n, pcd._ptr(g.indices), pcd._ptr(g.adj), pcd._ptr(tri), pcd._ptr(lab))
         assert st == 0
         assert np.array_equal(lab, port.clustering())
+
+
+def declared_arity():
+    """Parameter count of every function declared in include/pcd.h."""
+    text = open(os.path.join(ROOT, "include", "pcd.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(pcd_[a-z_]+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S):
+        params = m.group(2).strip()
+        out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_python_bindings_match_the_header():
+    """Every function pcd.py binds takes as many arguments as the header
+    declares (a wrong count would pass garbage through ctypes)."""
+    import pcd
+
+    arity = declared_arity()
+    bound = [n for n in dir(pcd.LIB) if n.startswith("pcd_")]
+    assert len(bound) >= 20
+    for name in bound:
+        f = getattr(pcd.LIB, name)
+        if f.argtypes is None:
+            continue
+        assert name in arity, f"{name} is bound but not declared"
+        assert len(f.argtypes) == arity[name], (name, len(f.argtypes), arity[name])
