@@ -140,13 +140,14 @@ def make_workload(args, device):
     return ind, adj
 
 
-def bins_bytes(ind):
+def bins_bytes(ind, bounds=(4, 8, 16, 32, 256, 2048, 8192)):
     """Algorithmic bytes per vertex class: 8 deg + 12 (row offsets, adjacency,
-    neighbour-label gathers, own label read, new label write)."""
+    neighbour-label gathers, own label read, new label write); `bounds` are
+    the classes' upper degrees (the graph's degree classes)."""
     import numpy as np
 
     deg = np.diff(ind.astype(np.int64))
-    edges = [0, 4, 8, 16, 32, 256, 2048, 8192, 1 << 62]
+    edges = [0] + [int(x) for x in bounds] + [1 << 62]
     names = ["sweep.g4", "sweep.g8", "sweep.g16", "sweep.g32", "sweep.warp", "sweep.block", "sweep.block_l",
              "sweep.hub"]
     out = {}
@@ -192,12 +193,46 @@ def cpu_sweeps(ind, adj, seeds, threads, steps, budget_s):
     return m * len(times) / sec, len(times), sec
 
 
-def schedule_seeds(n, count):
-    import pcd
+def schedule_seeds(ind, adj, count):
+    """The rand_r seeds of the schedule's first `count` refinement calls: the
+    reference's glibc rand() stream (seed 1) after create_singleton_partition's
+    n draws.  Drawn through the oracle's restatement of rand(), so the
+    reference arm maps no library of the product."""
+    import oracle
 
-    r = pcd.GlibcRand()
-    r.skip(n)
-    return [r() for _ in range(count)]
+    port = oracle.Port()
+    port.load(ind, adj)
+    port.singleton()
+    return [port.rand() for _ in range(count)]
+
+
+def oracle_sweep_parity(ind, adj, starts, seeds, gpu_out, budget_s):
+    """Bit-exact check of the timed sweeps: the oracle's single-threaded
+    PropagationRefinement::refine (the reference's -p 1 schedule) from each
+    sweep's start partition with its seed, against the GPU's labels of the
+    same sweep.  The sweeps run side by side on host threads (the oracle's C
+    call releases the interpreter lock).  Returns a dict for the JSON line."""
+    import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+
+    import oracle
+
+    port = oracle.Port()
+    port.load(ind, adj)
+    t0 = time.time()
+
+    def one(j):
+        st = port.stats(starts[j])
+        want = port.refine_prop(0, 0.0, starts[j], 1.0, seed=seeds[j], threads=1, st=st)
+        return j, int(np.count_nonzero(want != gpu_out[j]))
+
+    with ThreadPoolExecutor(max(1, min(len(starts), os.cpu_count() or 1))) as ex:
+        res = list(ex.map(one, range(len(starts))))
+    diff = {j: d for j, d in res}
+    return {"sweeps_checked": len(res), "bit_exact": all(d == 0 for d in diff.values()),
+            "labels_differing": [diff[j] for j in range(len(res))],
+            "oracle": "single-threaded C restatement of PropagationRefinement::refine (-p 1 schedule)",
+            "seconds": round(time.time() - t0, 1)}
 
 
 def run_reference_arm(args, rank, world):
@@ -209,7 +244,7 @@ def run_reference_arm(args, rank, world):
     ind, adj = make_workload(args, dev)
     n = ind.shape[0] - 1
     m = adj.shape[0] // 2
-    seeds = schedule_seeds(n, args.sweeps)
+    seeds = schedule_seeds(ind, adj, args.sweeps)
     threads = os.cpu_count() or 1
     if args.warmup:
         cpu_sweeps(ind, adj, seeds[:1], threads, 1, 60.0)
@@ -232,7 +267,9 @@ def run_reference_arm(args, rank, world):
         "cpu_baseline": {"value": value, "unit": "edges/s", "cores": threads, "kind": "port",
                          "sample": f"{k} propagation sweeps (the schedule's first {args.sweeps}, cycled) of the "
                                    f"workload graph by the oracle's OpenMP restatement of "
-                                   f"PropagationRefinement::refine on {threads} host threads, {sec:.1f}s"},
+                                   f"PropagationRefinement::refine on {threads} host threads (-p {threads}), "
+                                   f"{sec:.1f}s; the restatement is pinned bit-exact to the reference's own "
+                                   f"objects at -p 1 (the reference's objects are not built on this host)"},
         "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -622,6 +659,153 @@ def served_leg(args, dev):
     return out
 
 
+def timed_sweeps(G, rule, start, seed, reps, stream):
+    """CUDA-event times (ms) of `reps` propagation sweeps (frac 1.0), each
+    from the device labels `start` with rand_r seed `seed`; the compress and
+    statistics of the start partition run before each timed sweep."""
+    import torch
+
+    import pcd
+
+    sweep = pcd.PropagationRefinement(1.0)
+    ms = []
+    for _ in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            G.set_labels_device(start.data_ptr())
+            G.compress(sync=False)
+            e0.record(stream)
+            sweep.refine(G, rule, seed)
+            e1.record(stream)
+        stream.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return ms
+
+
+def powerlaw_leg(args, dev):
+    """The power-law planted-community workload (8 M vertices, degree exponent
+    2.5 in [8, 5000], community sizes exponent 1.5 in [20, 20000], mu 0.3,
+    seed 3), generated on the device.  CPM(0.01) from singletons and WCC from
+    the triangle-based start partition (-i 1), each through the driver loop
+    with -s 2 (propagation, then merge).  Timed on the GPU: the first
+    propagation sweep of each (CUDA events, repeated), the triangle count, the
+    start partition and the whole schedule.  Checked on the host afterwards
+    against the oracle's -p 1 schedule: every sweep's labels bit-exact, the
+    contracted weights (a, b, w) of the final partition exact, the
+    triangle counts exact, scores within 1e-12 (or the reference's own
+    summation error bound)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import numpy as np
+    import torch
+
+    import graphs
+    import oracle
+    import pcd
+
+    t0 = time.time()
+    ind, adj, _, _ = graphs.powerlaw_torch(args.pl_n, 2.5, 8, 5000, 1.5, 20, 20000, 0.3, seed=3, device=dev)
+    torch.cuda.empty_cache()
+    n, m = ind.shape[0] - 1, adj.shape[0] // 2
+    log(f"[bench] power-law: n={n} m={m} ({time.time() - t0:.1f}s)")
+    stream = torch.cuda.Stream(device=dev)
+    ctx = pcd.Context(0)
+    ctx.set_stream(stream.cuda_stream)
+    out = {"workload": f"power-law planted communities n={args.pl_n} (degree exp 2.5 in [8, 5000], community exp "
+                       f"1.5 in [20, 20000], mu 0.3, seed 3, device generator), degree-sorted",
+           "n": int(n), "m": int(m), "max_degree": int(np.diff(ind).max())}
+    gpu = {}
+    for metric, init, iters in (("cpm-0.01", 0, args.pl_iters), ("wcc", 1, args.pl_wcc_iters)):
+        rule = pcd.parse_metric(metric)
+        G = pcd.Graph.from_csr(ctx, ind, adj)
+        rec = {}
+        if init == 1:
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            G.count_triangles()
+            rec["triangles_ms"] = 1000 * (time.perf_counter() - t)
+            t = time.perf_counter()
+            pcd.create_clustering_partition_device(G)
+            rec["start_partition_ms"] = 1000 * (time.perf_counter() - t)
+        else:
+            G.labels = pcd.create_singleton_partition(G, pcd.GlibcRand(1))
+        G.compress()
+        start = torch.empty(n, dtype=torch.int32, device=dev)
+        G.get_labels_device(start.data_ptr())
+        seed1 = pcd.GlibcRand(1)
+        if init == 0:
+            seed1.skip(n)
+        seed = seed1()
+        ms = timed_sweeps(G, rule, start, seed, args.pl_reps + 1, stream)[1:]
+        rec["sweep1_ms"] = statistics.median(ms)
+        rec["sweep1_edges_per_s"] = m / (rec["sweep1_ms"] / 1e3)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        res = pcd.run(G, rule, 2, 1.0, 1, iters, 0.0, init, keep_raw=True, initial_on_device=True)
+        rec["schedule_s"] = time.perf_counter() - t
+        rec["schedule"] = f"-m {metric} -s 2 -f 1.0 -n {iters} -i {init}"
+        rec["score"] = res.score
+        rec["k"] = res.k
+        a, b, w = G.contract()
+        tri = G.count_triangles()[:2] if init == 1 else None
+        G.free()
+        gpu[metric] = (rec, res, (a, b, w), tri)
+        log(f"[bench] power-law {metric}: sweep 1 {rec['sweep1_ms']:.2f} ms, schedule {rec['schedule_s']:.2f} s")
+    ctx.close()
+    # the oracle checks, the two metrics side by side on host threads
+    threads = os.cpu_count() or 1
+
+    def check(metric, init, iters):
+        rec, res, (a, b, w), tri = gpu[metric]
+        port = oracle.Port()
+        t = time.time()
+        lab, score, sweeps = oracle.run_schedule(port, ind, adj, metric, 2, 1.0, 1, iters, 0.0, init,
+                                                 aux_threads=max(1, threads - 2))
+        diff = [int(np.count_nonzero(x.raw != y.raw)) for x, y in zip(res.log, sweeps)]
+        st = port.stats(lab)
+        ca, cb, cw = port.contract(lab, st)
+        from_tol = abs(res.score - score) <= (1e-12 * abs(score) if metric == "wcc" else
+                                              score_bound(metric, score, st, m))
+        chk = {"sweeps_checked": len(diff), "labels_differing": diff,
+               "bit_exact": len(res.log) == len(sweeps) and all(d == 0 for d in diff)
+                            and np.array_equal(res.labels, lab),
+               "contracted_pairs": int(len(ca)),
+               "contracted_weights_exact": bool(np.array_equal(a, ca) and np.array_equal(b, cb)
+                                                and np.array_equal(w, cw)),
+               "score": res.score, "oracle_score": score, "score_within_tolerance": bool(from_tol),
+               "oracle_seconds": round(time.time() - t, 1)}
+        if tri is not None:
+            chk["triangles_exact"] = bool(np.array_equal(tri[0], port.tri) and np.array_equal(tri[1], port.tri_deg))
+        return metric, chk
+
+    with ThreadPoolExecutor(2) as ex:
+        checks = dict(ex.map(lambda c: check(*c), (("cpm-0.01", 0, args.pl_iters), ("wcc", 1, args.pl_wcc_iters))))
+    for metric in gpu:
+        out[metric] = gpu[metric][0] | {"parity": checks[metric]}
+    log(f"[bench] power-law: {json.dumps(out)}")
+    return out
+
+
+def score_bound(metric, want, st, m):
+    """1e-12 relative, or the reference's sequential FP64 sum's own rounding
+    bound ((k + 3) 2^-53 sum |terms|) where larger (Modularity / CPM)."""
+    import numpy as np
+
+    import oracle
+
+    rule, lam = oracle.parse_rule(metric)
+    s = st.sizes.astype(np.float64)
+    iv = st.int_volume.astype(np.float64)
+    ev = st.ext_volume.astype(np.float64)
+    if rule == 0:
+        x = (iv + ev) / (2.0 * m)
+        mag = float(np.sum(iv / (2.0 * m) + x * x))
+    else:
+        mag = float(np.sum(np.abs(iv) + lam * s * np.maximum(s - 1, 0))) / (2.0 * m)
+    return max(1e-12 * abs(want), (len(s) + 3) * 2.0 ** -53 * mag)
+
+
 def workload_config(args, n, m):
     return {
         "workload": f"rmat-s{args.scale}-ef{args.edge_factor} (a,b,c,d)=(.57,.19,.19,.05) seed 2, degree-sorted; "
@@ -646,6 +830,7 @@ def main():
     ap.add_argument("--sweeps", type=int, default=5, help="cycle through the first S sweeps of the schedule")
     ap.add_argument("--bins", default="", help="degree classes, 7 comma-separated bounds (default: library's)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of the timed sweeps")
     ap.add_argument("--batch-graphs", type=int, default=4096, help="0: skip the many-graph workload")
     ap.add_argument("--batch-reps", type=int, default=2)
     ap.add_argument("--batch-plain-stride", type=int, default=8)
@@ -657,6 +842,10 @@ def main():
     ap.add_argument("--convert", type=int, default=1, help="0: skip the converter timing")
     ap.add_argument("--extras", type=int, default=1,
                     help="0: skip the components / NMI / initial-partition timings")
+    ap.add_argument("--pl-n", type=int, default=8_000_000, help="power-law workload vertices (0: skip)")
+    ap.add_argument("--pl-iters", type=int, default=4, help="CPM schedule iterations on the power-law graph")
+    ap.add_argument("--pl-wcc-iters", type=int, default=2, help="WCC schedule iterations on the power-law graph")
+    ap.add_argument("--pl-reps", type=int, default=5, help="timed repetitions of each first sweep")
     ap.add_argument("--serve-requests", type=int, default=600, help="0: skip the served workload")
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[200.0, 2000.0])
     ap.add_argument("--serve-workers", type=int, default=4)
@@ -707,7 +896,7 @@ def main():
     sweep = pcd.PropagationRefinement(1.0)
     # The reference schedule (-s 0, frac 1.0): the start partition and rand_r
     # seed of each of its first S sweeps, kept on the device.
-    seeds = schedule_seeds(n, args.sweeps)  # after create_singleton_partition's n draws
+    seeds = schedule_seeds(ind, adj, args.sweeps)  # after create_singleton_partition's n draws
     starts = []
     G.set_labels_device(torch.arange(n, dtype=torch.int32, device=dev).data_ptr())
     for i in range(args.sweeps):
@@ -736,7 +925,7 @@ def main():
     for i in range(max(3, args.warmup, args.sweeps)):
         j = step(i)
         stream.synchronize()
-        results[j] = G.labels  # each sweep's result, for a self-consistency check below
+        results[j] = G.labels  # each sweep's result: checked against the oracle below
 
     k_before = G.info().kernels_total
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -768,11 +957,14 @@ def main():
     phases = {}
     for nm, ms in ctx.profile_read():  # a class may run as several launches (degree sub-ranges)
         phases[nm] = phases.get(nm, 0.0) + ms
+    hub_parts = [nm for nm in phases if nm.startswith("sweep.hub_")]
+    if hub_parts:  # the hub class runs as consecutive launches on one stream
+        phases["sweep.hub"] = sum(phases[nm] for nm in hub_parts)
     ctx.profile(False)
     info = G.info()
     bins_now = G.get_bins()
     peak, peak_kind = load_peaks()
-    bb = bins_bytes(ind)
+    bb = bins_bytes(ind, bins_now[0])
     sweep_phases = {nm: ms for nm, ms in phases.items() if nm.startswith("sweep.")}
     dom = max(((nm, ms) for nm, ms in sweep_phases.items() if nm in bb), key=lambda x: x[1])
     dom_gbs = bb[dom[0]] / (dom[1] / 1e3) / 1e9
@@ -832,10 +1024,21 @@ def main():
         torch.cuda.empty_cache()
         extras = extras_leg(args, dev, ind, adj)
 
+    powerlaw = None
+    if args.pl_n > 0:
+        torch.cuda.empty_cache()
+        powerlaw = powerlaw_leg(args, dev)
+
     served = None
     if args.serve_requests > 0:
         torch.cuda.empty_cache()
         served = served_leg(args, dev)
+
+    parity = None
+    if rank == 0 and not args.no_parity:
+        h_starts = [x.cpu().numpy() for x in starts]
+        parity = oracle_sweep_parity(ind, adj, h_starts, seeds, results, 600.0)
+        log(f"[bench] parity: {json.dumps(parity)}")
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -867,9 +1070,11 @@ def main():
                          "sweep_achieved": sweep_bytes / (ms_per_step / 1e3) / 1e9,
                          "sweep_frac": sweep_bytes / (ms_per_step / 1e3) / 1e9 / peak},
             "cpu_baseline": cpu,
+            "parity": parity,
             "e2e": e2e,
             "batched": batched,
             "served": served,
+            "powerlaw": powerlaw,
             "convert": converted,
             "extras": extras,
             "gpu_launches": int(launches),

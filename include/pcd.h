@@ -82,6 +82,12 @@ pcd_status pcd_destroy(pcd_ctx *ctx);
  * NULL restores the context's own stream. */
 pcd_status pcd_set_stream(pcd_ctx *ctx, void *cuda_stream);
 pcd_status pcd_synchronize(pcd_ctx *ctx);
+/* No counterpart in the reference (its sweep is one kernel sequence).  on = 1:
+ * the degree classes of a refine sweep run concurrently on side streams
+ * forked from the context's stream and joined before the sweep continues
+ * (they read only the old labels and write disjoint outputs, so results are
+ * the same); on = 0 (default): one after another on the context's stream. */
+pcd_status pcd_set_class_streams(pcd_ctx *ctx, int32_t on);
 
 /* cuda_transfer_graph (src/framework-cuda.cu:89-133) with Graph::read's
  * semantics (src/graph.cpp:40-105): n vertices, m undirected edges,
@@ -308,9 +314,12 @@ pcd_status pcd_serve_stop(pcd_server *s);
  * Scratch is a fixed file-scope device array sized for PCD_NOALLOC_MAX_LABELS
  * labels (about 8 MiB per GPU, held until the process exits); larger n is
  * rejected with PCD_ERR_INVALID_ARGUMENT.  The first call on a device, with
- * that device current, looks up the array's address; make that first call
- * before any stream capture.  Calls share the array: calls that overlap on the
- * GPU race.  Asynchronous on `cuda_stream` (NULL = legacy default stream). */
+ * that device current, looks up the array's address (again after a
+ * cudaDeviceReset); make that first call before any stream capture.  Calls
+ * share the array: calls that overlap on the GPU race.  A CUDA error already
+ * pending on the calling thread is left pending and returned as PCD_ERR_CUDA
+ * with nothing launched.  Asynchronous on `cuda_stream` (NULL = legacy
+ * default stream). */
 #define PCD_NOALLOC_MAX_LABELS (1 << 20)
 pcd_status pcd_compress_labels_noalloc(const int32_t *d_labels_in, int32_t n, int32_t *d_labels_out,
                                        int32_t *d_num_labels, void *cuda_stream);

@@ -96,7 +96,7 @@ class Port:
         L.pcdo_rand_r.restype = C.c_int32
         L.pcdo_compress_labels.restype = C.c_int32
         L.pcdo_collect_statistics.restype = C.c_int32
-        for f in ("pcdo_calculate", "pcdo_score_join", "pcdo_score_leave", "pcdo_score_merge"):
+        for f in ("pcdo_calculate", "pcdo_calculate_mt", "pcdo_score_join", "pcdo_score_leave", "pcdo_score_merge"):
             getattr(L, f).restype = C.c_double
         L.pcdo_contract.restype = C.c_int64
         self.rand = GlibcRand(L, 1)
@@ -131,12 +131,18 @@ class Port:
     def srand(self, seed: int = 1):
         self.rand = GlibcRand(self.lib, seed)
 
-    def count_triangles(self):
+    def count_triangles(self, threads: int = 1):
+        """Graph::count_triangles (graph.cpp:107-175); threads > 1 runs the edge
+        loop on OpenMP threads with identical results."""
         tri = np.zeros(self.n, np.int32)
         td = np.zeros(self.n, np.int32)
         cc = C.c_double()
-        self.lib.pcdo_count_triangles(C.byref(self._g), tri.ctypes.data_as(C.c_void_p),
-                                      td.ctypes.data_as(C.c_void_p), C.byref(cc))
+        if threads > 1:
+            self.lib.pcdo_count_triangles_mt(C.byref(self._g), tri.ctypes.data_as(C.c_void_p),
+                                             td.ctypes.data_as(C.c_void_p), C.byref(cc), C.c_int32(threads))
+        else:
+            self.lib.pcdo_count_triangles(C.byref(self._g), tri.ctypes.data_as(C.c_void_p),
+                                          td.ctypes.data_as(C.c_void_p), C.byref(cc))
         self.tri, self.tri_deg, self.cc = tri, td, cc.value
         self._mk_graph()
         return tri, td, cc.value
@@ -192,10 +198,15 @@ class Port:
         p.ext_volume = st.ext_volume.ctypes.data
         return p
 
-    def score(self, rule, lam, labels, st: Stats | None = None) -> float:
+    def score(self, rule, lam, labels, st: Stats | None = None, threads: int = 1) -> float:
+        """Rule::calculate; threads > 1 runs WCC's intersections on OpenMP
+        threads with an identical value."""
         lab = np.ascontiguousarray(labels, dtype=np.int32)
         st = st or self.stats(lab)
         p = self._part(lab, st)
+        if threads > 1:
+            return float(self.lib.pcdo_calculate_mt(rule, C.c_double(lam), C.byref(self._g), C.byref(p),
+                                                    C.c_int32(threads)))
         return float(self.lib.pcdo_calculate(rule, C.c_double(lam), C.byref(self._g), C.byref(p)))
 
     def gain(self, kind, rule, lam, labels, a, b, k, st: Stats | None = None) -> float:
@@ -402,16 +413,20 @@ class Sweep:
 
 
 def run_schedule(be, indices, adj, metric="mod", strategy=0, frac=1.0, rounds=1, n_iter=10,
-                 threshold=0.0, initial=0, threads=1, callback=None):
+                 threshold=0.0, initial=0, threads=1, callback=None, aux_threads=1):
     """The reference driver loop (src/main.cpp:187-266) on back-end `be`.
 
+    `threads` is the refinements' thread count (the reference's -p: it changes
+    the rand_r streams); `aux_threads` > 1 runs the port's triangle count and
+    WCC score on OpenMP threads, which leaves every result unchanged.
     Returns (final compressed labels, final score, list[Sweep]).
     """
     rule, lam = parse_rule(metric)
     be.load(indices, adj)
     be.srand(1)
+    aux = {"threads": aux_threads} if aux_threads > 1 and isinstance(be, Port) else {}
     if initial == 1 or rule == 2:
-        be.count_triangles()
+        be.count_triangles(**aux)
     labels = be.singleton() if initial == 0 else be.clustering()
     prev = 0.0
     it = 0
@@ -419,7 +434,7 @@ def run_schedule(be, indices, adj, metric="mod", strategy=0, frac=1.0, rounds=1,
     while True:
         labels, k = be.compress(labels)
         st = be.stats(labels)
-        score = be.score(rule, lam, labels, st)
+        score = be.score(rule, lam, labels, st, **aux)
         done = (it >= n_iter) if n_iter != -1 else (prev > 0 and score > 0 and score / prev - 1 <= threshold)
         if done:
             break

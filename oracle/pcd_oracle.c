@@ -380,6 +380,41 @@ void pcdo_count_triangles(const pcdo_graph *g, int32_t *tri, int32_t *tri_deg, d
     *cc_out = cc;
 }
 
+/* The same counts with the edge loop on `threads` OpenMP threads: integer
+ * sums (atomic adds) do not depend on the order, and the clustering
+ * coefficient is still summed in vertex order, so the results are identical
+ * to pcdo_count_triangles'. */
+void pcdo_count_triangles_mt(const pcdo_graph *g, int32_t *tri, int32_t *tri_deg, double *cc_out,
+                             int32_t threads) {
+    int32_t n = g->n;
+    if (threads < 1) threads = 1;
+    for (int32_t v = 0; v < n; v++) tri[v] = tri_deg[v] = 0;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 64)
+    for (int32_t v = 0; v < n; v++) {
+        for (int32_t e = g->indices[v]; e < g->indices[v + 1]; e++) {
+            int32_t u = g->adj[e];
+            if (u >= v) continue;
+            int32_t c = intersect_count(g, v, u, NULL, 0);
+            if (c > 0) {
+#pragma omp atomic
+                tri[v] += c;
+#pragma omp atomic
+                tri[u] += c;
+#pragma omp atomic
+                tri_deg[v]++;
+#pragma omp atomic
+                tri_deg[u]++;
+            }
+        }
+    }
+    double cc = 0;
+    for (int32_t v = 0; v < n; v++) {
+        int32_t t = tri[v], deg = degree(g, v);
+        if (deg > 1) cc += (t / (deg * (deg - 1.0))) / n;
+    }
+    *cc_out = cc;
+}
+
 /* ------------------------------------------------------------------------ */
 /* rules.cpp                                                                 */
 /* ------------------------------------------------------------------------ */
@@ -544,6 +579,69 @@ double pcdo_calculate(int32_t rule, double lambda, const pcdo_graph *g, const pc
                     it[v] += cnt;
                     it[u] += cnt;
                     itd[v]++;
+                    itd[u]++;
+                }
+            }
+        }
+        double score = 0.0;
+        for (int32_t v = 0; v < n; v++) {
+            int32_t size = p->sizes[labels[v]];
+            int32_t t = g->tri[v], dt = g->tri_deg[v], ti = it[v], dti = itd[v];
+            if (t > 0) {
+                double a = ti / (double)t;
+                double b = dt / (double)(size - 1 + dt - dti);
+                score += (a * b) / n;
+            }
+        }
+        free(it);
+        free(itd);
+        return score;
+    }
+}
+
+/* pcdo_calculate with WCC's intra-community intersections on `threads` OpenMP
+ * threads (atomic integer adds); every FP64 sum keeps pcdo_calculate's order,
+ * so the value is identical. */
+double pcdo_calculate_mt(int32_t rule, double lambda, const pcdo_graph *g, const pcdo_partition *p,
+                         int32_t threads) {
+    if (threads < 1) threads = 1;
+    int32_t c = p->num_labels;
+    if (rule == PCDO_MODULARITY) {
+        int32_t m = g->m;
+        double mod = 0.0;
+        for (int32_t i = 0; i < c; i++) {
+            double actual = p->int_volume[i] / (2.0 * m);
+            double x = (p->int_volume[i] + p->ext_volume[i]) / (2.0 * m);
+            double expect = x * x;
+            mod += actual - expect;
+        }
+        return mod;
+    } else if (rule == PCDO_CPM) {
+        double score = 0.0;
+        for (int32_t i = 0; i < c; i++)
+            score += p->int_volume[i] - lambda * p->sizes[i] * (p->sizes[i] - 1);
+        return score / (double)(2 * g->m);
+    } else {
+        int32_t n = g->n;
+        const int32_t *labels = p->labels;
+        int32_t *it = (int32_t *)calloc(n ? n : 1, sizeof(int32_t));
+        int32_t *itd = (int32_t *)calloc(n ? n : 1, sizeof(int32_t));
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 64)
+        for (int32_t v = 0; v < n; v++) {
+            int32_t l = labels[v];
+            for (int32_t e = g->indices[v]; e < g->indices[v + 1]; e++) {
+                int32_t u = g->adj[e];
+                if (u >= v) break;
+                if (labels[u] != l) continue;
+                int32_t cnt = intersect_count(g, v, u, labels, l);
+                if (cnt > 0) {
+#pragma omp atomic
+                    it[v] += cnt;
+#pragma omp atomic
+                    it[u] += cnt;
+#pragma omp atomic
+                    itd[v]++;
+#pragma omp atomic
                     itd[u]++;
                 }
             }

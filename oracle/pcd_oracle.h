@@ -65,9 +65,14 @@ int32_t pcdo_collect_statistics(const pcdo_graph *g, const int32_t *labels, int3
 
 /* graph.cpp */
 void pcdo_count_triangles(const pcdo_graph *g, int32_t *tri, int32_t *tri_deg, double *cc);
+/* the same results with the edge loop on `threads` OpenMP threads */
+void pcdo_count_triangles_mt(const pcdo_graph *g, int32_t *tri, int32_t *tri_deg, double *cc, int32_t threads);
 
 /* rules.cpp */
 double pcdo_calculate(int32_t rule, double lambda, const pcdo_graph *g, const pcdo_partition *p);
+/* the same value with WCC's intersections on `threads` OpenMP threads */
+double pcdo_calculate_mt(int32_t rule, double lambda, const pcdo_graph *g, const pcdo_partition *p,
+                         int32_t threads);
 double pcdo_score_join(int32_t rule, double lambda, const pcdo_graph *g, const pcdo_partition *p,
                        int32_t v, int32_t c, int32_t k);
 double pcdo_score_leave(int32_t rule, double lambda, const pcdo_graph *g, const pcdo_partition *p,

@@ -46,27 +46,84 @@ __global__ void k_degree_max(const int32_t *indices, int32_t n, int32_t *out) {
     if ((threadIdx.x & 31) == 0) atomicMax(out, mx);
 }
 
-static void prof_record(pcd_ctx *ctx, const char *name, cudaStream_t st) {
+// one more event of the pool recorded on st; returns its index (-1 on failure)
+static int32_t prof_record(pcd_ctx *ctx, cudaStream_t st) {
     if (ctx->prof_used == ctx->prof_pool.size()) {
         cudaEvent_t e;
-        if (cudaEventCreate(&e) != cudaSuccess) return;
+        if (cudaEventCreate(&e) != cudaSuccess) return -1;
         ctx->prof_pool.push_back(e);
-        ctx->prof_names.push_back(nullptr);
     }
-    ctx->prof_names[ctx->prof_used] = name;
     cudaEventRecord(ctx->prof_pool[ctx->prof_used], st);
-    ++ctx->prof_used;
+    return (int32_t)ctx->prof_used++;
+}
+
+static int32_t &prof_last_of(pcd_ctx *ctx, cudaStream_t st) {
+    for (auto &p : ctx->prof_last)
+        if (p.first == st) return p.second;
+    ctx->prof_last.emplace_back(st, -1);
+    return ctx->prof_last.back().second;
 }
 
 void prof_begin(pcd_ctx *ctx, cudaStream_t st) {
     if (!ctx->prof_on) return;
     ctx->prof_used = 0;
-    prof_record(ctx, "begin", st);
+    ctx->prof_spans.clear();
+    ctx->prof_last.clear();
+    prof_last_of(ctx, st) = prof_record(ctx, st);
 }
 
 void prof_mark(pcd_ctx *ctx, const char *name, cudaStream_t st) {
     if (!ctx->prof_on || ctx->prof_used == 0) return;
-    prof_record(ctx, name, st);
+    int32_t &last = prof_last_of(ctx, st);
+    const int32_t e = prof_record(ctx, st);
+    if (last >= 0 && e >= 0) ctx->prof_spans.push_back({name, last, e});
+    last = e;
+}
+
+void prof_fork(pcd_ctx *ctx, cudaStream_t side) {
+    if (!ctx->prof_on || ctx->prof_used == 0) return;
+    prof_last_of(ctx, side) = prof_record(ctx, side);
+}
+
+pcd_status side_fork(pcd_ctx *ctx, int k, cudaStream_t *out) {
+    if (k > pcd_ctx::kSide) k = pcd_ctx::kSide;
+    int prio = 0;
+    if (cudaStreamGetPriority(ctx->stream, &prio) != cudaSuccess) prio = 0;
+    if (!ctx->ev_fork) {
+        if (cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess)
+            return check_cuda(ctx, cudaGetLastError(), "side streams");
+        for (auto &e : ctx->ev_join)
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+                return check_cuda(ctx, cudaGetLastError(), "side streams");
+    }
+    if (!ctx->side[0] || prio != ctx->side_prio) {
+        for (auto &s : ctx->side) {
+            if (s) {
+                cudaStreamSynchronize(s);
+                cudaStreamDestroy(s);
+            }
+            s = nullptr;
+        }
+        for (auto &s : ctx->side)
+            if (cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio) != cudaSuccess)
+                return check_cuda(ctx, cudaGetLastError(), "side streams");
+        ctx->side_prio = prio;
+    }
+    cudaEventRecord(ctx->ev_fork, ctx->stream);
+    for (int i = 0; i < k; ++i) {
+        cudaStreamWaitEvent(ctx->side[i], ctx->ev_fork, 0);
+        prof_fork(ctx, ctx->side[i]);
+        out[i] = ctx->side[i];
+    }
+    return PCD_OK;
+}
+
+void side_join(pcd_ctx *ctx, int k) {
+    if (k > pcd_ctx::kSide) k = pcd_ctx::kSide;
+    for (int i = 0; i < k; ++i) {
+        cudaEventRecord(ctx->ev_join[i], ctx->side[i]);
+        cudaStreamWaitEvent(ctx->stream, ctx->ev_join[i], 0);
+    }
 }
 
 }  // namespace pcd
@@ -233,7 +290,7 @@ pcd_status pcd_graph_free(pcd_graph *g) {
     cudaStream_t fs = ctx ? ctx->stream : nullptr;
     for (void *p : g->allocs)
         if (p) cudaFreeAsync(p, fs);
-    if (g->hub_scratch) cudaFreeAsync(g->hub_scratch, fs);
+    hub_release(g, fs);
     if (g->merge_buf) cudaFreeAsync(g->merge_buf, fs);
     if (g->batch && g->batch->seed_table) cudaFreeAsync(g->batch->seed_table, fs);
     delete g->batch;
@@ -246,6 +303,14 @@ pcd_status pcd_destroy(pcd_ctx *ctx) {
     if (!ctx) return PCD_ERR_INVALID_ARGUMENT;
     while (!ctx->graphs.empty()) pcd_graph_free(ctx->graphs.back());
     for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
+    for (auto &sd : ctx->side)
+        if (sd) {
+            cudaStreamSynchronize(sd);
+            cudaStreamDestroy(sd);
+        }
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    for (auto &e : ctx->ev_join)
+        if (e) cudaEventDestroy(e);
     if (ctx->own_stream) {
         cudaStreamSynchronize(ctx->own_stream);
         cudaStreamDestroy(ctx->own_stream);
@@ -262,6 +327,12 @@ pcd_status pcd_set_stream(pcd_ctx *ctx, void *stream) {
     return PCD_OK;
 }
 
+pcd_status pcd_set_class_streams(pcd_ctx *ctx, int32_t on) {
+    if (!ctx || !ctx->stream) return PCD_ERR_INVALID_ARGUMENT;
+    ctx->class_streams = on != 0;
+    return PCD_OK;
+}
+
 pcd_status pcd_profile_enable(pcd_ctx *ctx, int32_t on) {
     if (!ctx) return PCD_ERR_INVALID_ARGUMENT;
     ctx->prof_on = on != 0;
@@ -272,11 +343,13 @@ pcd_status pcd_profile_enable(pcd_ctx *ctx, int32_t on) {
 int32_t pcd_profile_read(pcd_ctx *ctx, const char **names, double *ms, int32_t cap) {
     if (!ctx || !ctx->stream) return -1;
     if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return -1;
-    const int32_t nph = ctx->prof_used > 0 ? (int32_t)ctx->prof_used - 1 : 0;
+    const int32_t nph = (int32_t)ctx->prof_spans.size();
     for (int32_t i = 0; i < nph && i < cap; ++i) {
+        const auto &sp = ctx->prof_spans[(size_t)i];
         float t = 0.f;
-        cudaEventElapsedTime(&t, ctx->prof_pool[i], ctx->prof_pool[i + 1]);
-        if (names) names[i] = ctx->prof_names[i + 1];
+        cudaEventSynchronize(ctx->prof_pool[(size_t)sp.ev1]);
+        cudaEventElapsedTime(&t, ctx->prof_pool[(size_t)sp.ev0], ctx->prof_pool[(size_t)sp.ev1]);
+        if (names) names[i] = sp.name;
         if (ms) ms[i] = t;
     }
     return nph;
@@ -285,32 +358,6 @@ int32_t pcd_profile_read(pcd_ctx *ctx, const char **names, double *ms, int32_t c
 pcd_status pcd_synchronize(pcd_ctx *ctx) {
     if (!ctx || !ctx->stream) return PCD_ERR_INVALID_ARGUMENT;
     CK(cudaStreamSynchronize(ctx->stream), "pcd_synchronize");
-    return PCD_OK;
-}
-
-// Hub slices: per block, a packed key and a label for every position of the
-// largest row; as many blocks as there are hub vertices (at most one per SM);
-// grown when the degree classes change.  No initial contents are needed.
-static pcd_status ensure_hub_scratch(pcd_graph *g) {
-    pcd_ctx *ctx = g->ctx;
-    const int64_t hubs = g->bin_off[NBINS] - g->bin_off[BIN_HUB];
-    const int32_t want = (int32_t)std::min<int64_t>(ctx->num_sms, hubs);
-    if (want <= g->hub_blocks) return PCD_OK;
-    const int64_t stride = hub_stride(g->max_deg);
-    cudaStream_t st = ctx->stream;
-    CK(cudaStreamSynchronize(st), "hub scratch");
-    if (g->hub_scratch) {
-        cudaFreeAsync(g->hub_scratch, st);
-        g->dev_bytes -= g->hub_bytes;
-    }
-    g->hub_scratch = nullptr;
-    g->hub_blocks = 0;
-    g->hub_bytes = 0;
-    const size_t bytes = sizeof(int32_t) * (size_t)(stride * want);
-    CK(cudaMallocAsync((void **)&g->hub_scratch, bytes, st), "hub scratch");
-    g->hub_blocks = want;
-    g->hub_bytes = bytes;
-    g->dev_bytes += bytes;
     return PCD_OK;
 }
 
@@ -378,7 +425,7 @@ static pcd_status graph_setup(pcd_ctx *ctx, pcd_graph *g) {
     // degree bins, then the hub slices (the same tables plus labels and counts by position)
     g->bins = BinConfig{{4, 8, 16, 32, 256, 2048, 8192}};
     if (n > 0) launch_bins(g, st);
-    TRY(ensure_hub_scratch(g));
+    TRY(hub_layout(g, st));
     // initial labels: singletons 0..n-1 (already compressed)
     g->k = g->n;
     g->compressed = false;
@@ -430,7 +477,7 @@ static pcd_status load_common(pcd_ctx *ctx, int32_t n, int32_t m, const int32_t 
         cudaStreamSynchronize(ctx->stream);
         for (void *p : g->allocs)
             if (p) cudaFreeAsync(p, ctx->stream);
-        if (g->hub_scratch) cudaFreeAsync(g->hub_scratch, ctx->stream);
+        hub_release(g, ctx->stream);
         delete g;
         return s;
     }
@@ -467,7 +514,7 @@ pcd_status pcd_graph_device_bytes(pcd_graph *g, int64_t *bytes) {
 // Upper bound of what pcd_batch_load + pcd_batch_run (or pcd_load_csr and the
 // phase calls, num_graphs = 1) hold on the device at their peak, from sizes
 // the caller knows before loading.  Mirrors the allocations of graph_setup,
-// ensure_hub_scratch, batch_setup, the batch staging copies, the seed table
+// hub_layout, batch_setup, the batch staging copies, the seed table
 // of pcd_batch_run (iteration cap) and the merge buffers.
 pcd_status pcd_estimate_device_bytes(int32_t n, int64_t nnz, int32_t max_deg, int64_t num_hubs, int32_t num_graphs,
                                      int32_t iteration_cap, int32_t merges, int32_t num_sms, int64_t *bytes) {
@@ -484,7 +531,10 @@ pcd_status pcd_estimate_device_bytes(int32_t n, int64_t nnz, int32_t max_deg, in
     while (slots < 2 * (int64_t)std::max(max_deg, 1)) slots <<= 1;
     const int64_t fb_stride = 3 * slots + max_deg;
     b += 4 * fb_stride * std::min<int64_t>(8, std::max<int64_t>(1, (1ll << 29) / (4 * fb_stride)));
-    b += 4 * hub_stride(max_deg) * std::min<int64_t>(num_sms, num_hubs);
+    // hub arrays: every hub position (at most min(nnz, hubs * max_deg)) plus
+    // each hub's padding to whole chunks, and the per-chunk / per-hub entries
+    const int64_t hub_pos = std::min<int64_t>(e, num_hubs * (int64_t)std::max(max_deg, 1)) + num_hubs * HUB_CHUNK;
+    b += HUB_BYTES_PER_POS * hub_pos + HUB_BYTES_PER_CHUNK * (hub_pos / HUB_CHUNK + 1) + 12 * (num_hubs + 1);
     // batch state, the staging copies of a batch load, the seed table of a run
     b += 8 * nn + 8 * (G + 1) + 52 * G + 64;
     b += 4 * (nn + 1) + 4 * e + 8 + 4 * (G + 1) + 4 * nn;
@@ -506,7 +556,7 @@ pcd_status pcd_graph_set_bins(pcd_graph *g, const int32_t max_deg[7]) {
     CK(cudaStreamSynchronize(ctx->stream), "set_bins");
     for (int i = 0; i < 7; ++i) g->bins.max_deg[i] = max_deg[i];
     if (g->n > 0) launch_bins(g, ctx->stream);
-    TRY(ensure_hub_scratch(g));
+    TRY(hub_layout(g, ctx->stream));
     return check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "set_bins");
 }
 

@@ -315,6 +315,8 @@ static pcd_status batch_step(pcd_graph *g, const pcd_rule *rule, bool merge, dou
     g->labels_vertex_space = false;
     CK(cudaMemcpyAsync(g->batch->gseed, seeds, sizeof(uint32_t) * g->batch->G, cudaMemcpyHostToDevice, ctx->stream),
        "seeds");
+    // a single step refines or merges every graph of the batch
+    CK(cudaMemsetAsync(g->batch->gdone, 0, sizeof(int32_t) * g->batch->G, ctx->stream), "batch step");
     if (merge)
         TRY(run_merge(g, rule->kind, rule->lambda, rounds, 0, ctx->stream, &launches));
     else
@@ -461,6 +463,7 @@ pcd_status pcd_batch_run(pcd_graph *g, const pcd_rule *rule, int32_t strategy, d
             // sweeps and statistics skip them (a captured iteration is re-captured)
             if (s == PCD_OK && done_count - done_at_bins >= std::max(1, G / 8)) {
                 launch_bins(g, st, true);
+                s = hub_layout(g, st);
                 done_at_bins = done_count;
                 if (exec) {
                     cudaGraphExecDestroy(exec);
@@ -470,7 +473,16 @@ pcd_status pcd_batch_run(pcd_graph *g, const pcd_rule *rule, int32_t strategy, d
         }
     }
     if (exec) cudaGraphExecDestroy(exec);
-    if (done_at_bins > 0) launch_bins(g, st);  // every vertex back in its class
+    if (done_at_bins > 0) {
+        // every vertex back in its class; the last statistics pass skipped the
+        // graphs that had left the classes, so recompute them for all graphs
+        launch_bins(g, st);
+        const pcd_status hs = hub_layout(g, st);
+        if (s == PCD_OK) s = hs;
+        launch_stats(g, st);
+    }
+    // graphs are "done" only inside a run: later single steps refine every graph
+    cudaMemsetAsync(B->gdone, 0, sizeof(int32_t) * G, st);
     ctx->prof_on = prof;
     g->compressed = true;
     g->labels_vertex_space = false;

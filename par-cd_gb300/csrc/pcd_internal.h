@@ -18,11 +18,26 @@ struct pcd_ctx {
     size_t smem_optin = 0;
     std::string last_error;
     std::vector<pcd_graph *> graphs;
-    // profiling: (phase name, event recorded at the END of that phase)
+    // profiling: spans (name, start event, end event), each on one stream;
+    // a span starts where the previous mark on the same stream ended
     bool prof_on = false;
     std::vector<cudaEvent_t> prof_pool;
-    std::vector<const char *> prof_names;
     size_t prof_used = 0;
+    struct ProfSpan {
+        const char *name;
+        int32_t ev0, ev1;
+    };
+    std::vector<ProfSpan> prof_spans;
+    std::vector<std::pair<cudaStream_t, int32_t>> prof_last;  // stream -> its last event
+    // side streams on which the sweep's degree classes run concurrently
+    // (created on first use with the priority of `stream`), and the
+    // fork/join events between them and `stream`
+    static constexpr int kSide = 3;
+    bool class_streams = false;  // pcd_set_class_streams
+    cudaStream_t side[kSide] = {nullptr, nullptr, nullptr};
+    int32_t side_prio = 0;
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_join[kSide] = {nullptr, nullptr, nullptr};
     pcd::DevCounters *h_ctr = nullptr;  // pinned copy of a graph's counters (shared by its graphs)
     // multiplies the resident-block caps of the sweep grids: above 1 the warp,
     // block and thread classes launch more blocks than fit at once, so blocks
@@ -89,10 +104,20 @@ struct pcd_graph {
     int32_t *fb_scratch = nullptr;
     int64_t fb_slots = 0;    // power of two >= 2 * max_deg
     int32_t fb_blocks = 0;
-    // hub kernel: one slice per hub block (hub_stride(max_deg) ints: packed
-    // keys, labels and (position, label) buckets of the row being refined)
-    int32_t *hub_scratch = nullptr;
-    int32_t hub_blocks = 0;
+    // hub class (rows above the large-block class): every hub's positions in
+    // one range padded to whole chunks of HUB_CHUNK positions, hub h from
+    // position hub_choff[h] * HUB_CHUNK (see hub_layout in propagate.cu)
+    int32_t *hub_lab = nullptr;     // label at each position, gathered once per sweep
+    long long *hub_key = nullptr;   // packed key at each candidate's first position
+    uint32_t *hub_bits = nullptr;   // one bit per position: a candidate's first position (zero between sweeps)
+    long long *hub_cmax = nullptr;  // per chunk: largest ordered key of its candidates (LLONG_MIN between sweeps)
+    int32_t *hub_cnf = nullptr;     // per chunk: scan flag, then final-level candidates, then their prefix
+    int32_t *hub_chunk = nullptr;   // per chunk: its hub (index in the hub list)
+    int32_t *hub_choff = nullptr;   // per hub: first chunk (hubs + 1 entries)
+    int32_t *hub_item = nullptr;    // per hub: first part item (hubs + 1 entries)
+    int32_t *hub_cf = nullptr;      // per hub: neighbours in its own community (0 between sweeps)
+    int64_t hub_cap_chunks = 0, hub_cap_hubs = 0;
+    int32_t hub_count = 0, hub_chunks = 0, hub_items = 0;
     size_t hub_bytes = 0;
     size_t dev_bytes = 0;             // device memory held through dev_alloc and the hub slices
     // degree bins
@@ -144,12 +169,19 @@ int launch_bins(pcd_graph *g, cudaStream_t st, bool active_only = false);
 // hist: 256 * grid words; sc: scratch for scans of 256 * grid items.
 bool radix_sort(unsigned long long *ka, uint32_t *va, unsigned long long *kb, uint32_t *vb, int64_t n, int bits,
                 uint32_t *hist, const pcd::ScanScratch &sc, int grid, cudaStream_t st, int *launches);
-// hub kernel: shared table slots, distinct labels per part, per-block slice in int32 units
+// hub class: positions per chunk of the hub arrays, shared table slots of a
+// part block, and the positions per part (a hub of degree d is split by label
+// hash into ceil(d / HUB_PART_LABELS) parts, each histogrammed by one block)
+constexpr int32_t HUB_CHUNK = 1024;
 constexpr int32_t HUB_TABLE_CAP = 16384;  // 192 KiB of table: one 1024-thread block per SM
 constexpr int32_t HUB_PART_LABELS = 6144;
-constexpr int32_t HUB_MAX_PARTS = 1024;   // rows above HUB_MAX_PARTS * HUB_PART_LABELS labels fill parts faster
-// per position: an 8-byte key, a 4-byte label and an 8-byte (position, label) bucket entry
-inline int64_t hub_stride(int64_t max_deg) { return (5 * std::max<int64_t>(max_deg, 1) + 3) & ~1ll; }
+// device bytes of the hub arrays per position (label, key, bit) and per chunk
+constexpr int64_t HUB_BYTES_PER_POS = 13;
+constexpr int64_t HUB_BYTES_PER_CHUNK = 16;
+// (re)builds the hub layout after the degree classes change: chunk and part
+// offsets of every hub, the chunk -> hub map; grows the hub arrays (syncs)
+pcd_status hub_layout(pcd_graph *g, cudaStream_t st);
+void hub_release(pcd_graph *g, cudaStream_t st);  // frees the hub arrays (stream-ordered)
 
 // propagate.cu
 int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32_t seed,
@@ -186,8 +218,17 @@ namespace pcd {
 void upload_jump_table(cudaStream_t st);
 
 // profiling marks (api.cu): prof_begin clears the span list and records the
-// start; prof_mark closes the phase `name`.  No-ops unless enabled.
+// start on `st`; prof_mark closes the phase `name` on stream st (the span
+// runs from the previous mark on st); prof_fork starts stream `side` at the
+// current point of `from`.  No-ops unless enabled.
 void prof_begin(pcd_ctx *ctx, cudaStream_t st);
 void prof_mark(pcd_ctx *ctx, const char *name, cudaStream_t st);
+void prof_fork(pcd_ctx *ctx, cudaStream_t side);
+
+// side streams (api.cu): fork `k` side streams off ctx->stream (they wait for
+// everything issued on it so far) and return them; join makes ctx->stream
+// wait for everything issued on them.  Capture-safe (events only).
+pcd_status side_fork(pcd_ctx *ctx, int k, cudaStream_t *out);
+void side_join(pcd_ctx *ctx, int k);
 
 }  // namespace pcd

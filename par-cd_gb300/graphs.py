@@ -395,6 +395,63 @@ def powerlaw(n: int, deg_exp: float, deg_min: int, deg_max: int, comm_exp: float
     return _dedup_undirected(a, b, n)
 
 
+def powerlaw_torch(n: int, deg_exp: float, deg_min: int, deg_max: int, comm_exp: float, comm_min: int,
+                   comm_max: int, mu: float, seed: int, device="cuda"):
+    """The construction of `powerlaw` (LFR-style planted communities) with
+    torch on a device, for the large power-law workloads (8 M vertices):
+    power-law degrees and community sizes by inverse-CDF sampling, a fraction
+    1 - mu of each vertex's stubs paired inside its community (stubs sorted
+    by (community, random key), consecutive stubs of one community paired),
+    the rest paired uniformly at random across the graph and kept when the two
+    ends lie in different communities.  torch's random streams, so the graph
+    differs from `powerlaw`'s draw for draw.  Returns numpy (indices, adj,
+    map, community of each original vertex) with the converter's semantics."""
+    import torch
+
+    dev = torch.device(device)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+
+    def plaw(count, exponent, lo, hi):
+        u = torch.rand(count, generator=gen, device=dev, dtype=torch.float64)
+        e1 = 1.0 - exponent
+        return torch.floor((lo ** e1 + u * (hi ** e1 - lo ** e1)) ** (1.0 / e1)).to(torch.int64)
+
+    deg = plaw(n, deg_exp, deg_min, deg_max)
+    # community sizes: draw until they cover n, the last one cut to fit
+    sizes = plaw(2 * n // max(1, comm_min) + 16, comm_exp, comm_min, comm_max)
+    cum = torch.cumsum(sizes, 0)
+    ncomm = int(torch.searchsorted(cum, torch.tensor([n], device=dev, dtype=torch.int64)).item()) + 1
+    sizes = sizes[:ncomm].clone()
+    sizes[-1] -= int(cum[ncomm - 1].item()) - n
+    comm = torch.repeat_interleave(torch.arange(ncomm, device=dev), sizes)
+    comm = comm[torch.randperm(n, generator=gen, device=dev)]
+    k_in = torch.round(deg.to(torch.float64) * (1.0 - mu)).to(torch.int64)
+    k_out = deg - k_in
+    ids = torch.arange(n, device=dev)
+    # intra-community stubs
+    sv = torch.repeat_interleave(ids, k_in)
+    key = comm[sv] * (1 << 31) + torch.randint(0, 1 << 31, (sv.shape[0],), generator=gen, device=dev)
+    sv = sv[torch.argsort(key)]
+    del key
+    h = sv.shape[0] // 2
+    a_in, b_in = sv[0:2 * h:2], sv[1:2 * h:2]
+    ok = comm[a_in] == comm[b_in]
+    a_in, b_in = a_in[ok], b_in[ok]
+    del sv, ok
+    # inter-community stubs
+    so = torch.repeat_interleave(ids, k_out)
+    so = so[torch.randperm(so.shape[0], generator=gen, device=dev)]
+    h = so.shape[0] // 2
+    a_out, b_out = so[:h], so[h:2 * h]
+    ok = comm[a_out] != comm[b_out]
+    src = torch.cat([a_in, a_out[ok]])
+    dst = torch.cat([b_in, b_out[ok]])
+    del so, a_out, b_out, ok, a_in, b_in
+    ind, adj, mp = csr_from_edges_torch(src, dst, n)
+    return ind, adj, mp, comm.cpu().numpy()
+
+
 def batch_sizes(count: int, median: float, sigma: float, lo: int, hi: int, seed: int) -> np.ndarray:
     rng = np.random.default_rng(seed)
     s = np.exp(np.log(median) + sigma * rng.standard_normal(count))

@@ -79,6 +79,7 @@ def _load() -> C.CDLL:
         "pcd_destroy": ([vp], i32),
         "pcd_set_stream": ([vp, vp], i32),
         "pcd_synchronize": ([vp], i32),
+        "pcd_set_class_streams": ([vp, i32], i32),
         "pcd_load_csr": ([vp, i32, i32, vp, vp, C.POINTER(vp)], i32),
         "pcd_load_csr_device": ([vp, i32, i32, vp, vp, C.POINTER(vp)], i32),
         "pcd_graph_free": ([vp], i32),
@@ -219,6 +220,10 @@ class Context:
 
     def set_stream(self, stream_ptr: int | None):
         self._check(LIB.pcd_set_stream(self.h, C.c_void_p(stream_ptr or 0)))
+
+    def class_streams(self, on: bool = True):
+        """Run a sweep's degree classes concurrently on side streams."""
+        self._check(LIB.pcd_set_class_streams(self.h, 1 if on else 0))
 
     def synchronize(self):
         self._check(LIB.pcd_synchronize(self.h))
@@ -529,18 +534,23 @@ THRESHOLD_ITER_CAP = 1000
 
 
 def run(g: Graph, rule: Rule, strategy: int = 0, frac: float = 0.5, rounds: int = 1, n_iter: int = -1,
-        threshold: float = 0.0, initial: int = 0, keep_raw: bool = False, callback=None) -> RunResult:
+        threshold: float = 0.0, initial: int = 0, keep_raw: bool = False, callback=None,
+        initial_on_device: bool = False) -> RunResult:
     """The reference driver loop (src/main.cpp:187-266) on the device.
 
     In threshold mode (n_iter == -1) the reference loops until the relative
     improvement drops to `threshold`, which never happens for a graph whose
     score stays <= 0 (e.g. a single edge); this loop, like pcd_batch_run, stops
-    after THRESHOLD_ITER_CAP iterations."""
+    after THRESHOLD_ITER_CAP iterations.  `initial_on_device`: the
+    triangle-based start partition (initial 1) is computed on the device
+    (the same labels as the host's)."""
     rand = GlibcRand(1)
     if initial == 1 or rule.kind == 2:
         g.count_triangles()
     if initial == 0:
         g.labels = create_singleton_partition(g, rand)
+    elif initial == 1 and initial_on_device:
+        create_clustering_partition_device(g)
     elif initial == 1:
         g.labels = create_clustering_partition(g)
     else:
@@ -653,6 +663,18 @@ class Batch:
         k = np.zeros(self.G, np.int32)
         self.ctx._check(LIB.pcd_batch_compress(self.h, _ptr(k)))
         return k
+
+    def stats(self):
+        """Per-graph statistics: a list of (sizes, int_volume, ext_volume),
+        graph g's communities numbered from 0 as in that graph alone."""
+        k = self.compress()
+        tot = int(k.sum())
+        s = np.zeros(max(tot, 1), np.int32)
+        i = np.zeros(max(tot, 1), np.int32)
+        e = np.zeros(max(tot, 1), np.int32)
+        self.ctx._check(LIB.pcd_stats_get(self.h, _ptr(s), _ptr(i), _ptr(e)))
+        off = np.concatenate([[0], np.cumsum(k)])
+        return [(s[off[g]:off[g + 1]], i[off[g]:off[g + 1]], e[off[g]:off[g + 1]]) for g in range(self.G)]
 
     def score(self, rule: Rule) -> np.ndarray:
         out = np.zeros(self.G, np.float64)

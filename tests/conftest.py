@@ -77,3 +77,28 @@ def ctx():
     c = pcd.Context(0)
     yield c
     c.close()
+
+
+def score_tolerance(metric, want, stats, m):
+    """Largest accepted |got - want| for a Modularity / CPM score: 1e-12
+    relative, or the reference's own rounding error where that is larger.
+    The reference adds one FP64 term per community in sequence
+    (src/rules.cpp:9-22, 121-129); that sum carries up to (k + 3) * 2^-53 *
+    sum |terms| of rounding error, which dominates when the terms cancel
+    (scores near zero on graphs with many communities).  The device sums are
+    exact integers rounded once."""
+    import oracle
+
+    rule, lam = oracle.parse_rule(metric)
+    sizes = stats.sizes.astype(np.float64)
+    iv = stats.int_volume.astype(np.float64)
+    ev = stats.ext_volume.astype(np.float64)
+    if rule == 0:
+        x = (iv + ev) / (2.0 * m)
+        mag = float(np.sum(np.abs(iv / (2.0 * m)) + x * x))
+    elif rule == 1:
+        mag = float(np.sum(np.abs(iv) + lam * sizes * np.maximum(sizes - 1, 0))) / (2.0 * m)
+    else:
+        return 1e-12 * abs(want)
+    k = len(sizes)
+    return max(1e-12 * abs(want), (k + 3) * 2.0 ** -53 * mag)

@@ -77,13 +77,33 @@ def test_schedule_seeds_are_the_reference_drivers():
     sys.path.insert(0, ROOT)
     import bench
 
+    import numpy as np
+
     libc = ctypes.CDLL("libc.so.6")
     libc.rand.restype = ctypes.c_int
     for n in (0, 1, 1000, 123457):
         libc.srand(ctypes.c_uint(1))
         for _ in range(n):
             libc.rand()
-        assert bench.schedule_seeds(n, 5) == [libc.rand() for _ in range(5)]
+        ind = np.zeros(n + 1, np.int32)  # n isolated vertices: only n matters
+        assert bench.schedule_seeds(ind, np.zeros(0, np.int32), 5) == [libc.rand() for _ in range(5)]
+
+
+def test_reference_arm_helpers_map_no_product_library():
+    """The reference arm draws its seeds and runs its sweeps through the
+    oracle only: libpcd.so is never mapped into that process."""
+    code = (
+        "import sys, numpy as np; sys.path.insert(0, %r); import bench, graphs; "
+        "g = graphs.convert_edges(graphs.rmat(10, 8, 0.57, 0.19, 0.19, seed=2)); "
+        "s = bench.schedule_seeds(g.indices, g.adj, 2); "
+        "bench.cpu_sweeps(g.indices, g.adj, s, 2, 2, 10.0); "
+        "maps = open('/proc/self/maps').read(); "
+        "print('libpcd.so' in maps, 'libpcd_oracle.so' in maps)" % ROOT)
+    env = dict(os.environ, PYTHONPATH=os.pathsep.join([ROOT, os.path.join(ROOT, "par-cd_gb300"),
+                                                       os.path.join(ROOT, "oracle")]))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.split() == ["False", "True"], r.stdout
 
 
 def test_bins_bytes_sum_to_the_sweep_formula():

@@ -61,7 +61,7 @@ def test_batch_run_matches_each_graph_alone(ctx, metric, strategy, frac, rounds,
         assert iters[i] == res.iterations
 
 
-def test_batch_threshold_mode_stops_each_graph_on_its_own(ctx):
+def test_batch_threshold_mode_stops_each_graph_on_its_own(ctx, port):
     import pcd
 
     # every graph here reaches a positive score (a lone edge never does: its
@@ -71,12 +71,57 @@ def test_batch_threshold_mode_stops_each_graph_on_its_own(ctx):
     B = pcd.Batch.from_graphs(ctx, graphs)
     scores, iters = B.run(rule, 2, 1.0, 1, -1, 0.01, True)
     labels = B.labels
+    # after the run, statistics and scores are those of every graph's final
+    # labels, including graphs that left the degree classes early
+    again = B.score(rule)
+    stats = B.stats()
     B.free()
     for i, (ind, adj) in enumerate(graphs):
         res = _alone(ctx, ind, adj, rule, 2, 1.0, 1, -1, 0.01)
         assert iters[i] == res.iterations, f"graph {i}"
-        assert np.array_equal(labels[B.voff[i]:B.voff[i + 1]], res.labels)
+        mine = labels[B.voff[i]:B.voff[i + 1]]
+        assert np.array_equal(mine, res.labels)
         assert scores[i] == res.score
+        assert again[i] == res.score, f"graph {i}: score after the run"
+        port.load(ind, adj)
+        st = port.stats(mine)
+        assert np.array_equal(stats[i][0], st.sizes), f"graph {i}: sizes after the run"
+        assert np.array_equal(stats[i][1], st.int_volume), f"graph {i}: int volume after the run"
+        assert np.array_equal(stats[i][2], st.ext_volume), f"graph {i}: ext volume after the run"
+
+
+def test_batch_steps_after_a_run_refine_every_graph(ctx, port):
+    """A run ends with every graph marked finished; single steps afterwards
+    still refine every graph."""
+    import oracle
+    import pcd
+
+    graphs = _mixed_graphs()[:6]
+    rule = pcd.ModularityRule()
+    B = pcd.Batch.from_graphs(ctx, graphs)
+    B.run(rule, 0, 1.0, 1, 3, 0.0, True)
+    B.compress()
+    start = B.labels
+    rng = np.random.default_rng(17)
+    seeds = rng.integers(0, 2**31, size=B.G).astype(np.uint32)
+    B.refine(rule, 1.0, seeds)
+    got = B.labels
+    B.labels = start
+    B.merge(rule, 1, seeds)
+    got_m = B.labels
+    B.free()
+    rk, lam = oracle.parse_rule("mod")
+    moved = 0
+    for i, (ind, adj) in enumerate(graphs):
+        port.load(ind, adj)
+        c = start[B.voff[i]:B.voff[i + 1]]
+        st = port.stats(c)
+        want = port.refine_prop(rk, lam, c, 1.0, seed=int(seeds[i]), st=st)
+        assert np.array_equal(got[B.voff[i]:B.voff[i + 1]], want), f"graph {i}: refine after a run"
+        want_m = port.refine_merge(rk, lam, c, 1, seed=int(seeds[i]), st=st)
+        assert np.array_equal(got_m[B.voff[i]:B.voff[i + 1]], want_m), f"graph {i}: merge after a run"
+        moved += int(np.count_nonzero(want != c))
+    assert moved > 0  # the steps did change labels
 
 
 def test_batch_single_steps_match_oracle(ctx, port):

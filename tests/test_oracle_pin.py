@@ -271,3 +271,22 @@ def test_extras_side_by_side_with_reference(port, seed):
     b = (a + rng.integers(0, 3, g.n)).astype(np.int32) % 40
     for x, y in ((a, b), (a, comp), (comp, comp)):
         assert repr(port.nmi(x, y)) == repr(ref.nmi(x, y))
+
+
+def test_threaded_triangles_and_wcc_score_equal_the_sequential_ones():
+    """The oracle's OpenMP triangle count and WCC score (used to check the
+    large power-law workload in reasonable time) give exactly the sequential
+    restatement's results."""
+    import numpy as np
+
+    import graphs
+    import oracle
+
+    ind, adj, _, _ = graphs.powerlaw_torch(30000, 2.5, 8, 2000, 1.5, 20, 2000, 0.3, seed=11, device="cpu")
+    p = oracle.Port().load(ind, adj)
+    t1, d1, c1 = p.count_triangles()
+    t4, d4, c4 = p.count_triangles(threads=4)
+    assert np.array_equal(t1, t4) and np.array_equal(d1, d4) and c1 == c4
+    lab, _ = p.compress(p.clustering())
+    st = p.stats(lab)
+    assert p.score(2, 0.0, lab, st) == p.score(2, 0.0, lab, st, threads=4)

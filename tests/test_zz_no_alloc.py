@@ -64,6 +64,29 @@ def test_noalloc_matches_allocating_compress_twice_in_a_row():
         want, k = _reference_compress(pcd, ctx, lab)
         assert int(d_k.item()) == k
         assert np.array_equal(d_out.cpu().numpy(), want)
+    # labels outside [-1, n) take a fresh id each, like NEW_LABEL (-1)
+    n = 50_000
+    lab = rng.integers(0, 2_000, size=n).astype(np.int32)
+    odd = rng.random(n)
+    lab[odd < 0.03] = n + rng.integers(0, 1000, size=int((odd < 0.03).sum())).astype(np.int32)
+    lab[(odd >= 0.03) & (odd < 0.06)] = -2 - rng.integers(0, 1000, size=int(((odd >= 0.03) & (odd < 0.06)).sum()))
+    lab[(odd >= 0.06) & (odd < 0.08)] = -1
+    lab[:3] = [n, -5, 2**31 - 1]
+    d_in = torch.from_numpy(lab).cuda()
+    d_out = torch.full((n,), -7, dtype=torch.int32, device="cuda")
+    d_k = torch.zeros(1, dtype=torch.int32, device="cuda")
+    assert lib.pcd_compress_labels_noalloc(d_in.data_ptr(), n, d_out.data_ptr(), d_k.data_ptr(),
+                                           C.c_void_p(stream.cuda_stream)) == 0
+    torch.cuda.synchronize()
+    as_new = np.where((lab < -1) | (lab >= n), -1, lab).astype(np.int32)
+    want, k = _reference_compress(pcd, ctx, as_new)
+    assert int(d_k.item()) == k
+    assert np.array_equal(d_out.cpu().numpy(), want)
+    # n == 0: no labels, a count of 0 written on the stream
+    d_k.fill_(-3)
+    assert lib.pcd_compress_labels_noalloc(None, 0, None, d_k.data_ptr(), C.c_void_p(stream.cuda_stream)) == 0
+    torch.cuda.synchronize()
+    assert int(d_k.item()) == 0
     # sizes beyond the fixed array are refused without touching the outputs
     big = torch.zeros(maxn + 1, dtype=torch.int32, device="cuda")
     out = torch.zeros(maxn + 1, dtype=torch.int32, device="cuda")
