@@ -957,9 +957,6 @@ def main():
     phases = {}
     for nm, ms in ctx.profile_read():  # a class may run as several launches (degree sub-ranges)
         phases[nm] = phases.get(nm, 0.0) + ms
-    hub_parts = [nm for nm in phases if nm.startswith("sweep.hub_")]
-    if hub_parts:  # the hub class runs as consecutive launches on one stream
-        phases["sweep.hub"] = sum(phases[nm] for nm in hub_parts)
     ctx.profile(False)
     info = G.info()
     bins_now = G.get_bins()

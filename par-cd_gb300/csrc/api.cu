@@ -290,7 +290,7 @@ pcd_status pcd_graph_free(pcd_graph *g) {
     cudaStream_t fs = ctx ? ctx->stream : nullptr;
     for (void *p : g->allocs)
         if (p) cudaFreeAsync(p, fs);
-    hub_release(g, fs);
+    if (g->hub_scratch) cudaFreeAsync(g->hub_scratch, fs);
     if (g->merge_buf) cudaFreeAsync(g->merge_buf, fs);
     if (g->batch && g->batch->seed_table) cudaFreeAsync(g->batch->seed_table, fs);
     delete g->batch;
@@ -361,6 +361,32 @@ pcd_status pcd_synchronize(pcd_ctx *ctx) {
     return PCD_OK;
 }
 
+// Hub slices: per block, a packed key and a label for every position of the
+// largest row; as many blocks as there are hub vertices (at most one per SM);
+// grown when the degree classes change.  No initial contents are needed.
+static pcd_status ensure_hub_scratch(pcd_graph *g) {
+    pcd_ctx *ctx = g->ctx;
+    const int64_t hubs = g->bin_off[NBINS] - g->bin_off[BIN_HUB];
+    const int32_t want = (int32_t)std::min<int64_t>(ctx->num_sms, hubs);
+    if (want <= g->hub_blocks) return PCD_OK;
+    const int64_t stride = hub_stride(g->max_deg);
+    cudaStream_t st = ctx->stream;
+    CK(cudaStreamSynchronize(st), "hub scratch");
+    if (g->hub_scratch) {
+        cudaFreeAsync(g->hub_scratch, st);
+        g->dev_bytes -= g->hub_bytes;
+    }
+    g->hub_scratch = nullptr;
+    g->hub_blocks = 0;
+    g->hub_bytes = 0;
+    const size_t bytes = sizeof(int32_t) * (size_t)(stride * want);
+    CK(cudaMallocAsync((void **)&g->hub_scratch, bytes, st), "hub scratch");
+    g->hub_blocks = want;
+    g->hub_bytes = bytes;
+    g->dev_bytes += bytes;
+    return PCD_OK;
+}
+
 static pcd_status graph_setup(pcd_ctx *ctx, pcd_graph *g) {
     const int64_t n = g->n, nn = std::max<int64_t>(n, 1);
     cudaStream_t st = ctx->stream;
@@ -425,7 +451,7 @@ static pcd_status graph_setup(pcd_ctx *ctx, pcd_graph *g) {
     // degree bins, then the hub slices (the same tables plus labels and counts by position)
     g->bins = BinConfig{{4, 8, 16, 32, 256, 2048, 8192}};
     if (n > 0) launch_bins(g, st);
-    TRY(hub_layout(g, st));
+    TRY(ensure_hub_scratch(g));
     // initial labels: singletons 0..n-1 (already compressed)
     g->k = g->n;
     g->compressed = false;
@@ -477,7 +503,7 @@ static pcd_status load_common(pcd_ctx *ctx, int32_t n, int32_t m, const int32_t 
         cudaStreamSynchronize(ctx->stream);
         for (void *p : g->allocs)
             if (p) cudaFreeAsync(p, ctx->stream);
-        hub_release(g, ctx->stream);
+        if (g->hub_scratch) cudaFreeAsync(g->hub_scratch, ctx->stream);
         delete g;
         return s;
     }
@@ -514,7 +540,7 @@ pcd_status pcd_graph_device_bytes(pcd_graph *g, int64_t *bytes) {
 // Upper bound of what pcd_batch_load + pcd_batch_run (or pcd_load_csr and the
 // phase calls, num_graphs = 1) hold on the device at their peak, from sizes
 // the caller knows before loading.  Mirrors the allocations of graph_setup,
-// hub_layout, batch_setup, the batch staging copies, the seed table
+// ensure_hub_scratch, batch_setup, the batch staging copies, the seed table
 // of pcd_batch_run (iteration cap) and the merge buffers.
 pcd_status pcd_estimate_device_bytes(int32_t n, int64_t nnz, int32_t max_deg, int64_t num_hubs, int32_t num_graphs,
                                      int32_t iteration_cap, int32_t merges, int32_t num_sms, int64_t *bytes) {
@@ -531,10 +557,7 @@ pcd_status pcd_estimate_device_bytes(int32_t n, int64_t nnz, int32_t max_deg, in
     while (slots < 2 * (int64_t)std::max(max_deg, 1)) slots <<= 1;
     const int64_t fb_stride = 3 * slots + max_deg;
     b += 4 * fb_stride * std::min<int64_t>(8, std::max<int64_t>(1, (1ll << 29) / (4 * fb_stride)));
-    // hub arrays: every hub position (at most min(nnz, hubs * max_deg)) plus
-    // each hub's padding to whole chunks, and the per-chunk / per-hub entries
-    const int64_t hub_pos = std::min<int64_t>(e, num_hubs * (int64_t)std::max(max_deg, 1)) + num_hubs * HUB_CHUNK;
-    b += HUB_BYTES_PER_POS * hub_pos + HUB_BYTES_PER_CHUNK * (hub_pos / HUB_CHUNK + 1) + 12 * (num_hubs + 1);
+    b += 4 * hub_stride(max_deg) * std::min<int64_t>(num_sms, num_hubs);
     // batch state, the staging copies of a batch load, the seed table of a run
     b += 8 * nn + 8 * (G + 1) + 52 * G + 64;
     b += 4 * (nn + 1) + 4 * e + 8 + 4 * (G + 1) + 4 * nn;
@@ -556,7 +579,7 @@ pcd_status pcd_graph_set_bins(pcd_graph *g, const int32_t max_deg[7]) {
     CK(cudaStreamSynchronize(ctx->stream), "set_bins");
     for (int i = 0; i < 7; ++i) g->bins.max_deg[i] = max_deg[i];
     if (g->n > 0) launch_bins(g, ctx->stream);
-    TRY(hub_layout(g, ctx->stream));
+    TRY(ensure_hub_scratch(g));
     return check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "set_bins");
 }
 

@@ -463,7 +463,6 @@ pcd_status pcd_batch_run(pcd_graph *g, const pcd_rule *rule, int32_t strategy, d
             // sweeps and statistics skip them (a captured iteration is re-captured)
             if (s == PCD_OK && done_count - done_at_bins >= std::max(1, G / 8)) {
                 launch_bins(g, st, true);
-                s = hub_layout(g, st);
                 done_at_bins = done_count;
                 if (exec) {
                     cudaGraphExecDestroy(exec);
@@ -477,8 +476,6 @@ pcd_status pcd_batch_run(pcd_graph *g, const pcd_rule *rule, int32_t strategy, d
         // every vertex back in its class; the last statistics pass skipped the
         // graphs that had left the classes, so recompute them for all graphs
         launch_bins(g, st);
-        const pcd_status hs = hub_layout(g, st);
-        if (s == PCD_OK) s = hs;
         launch_stats(g, st);
     }
     // graphs are "done" only inside a run: later single steps refine every graph

@@ -87,27 +87,36 @@ __global__ void k_set_k(DevCounters *ctr, const uint32_t *total) { ctr->k = (int
 // collect_statistics.  sizes[l] += 1, intv[l] += d_int, extv[l] += d_ext,
 // vol[l] += deg.  Integer sums: the result does not depend on order.
 // ---------------------------------------------------------------------------
+// Lanes of the warp that share a community add once, through their leader.
+// The leader sums its group's counts from shared memory (a loop as long as
+// the largest group; warp reductions over per-group masks would run once per
+// distinct community of the warp).  `wsh`: this warp's 32 slots.
 __device__ __forceinline__ void add_stats(int32_t l, int32_t di, int32_t de, int32_t *sizes, int32_t *intv,
-                                          int32_t *extv, int32_t *vol, bool valid) {
-    // lanes of the warp that share a community add once, through their leader
+                                          int32_t *extv, int32_t *vol, bool valid, int2 *wsh) {
     const int lane = threadIdx.x & 31;
-    unsigned act = __ballot_sync(FULL, valid);
-    if (!valid) return;
-    unsigned peers = __match_any_sync(act, l);
-    int s = __reduce_add_sync(peers, 1);
-    int a = __reduce_add_sync(peers, di);
-    int b = __reduce_add_sync(peers, de);
-    if (lane == __ffs(peers) - 1) {
-        atomicAdd(sizes + l, s);
+    const unsigned peers = __match_any_sync(FULL, valid ? l : -1 - lane);
+    wsh[lane] = make_int2(di, de);
+    __syncwarp();
+    if (valid && lane == __ffs(peers) - 1) {
+        int32_t a = 0, b = 0;
+        for (unsigned m = peers; m; m &= m - 1) {
+            const int2 x = wsh[__ffs(m) - 1];
+            a += x.x;
+            b += x.y;
+        }
+        atomicAdd(sizes + l, __popc(peers));
         atomicAdd(intv + l, a);
         atomicAdd(extv + l, b);
         atomicAdd(vol + l, a + b);
     }
+    __syncwarp();
 }
 
 __global__ void k_stats_thread(const int32_t *__restrict__ indices, const int32_t *__restrict__ adj,
                                const int32_t *__restrict__ labels, const int32_t *__restrict__ list,
                                int64_t count, int32_t *sizes, int32_t *intv, int32_t *extv, int32_t *vol) {
+    __shared__ int2 sh[1024];
+    int2 *wsh = sh + (threadIdx.x & ~31u);
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t start = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t rounds = (count + stride - 1) / stride;
@@ -122,7 +131,7 @@ __global__ void k_stats_thread(const int32_t *__restrict__ indices, const int32_
             for (int32_t j = b; j < e; ++j) di += (labels[adj[j]] == l);
             de = (e - b) - di;
         }
-        add_stats(l, di, de, sizes, intv, extv, vol, valid);
+        add_stats(l, di, de, sizes, intv, extv, vol, valid, wsh);
     }
 }
 

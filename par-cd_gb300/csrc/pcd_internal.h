@@ -104,20 +104,10 @@ struct pcd_graph {
     int32_t *fb_scratch = nullptr;
     int64_t fb_slots = 0;    // power of two >= 2 * max_deg
     int32_t fb_blocks = 0;
-    // hub class (rows above the large-block class): every hub's positions in
-    // one range padded to whole chunks of HUB_CHUNK positions, hub h from
-    // position hub_choff[h] * HUB_CHUNK (see hub_layout in propagate.cu)
-    int32_t *hub_lab = nullptr;     // label at each position, gathered once per sweep
-    long long *hub_key = nullptr;   // packed key at each candidate's first position
-    uint32_t *hub_bits = nullptr;   // one bit per position: a candidate's first position (zero between sweeps)
-    long long *hub_cmax = nullptr;  // per chunk: largest ordered key of its candidates (LLONG_MIN between sweeps)
-    int32_t *hub_cnf = nullptr;     // per chunk: scan flag, then final-level candidates, then their prefix
-    int32_t *hub_chunk = nullptr;   // per chunk: its hub (index in the hub list)
-    int32_t *hub_choff = nullptr;   // per hub: first chunk (hubs + 1 entries)
-    int32_t *hub_item = nullptr;    // per hub: first part item (hubs + 1 entries)
-    int32_t *hub_cf = nullptr;      // per hub: neighbours in its own community (0 between sweeps)
-    int64_t hub_cap_chunks = 0, hub_cap_hubs = 0;
-    int32_t hub_count = 0, hub_chunks = 0, hub_items = 0;
+    // hub kernel: one slice per hub block (hub_stride(max_deg) ints: packed
+    // keys, labels and (position, label) buckets of the row being refined)
+    int32_t *hub_scratch = nullptr;
+    int32_t hub_blocks = 0;
     size_t hub_bytes = 0;
     size_t dev_bytes = 0;             // device memory held through dev_alloc and the hub slices
     // degree bins
@@ -169,19 +159,12 @@ int launch_bins(pcd_graph *g, cudaStream_t st, bool active_only = false);
 // hist: 256 * grid words; sc: scratch for scans of 256 * grid items.
 bool radix_sort(unsigned long long *ka, uint32_t *va, unsigned long long *kb, uint32_t *vb, int64_t n, int bits,
                 uint32_t *hist, const pcd::ScanScratch &sc, int grid, cudaStream_t st, int *launches);
-// hub class: positions per chunk of the hub arrays, shared table slots of a
-// part block, and the positions per part (a hub of degree d is split by label
-// hash into ceil(d / HUB_PART_LABELS) parts, each histogrammed by one block)
-constexpr int32_t HUB_CHUNK = 1024;
+// hub kernel: shared table slots, distinct labels per part, per-block slice in int32 units
 constexpr int32_t HUB_TABLE_CAP = 16384;  // 192 KiB of table: one 1024-thread block per SM
 constexpr int32_t HUB_PART_LABELS = 6144;
-// device bytes of the hub arrays per position (label, key, bit) and per chunk
-constexpr int64_t HUB_BYTES_PER_POS = 13;
-constexpr int64_t HUB_BYTES_PER_CHUNK = 16;
-// (re)builds the hub layout after the degree classes change: chunk and part
-// offsets of every hub, the chunk -> hub map; grows the hub arrays (syncs)
-pcd_status hub_layout(pcd_graph *g, cudaStream_t st);
-void hub_release(pcd_graph *g, cudaStream_t st);  // frees the hub arrays (stream-ordered)
+constexpr int32_t HUB_MAX_PARTS = 1024;   // rows above HUB_MAX_PARTS * HUB_PART_LABELS labels fill parts faster
+// per position: an 8-byte key, a 4-byte label and an 8-byte (position, label) bucket entry
+inline int64_t hub_stride(int64_t max_deg) { return (5 * std::max<int64_t>(max_deg, 1) + 3) & ~1ll; }
 
 // propagate.cu
 int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32_t seed,

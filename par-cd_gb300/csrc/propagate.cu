@@ -763,9 +763,12 @@ __global__ void __launch_bounds__(BT) k_prop_block(SweepArgs a, R rule, const in
 // ---------------------------------------------------------------------------
 // ---------------------------------------------------------------------------
 // block per vertex, one keyed pass (degrees up to NW * 32 * RPL).
-//   H  histogram: labels into the shared table (label, count, first position by
-//      atomicMin); pos_slot[p] = the slot of p's label for the first lane of
-//      each warp-level match group, -1 for the others (never first positions).
+//   H  histogram: every position inserts its label into the shared table
+//      (positions with one label meet in one slot, one CAS wins; count and
+//      first position by shared-memory atomics); pos_slot[p] = the slot of p's
+//      label.  (Pre-aggregating equal labels across the warp with match_any
+//      cost more than the atomics it saved: R-MAT scale 24, large-block class
+//      4.99 -> 4.54 ms without it.)
 //   K  every warp owns a contiguous position range, RPL positions per lane in
 //      registers; a position is a candidate iff first[slot] == p.  Packed keys
 //      and the range maximum; one barrier, then every warp knows its carry-in
@@ -833,25 +836,20 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
             for (int u = 0; u < 4; ++u) {
                 const int32_t p = p0 + u * BT + tid;
                 const int32_t l = lab[u];
-                const unsigned peers = __match_any_sync(FULL, l);
                 if (p < d) {
-                    int32_t slot = -1;
-                    if (lane == __ffs(peers) - 1) {
-                        uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
-                        for (;;) {
-                            const int32_t kk = keys[h];
-                            if (kk == l) break;
-                            if (kk == -1) {
-                                const int32_t old = atomicCAS(&keys[h], -1, l);
-                                if (old == -1 || old == l) break;
-                            }
-                            h = (h + 1) & (uint32_t)(ts - 1);
+                    uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
+                    for (;;) {
+                        const int32_t kk = keys[h];
+                        if (kk == l) break;
+                        if (kk == -1) {
+                            const int32_t old = atomicCAS(&keys[h], -1, l);
+                            if (old == -1 || old == l) break;
                         }
-                        atomicAdd(&cnts[h], __popc(peers));
-                        atomicMin(&first[h], (uint32_t)p);  // the leader is its group's first position
-                        slot = (int32_t)h;
+                        h = (h + 1) & (uint32_t)(ts - 1);
                     }
-                    pos_slot[p] = slot;
+                    atomicAdd(&cnts[h], 1);
+                    atomicMin(&first[h], (uint32_t)p);
+                    pos_slot[p] = (int32_t)h;
                 }
             }
         }
@@ -981,370 +979,264 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
 }
 
 // ---------------------------------------------------------------------------
-// Hubs (rows above the large-block class), in three launches over all hubs:
-//   gather  every hub's neighbour labels into hub_lab, once per sweep;
-//   parts   a hub of degree d is split by label hash into P = ceil(d / 6144)
-//           parts; each (hub, part) item is one block's work: it scans the
-//           hub's labels, histograms those of its part in the shared table
-//           (label, count, first position), then walks the table once, writing
-//           each candidate's packed key at its first position (hub_key), the
-//           position's bit (hub_bits) and the chunk maximum (hub_cmax, one per
-//           HUB_CHUNK positions); items are taken from a queue, hub after hub;
-//   order   one block per hub: chunk carry-ins are the prefix maxima of the
-//           chunk maxima (from the initial 0.0); a chunk whose maximum lies
-//           below its carry-in level can hold neither a tie with the running
-//           maximum nor a final-level candidate, so only the other chunks are
-//           scanned in position order (ties, FP64 ambiguity, final level).
-//           Then the decision and the final level's labels, as in the one-pass
-//           block kernel, and the bits and chunk maxima are cleared again.
-// A chunk never straddles two hubs (each hub's range is padded to whole
-// chunks), so bit words and chunk entries belong to one hub.
+// Hubs: 1024-thread blocks (one per SM) that take hubs from a queue in list
+// order (largest first), so one very large hub does not leave the others to a
+// fixed share of the blocks.  A hub's labels are split by hash into P parts of
+// at most part_labels distinct labels; each part is histogrammed in the shared
+// table (label, count, first position: every bucket entry inserts itself,
+// with shared-memory atomics for the count and the minimum position, since
+// bucket order is not position order), then the table is walked once in slot
+// order: each label's packed key is written at its first position and the
+// slot is cleared in the same walk.  Position-indexed arrays in a per-block
+// global slice carry the row between parts: pos_lab[p] (the label at position
+// p, gathered once) and pos_key[p] (the identity, then the packed key at each
+// candidate's first position).  The ordered pass of the one-pass kernel then
+// runs over pos_key: range maxima, carry-ins, ties and the final level.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t hub_part(uint32_t hv, int32_t parts) {
     return (uint32_t)(((unsigned long long)hv * (uint32_t)parts) >> 32);
 }
 
-__device__ __forceinline__ int32_t hub_parts_of(int32_t d) { return max(1, (d + HUB_PART_LABELS - 1) / HUB_PART_LABELS); }
-
-// Packed keys as order-preserving int64 (the chunk maxima use integer atomicMax).
-__device__ __forceinline__ long long key_ord(long long k) { return k; }
-__device__ __forceinline__ long long key_ord(double k) {
-    const long long b = __double_as_longlong(k);
-    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
-}
-template <class K>
-__device__ __forceinline__ K ord_key(long long o);
-template <>
-__device__ __forceinline__ long long ord_key<long long>(long long o) {
-    return o;
-}
-template <>
-__device__ __forceinline__ double ord_key<double>(long long o) {
-    return __longlong_as_double(o ^ ((o >> 63) & 0x7fffffffffffffffLL));
-}
-constexpr long long ORD_NONE = LLONG_MIN;  // no candidate in the chunk
-// a packed key's bits in the int64 hub_key array, and back
-__device__ __forceinline__ long long key_bits(long long k) { return k; }
-__device__ __forceinline__ long long key_bits(double k) { return __double_as_longlong(k); }
-template <class K>
-__device__ __forceinline__ K bits_key(long long b);
-template <>
-__device__ __forceinline__ long long bits_key<long long>(long long b) {
-    return b;
-}
-template <>
-__device__ __forceinline__ double bits_key<double>(long long b) {
-    return __longlong_as_double(b);
-}
-
-struct HubView {
-    int32_t *lab;
-    long long *key;
-    uint32_t *bits;
-    long long *cmax;
-    int32_t *cnf;
-    const int32_t *chunk;
-    const int32_t *choff;
-    const int32_t *item;
-    int32_t *cf;
-    int32_t count, chunks, items;
-};
-
-// gather: hub_lab[choff[h] * CHUNK + p] = labels[adj[b + p]], one chunk per block step
-__global__ void __launch_bounds__(256) k_hub_gather(SweepArgs a, HubView hv, const int32_t *__restrict__ list) {
-    for (int64_t c = blockIdx.x; c < hv.chunks; c += gridDim.x) {
-        const int32_t h = hv.chunk[c];
-        const int32_t v = list[h];
-        const int32_t b = a.g.indices[v], d = a.g.indices[v + 1] - b;
-        const int32_t p0 = (int32_t)(c - hv.choff[h]) * HUB_CHUNK;
-        int32_t l[HUB_CHUNK / 256];
-#pragma unroll
-        for (int u = 0; u < HUB_CHUNK / 256; ++u) {
-            const int32_t p = p0 + u * 256 + (int32_t)threadIdx.x;
-            l[u] = p < d ? a.g.adj[b + p] : -1;
-        }
-#pragma unroll
-        for (int u = 0; u < HUB_CHUNK / 256; ++u)
-            if (l[u] >= 0) hv.lab[c * HUB_CHUNK + u * 256 + threadIdx.x] = a.labels[l[u]];
-    }
-}
-
-// The hub of work item `it`: the last h with item[h] <= it.
-__device__ __forceinline__ int32_t hub_of_item(const int32_t *__restrict__ item, int32_t count, int32_t it) {
-    int32_t lo = 0, hi = count - 1;
-    while (lo < hi) {
-        const int32_t mid = (lo + hi + 1) >> 1;
-        if (item[mid] <= it) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
-constexpr int HUB_SMEM_CHUNKS = 512;  // chunk maxima kept in shared memory up to this many chunks per hub
-
 template <class R>
-__global__ void __launch_bounds__(1024) k_hub_parts(SweepArgs a, R rule, HubView hv, const int32_t *__restrict__ list) {
+__global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, const int32_t *__restrict__ list,
+                                                         int64_t count, int32_t table_cap, int32_t part_labels,
+                                                         int32_t *gscratch, int64_t gstride, int32_t pos_cap) {
     using PK = PackedKey<R>;
-    constexpr int BT = 1024, U = 4;
+    using K = typename PK::K;
+    constexpr int BT = 1024, NW = 32;
     extern __shared__ int32_t smem[];
     int32_t *keys = smem;
-    int32_t *cnts = smem + HUB_TABLE_CAP;
-    uint32_t *first = reinterpret_cast<uint32_t *>(smem + 2 * HUB_TABLE_CAP);
-    __shared__ long long s_cmax[HUB_SMEM_CHUNKS];
-    __shared__ int32_t s_it[2];  // by iteration parity: a slot is rewritten only after every thread read it
-    const int tid = threadIdx.x, lane = tid & 31;
-    for (int32_t i = tid; i < HUB_TABLE_CAP; i += BT) {
+    int32_t *cnts = smem + table_cap;
+    uint32_t *first = reinterpret_cast<uint32_t *>(smem + 2 * table_cap);
+    __shared__ int32_t s_start[HUB_MAX_PARTS + 1], s_cur[HUB_MAX_PARTS];
+    __shared__ K s_agg[NW];
+    __shared__ uint32_t s_t[NW];
+    __shared__ int32_t s_nfin[NW];
+    __shared__ int32_t s_amb, s_curr_freq;
+    __shared__ int32_t s_vi[2];  // by iteration parity: a slot is rewritten only after every thread read it
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    K *pos_key = reinterpret_cast<K *>(gscratch + (int64_t)blockIdx.x * gstride);
+    int32_t *pos_lab = reinterpret_cast<int32_t *>(pos_key + pos_cap);
+    // (position, label) grouped by part; starts on an 8-byte boundary whatever pos_cap is
+    int2 *bucket = reinterpret_cast<int2 *>(pos_lab + ((pos_cap + 1) & ~1));
+    for (int32_t i = tid; i < table_cap; i += BT) {
         keys[i] = -1;
         cnts[i] = 0;
         first[i] = 0xffffffffu;
     }
+    __syncthreads();
     for (int it = 0;; ++it) {
-        if (tid == 0) s_it[it & 1] = atomicAdd(&a.ctr->hub_next, 1);
+        if (tid == 0) s_vi[it & 1] = atomicAdd(&a.ctr->hub_next, 1);
         __syncthreads();
-        const int32_t item = s_it[it & 1];
-        if (item >= hv.items) break;
-        const int32_t h = hub_of_item(hv.item, hv.count, item);
-        const int32_t part = item - hv.item[h], parts = hv.item[h + 1] - hv.item[h];
-        const int32_t v = list[h];
+        const int64_t vi = s_vi[it & 1];
+        if (vi >= count) break;
+        const int32_t v = list[vi];
         const int32_t b = a.g.indices[v], d = a.g.indices[v + 1] - b;
         const int32_t curr = a.labels[v];
         const R vr = rule.at(v);
-        if (vr.vertex_ambiguous(d)) continue;  // the order pass queues it for the FP64 rule
-        const int32_t c0 = hv.choff[h], nch = hv.choff[h + 1] - c0;
-        const int64_t off = (int64_t)c0 * HUB_CHUNK;
-        const bool smem_max = nch <= HUB_SMEM_CHUNKS;
-        const int32_t per_part = (d + parts - 1) / parts;
-        int32_t ts = 64;
-        while (ts < 2 * per_part && ts < HUB_TABLE_CAP) ts <<= 1;
-        if (smem_max)
-            for (int32_t c = tid; c < nch; c += BT) s_cmax[c] = ORD_NONE;
-        __syncthreads();
-        // histogram of this part's labels
-        for (int32_t q0 = 0; q0 < d; q0 += BT * U) {
-            int32_t l[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int32_t p = q0 + u * BT + tid;
-                l[u] = p < d ? hv.lab[off + p] : -1;
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int32_t p = q0 + u * BT + tid;
-                const bool in = p < d && (int32_t)hub_part(hash_label(l[u]), parts) == part;
-                const unsigned peers = __match_any_sync(FULL, in ? l[u] : -2 - lane);
-                if (in && lane == __ffs(peers) - 1) {  // the group's lowest lane: its first position
-                    uint32_t hh = hash_label(l[u]) & (uint32_t)(ts - 1);
-                    int32_t probes = 0;
-                    for (; probes < ts; ++probes) {
-                        const int32_t kk = keys[hh];
-                        if (kk == l[u]) break;
-                        if (kk == -1) {
-                            const int32_t old = atomicCAS(&keys[hh], -1, l[u]);
-                            if (old == -1 || old == l[u]) break;
-                        }
-                        hh = (hh + 1) & (uint32_t)(ts - 1);
-                    }
-                    if (probes < ts) {
-                        atomicAdd(&cnts[hh], __popc(peers));
-                        atomicMin(&first[hh], (uint32_t)p);
-                    } else {
-                        atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);  // a part overfilled the table
-                    }
-                }
-            }
-        }
-        __syncthreads();
-        // slot walk: each candidate's key at its first position; the table is cleared
-        for (int32_t i = tid; i < ts; i += BT) {
-            const int32_t l = keys[i];
-            if (l == -1) continue;
-            const int32_t k = cnts[i];
-            const uint32_t p = first[i];
-            keys[i] = -1;
-            cnts[i] = 0;
-            first[i] = 0xffffffffu;
-            if (l == curr) {
-                hv.cf[h] = k;
-            } else {
-                Tag tag{0, 0};
-                const typename R::Key raw = vr.join(v, d, l, k, a.cm, tag);
-                if (!R::usable(raw)) continue;
-                const auto pk = PK::make(raw, k);
-                hv.key[off + p] = key_bits(pk);
-                atomicOr(&hv.bits[(off + p) >> 5], 1u << (p & 31u));
-                if (smem_max)
-                    atomicMax(&s_cmax[p / HUB_CHUNK], key_ord(pk));
-                else
-                    atomicMax(&hv.cmax[c0 + p / HUB_CHUNK], key_ord(pk));
-            }
-        }
-        __syncthreads();
-        if (smem_max)
-            for (int32_t c = tid; c < nch; c += BT)
-                if (s_cmax[c] != ORD_NONE) atomicMax(&hv.cmax[c0 + c], s_cmax[c]);
-    }
-}
-
-template <class R>
-__global__ void __launch_bounds__(1024) k_hub_order(SweepArgs a, R rule, HubView hv, const int32_t *__restrict__ list) {
-    using PK = PackedKey<R>;
-    using K = typename PK::K;
-    constexpr int BT = 1024, NW = BT / 32;
-    __shared__ uint32_t s_t;
-    __shared__ int32_t s_amb, s_total, s_cfirst;
-    __shared__ long long s_mreal;
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    for (int64_t h = blockIdx.x; h < hv.count; h += gridDim.x) {
-        const int32_t v = list[h];
-        const int32_t b = a.g.indices[v], d = a.g.indices[v + 1] - b;
-        const int32_t curr = a.labels[v];
-        const R vr = rule.at(v);
-        const int32_t c0 = hv.choff[h], nch = hv.choff[h + 1] - c0;
-        const int64_t off = (int64_t)c0 * HUB_CHUNK;
         if (vr.vertex_ambiguous(d)) {
             if (tid == 0) push_ambiguous(a, v, d);
-            continue;  // the part pass wrote nothing for it
+            continue;
         }
-        // chunk carry-ins (warp 0, 32 chunks at a time): hub_cmax[c] <- the
-        // carry-in of chunk c, hub_cnf[c] <- whether chunk c must be scanned
-        if (wid == 0) {
-            long long carry = key_ord(PK::init());
-            long long mreal = ORD_NONE;
-            for (int32_t cb = 0; cb < nch; cb += 32) {
-                const int32_t c = cb + lane;
-                const long long x = c < nch ? hv.cmax[c0 + c] : ORD_NONE;
-                long long inc = x;
+        if (d > pos_cap) {  // the slices hold the largest degree: never expected
+            if (tid == 0) atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);
+            continue;
+        }
+        const int32_t parts = min(HUB_MAX_PARTS, max(1, (d + part_labels - 1) / part_labels));
+        for (int32_t i = tid; i < parts; i += BT) s_cur[i] = 0;
+        if (tid == 0) {
+            s_amb = 0;
+            s_curr_freq = 0;
+        }
+        __syncthreads();
+        // the row's labels by position (gathered once) and the part sizes
+        for (int32_t p0 = 0; p0 < d; p0 += BT * 4) {
+            int32_t l[4];
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const long long y = __shfl_up_sync(FULL, inc, o);
-                    if (lane >= o) inc = max(inc, y);
-                }
-                long long ex = __shfl_up_sync(FULL, inc, 1);
-                if (lane == 0) ex = ORD_NONE;
-                const long long cin = max(carry, ex);
-                if (c < nch) {
-                    const bool need = x != ORD_NONE && PK::level(ord_key<K>(x)) >= PK::level(ord_key<K>(cin));
-                    hv.cmax[c0 + c] = cin;
-                    hv.cnf[c0 + c] = need ? 1 : 0;
-                }
-                const long long tot = __shfl_sync(FULL, inc, 31);
-                carry = max(carry, tot);
-                mreal = max(mreal, tot);
+            for (int u = 0; u < 4; ++u) {
+                const int32_t p = p0 + u * BT + tid;
+                l[u] = p < d ? a.g.adj[b + p] : -1;
             }
-            if (lane == 0) {
-                s_mreal = mreal;
-                s_t = 0;
-                s_amb = 0;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int32_t p = p0 + u * BT + tid;
+                int32_t pt = -1 - lane;
+                if (p < d) {
+                    l[u] = a.labels[l[u]];
+                    pos_lab[p] = l[u];
+                    pos_key[p] = PK::ident();
+                    pt = (int32_t)hub_part(hash_label(l[u]), parts);
+                }
+                const unsigned peers = __match_any_sync(FULL, pt);
+                if (p < d && lane == __ffs(peers) - 1) atomicAdd(&s_cur[pt], __popc(peers));
             }
         }
         __syncthreads();
-        const long long mreal_o = s_mreal;
-        const K mreal = mreal_o == ORD_NONE ? PK::ident() : ord_key<K>(mreal_o);
-        const auto lfin = PK::level(kmax(PK::init(), mreal));
-        // ordered scan of the flagged chunks, one warp per chunk
-        for (int32_t c = wid; c < nch; c += NW) {
-            if (!hv.cnf[c0 + c]) continue;  // stays 0: no final-level candidate here
-            K carry = ord_key<K>(hv.cmax[c0 + c]);
-            uint32_t t = 0;
-            int32_t nfin = 0;
-            bool amb = false;
-            int32_t *fin_list = hv.lab + off + (int64_t)c * HUB_CHUNK;  // entries already read are overwritten
-            for (int32_t j0 = 0; j0 < HUB_CHUNK; j0 += 32) {
-                const int32_t p = c * HUB_CHUNK + j0 + lane;
-                const uint32_t word = hv.bits[(off + c * HUB_CHUNK + j0) >> 5];
-                const bool cand = p < d && ((word >> lane) & 1u);
-                K key = PK::ident();
-                int32_t l = -1;
-                if (cand) {
-                    key = bits_key<K>(hv.key[off + p]);
-                    l = hv.lab[off + p];
-                }
-                __syncwarp();
-                const bool fin = cand && PK::level(key) == lfin;
-                const unsigned fm = __ballot_sync(FULL, fin);
-                if (fin) fin_list[nfin + __popc(fm & lanemask_lt())] = l;
-                nfin += __popc(fm);
-                if (!__any_sync(FULL, cand && PK::level(key) >= PK::level(carry))) continue;
-                K inc = key;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const K y = __shfl_up_sync(FULL, inc, o);
-                    if (lane >= o) inc = kmax(inc, y);
-                }
-                K ex = __shfl_up_sync(FULL, inc, 1);
-                if (lane == 0) ex = PK::ident();
-                const K pre = kmax(carry, ex);
-                const bool tie = cand && PK::level(key) == PK::level(pre);
-                if (tie && PK::tie_ambiguous(key, pre)) amb = true;
-                t += __popc(__ballot_sync(FULL, tie));
-                carry = kmax(carry, __shfl_sync(FULL, inc, 31));
-            }
-            amb = __any_sync(FULL, amb);
-            if (lane == 0) {
-                hv.cnf[c0 + c] = nfin;
-                if (t) atomicAdd(&s_t, t);
-                if (amb) s_amb = 1;
-            }
-        }
-        __syncthreads();
-        // exclusive prefix of the final-level counts over chunks (warp 0)
-        if (wid == 0) {
-            int32_t run = 0, cfirst = -1;
-            for (int32_t cb = 0; cb < nch; cb += 32) {
-                const int32_t c = cb + lane;
-                const int32_t x = c < nch ? hv.cnf[c0 + c] : 0;
-                int32_t inc = x;
+        if (wid == 0) {  // exclusive scan of the part sizes
+            int32_t carry = 0;
+            for (int32_t i0 = 0; i0 < parts; i0 += 32) {
+                const int32_t i = i0 + lane;
+                const int32_t c = i < parts ? s_cur[i] : 0;
+                int32_t inc = c;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
                     const int32_t y = __shfl_up_sync(FULL, inc, o);
                     if (lane >= o) inc += y;
                 }
-                const unsigned nz = __ballot_sync(FULL, x > 0);
-                if (cfirst < 0 && nz) cfirst = cb + __ffs(nz) - 1;
-                if (c < nch) hv.cnf[c0 + c] = run + inc - x;
-                run += __shfl_sync(FULL, inc, 31);
+                if (i < parts) s_start[i] = carry + inc - c;
+                carry += __shfl_sync(FULL, inc, 31);
             }
-            if (lane == 0) {
-                s_total = run;
-                s_cfirst = cfirst;
-            }
+            if (lane == 0) s_start[parts] = carry;
         }
         __syncthreads();
-        const int32_t nf = s_total;
+        for (int32_t i = tid; i < parts; i += BT) s_cur[i] = s_start[i];
+        __syncthreads();
+        for (int32_t p0 = 0; p0 < d; p0 += BT) {  // positions into their part's bucket
+            const int32_t p = p0 + tid;
+            const int32_t pt = p < d ? (int32_t)hub_part(hash_label(pos_lab[p]), parts) : -1 - lane;
+            const unsigned peers = __match_any_sync(FULL, pt);
+            int32_t base = 0;
+            if (p < d && lane == __ffs(peers) - 1) base = atomicAdd(&s_cur[pt], __popc(peers));
+            base = __shfl_sync(FULL, base, __ffs(peers) - 1);
+            if (p < d) bucket[base + __popc(peers & lanemask_lt())] = make_int2(p, pos_lab[p]);
+        }
+        __syncthreads();
+        for (int32_t part = 0; part < parts; ++part) {
+            const int32_t i0 = s_start[part], i1 = s_start[part + 1];
+            int32_t ts = 64;
+            while (ts < 2 * (i1 - i0) && ts < table_cap) ts <<= 1;
+            // histogram of this part's labels
+            for (int32_t j0 = i0; j0 < i1; j0 += BT) {
+                const int32_t j = j0 + tid;
+                const int2 e = j < i1 ? bucket[j] : make_int2(-1, -2);
+                const int32_t p = e.x, l = e.y;
+                if (p >= 0) {
+                    uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
+                    int32_t probes = 0;
+                    for (; probes < ts; ++probes) {
+                        const int32_t kk = keys[h];
+                        if (kk == l) break;
+                        if (kk == -1) {
+                            const int32_t old = atomicCAS(&keys[h], -1, l);
+                            if (old == -1 || old == l) break;
+                        }
+                        h = (h + 1) & (uint32_t)(ts - 1);
+                    }
+                    if (probes < ts) {
+                        atomicAdd(&cnts[h], 1);
+                        atomicMin(&first[h], (uint32_t)p);
+                    } else {
+                        atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);  // a part overfilled the table
+                    }
+                }
+            }
+            __syncthreads();
+            // slot walk: each label's key at its first position; the slot is cleared
+            for (int32_t i = tid; i < ts; i += BT) {
+                const int32_t l = keys[i];
+                if (l != -1) {
+                    const int32_t k = cnts[i];
+                    const uint32_t p = first[i];
+                    if (l == curr) {
+                        s_curr_freq = k;
+                    } else {
+                        Tag tag{0, 0};
+                        const typename R::Key raw = vr.join(v, d, l, k, a.cm, tag);
+                        if (R::usable(raw)) pos_key[p] = PK::make(raw, k);
+                    }
+                    keys[i] = -1;
+                    cnts[i] = 0;
+                    first[i] = 0xffffffffu;
+                }
+            }
+            __syncthreads();
+        }
+        // ordered pass over the keyed positions, one contiguous range per warp
+        const int32_t span = ((d + NW - 1) / NW + 31) & ~31;
+        const int32_t lo = min(d, wid * span), hi = min(d, lo + span);
+        K wmax = PK::ident();
+        for (int32_t p = lo + lane; p < hi; p += 32) wmax = kmax(wmax, pos_key[p]);
+#pragma unroll
+        for (int o = 16; o; o >>= 1) wmax = kmax(wmax, __shfl_xor_sync(FULL, wmax, o));
+        if (lane == 0) s_agg[wid] = wmax;
+        __syncthreads();
+        K carry = PK::init(), mreal = PK::ident();
+        for (int w2 = 0; w2 < NW; ++w2) {
+            const K x = s_agg[w2];
+            if (w2 < wid) carry = kmax(carry, x);
+            mreal = kmax(mreal, x);
+        }
+        const auto lfin = PK::level(kmax(PK::init(), mreal));
+        uint32_t t = 0;
+        int32_t nfin = 0;
+        bool amb = false;
+        int32_t *fin_list = pos_lab + lo;  // entries already read are overwritten
+        for (int32_t base = lo; base < hi; base += 32) {
+            const int32_t p = base + lane;
+            const K key = p < hi ? pos_key[p] : PK::ident();
+            const bool cand = key != PK::ident();
+            const int32_t l = cand ? pos_lab[p] : -1;
+            __syncwarp();
+            const bool fin = cand && PK::level(key) == lfin;
+            const unsigned fm = __ballot_sync(FULL, fin);
+            if (fin) fin_list[nfin + __popc(fm & lanemask_lt())] = l;
+            nfin += __popc(fm);
+            if (!__any_sync(FULL, cand && PK::level(key) >= PK::level(carry))) continue;
+            K inc = key;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const K y = __shfl_up_sync(FULL, inc, o);
+                if (lane >= o) inc = kmax(inc, y);
+            }
+            K ex = __shfl_up_sync(FULL, inc, 1);
+            if (lane == 0) ex = PK::ident();
+            const K pre = kmax(carry, ex);
+            const bool tie = cand && PK::level(key) == PK::level(pre);
+            if (tie && PK::tie_ambiguous(key, pre)) amb = true;
+            t += __popc(__ballot_sync(FULL, tie));
+            carry = kmax(carry, __shfl_sync(FULL, inc, 31));
+        }
+        amb = __any_sync(FULL, amb);
+        if (lane == 0) {
+            s_t[wid] = t;
+            s_nfin[wid] = nfin;
+            if (amb) s_amb = 1;
+        }
+        __syncthreads();
+        uint32_t tt = 0;
+        int32_t nf = 0, before = 0, hw = -1;
+        for (int w2 = 0; w2 < NW; ++w2) {
+            const int32_t c = s_nfin[w2];
+            tt += s_t[w2];
+            if (w2 < wid) before += c;
+            if (hw < 0 && c > 0) hw = w2;
+            nf += c;
+        }
         const bool has_best = mreal != PK::ident() && PK::level(mreal) > PK::level(PK::init());
-        const int32_t holder = has_best && s_cfirst >= 0 ? hv.lab[off + (int64_t)s_cfirst * HUB_CHUNK] : -1;
+        const int32_t holder = has_best && hw >= 0 ? pos_lab[hw * span] : -1;
         const int32_t r = has_best ? nf - 1 : 0;
         int32_t dec = DEC_AMBIGUOUS;
         if (!s_amb) {
             const typename R::Key best = has_best ? PK::raw_level(mreal) : R::initial();
-            dec = vr.decide(best, has_best, v, d, curr, hv.cf[h], a.cm);
+            dec = vr.decide(best, has_best, v, d, curr, s_curr_freq, a.cm);
         }
         const bool rec = dec == DEC_MOVE && r > 0;
         if (tid == 0) {
             if (dec == DEC_AMBIGUOUS) {
                 push_ambiguous(a, v, d);
             } else {
-                a.ndraw[v] = s_t;
+                a.ndraw[v] = tt;
                 write_decision(a, v, dec, holder, curr);
                 record_ties(a, v, b, rec, r, holder);
             }
         }
-        if (rec) {  // chunk c's final-level labels follow those of the chunks before it
-            const long long toff = (long long)b + v;  // record_ties' slots: holder, then the ties
-            for (int32_t c = wid; c < nch; c += NW) {
-                const int32_t before = hv.cnf[c0 + c];
-                const int32_t cnt = (c + 1 < nch ? hv.cnf[c0 + c + 1] : nf) - before;
-                for (int32_t j = lane; j < cnt; j += 32) {
-                    const int32_t gi = before + j;  // 0 is the holder
-                    if (gi > 0) a.tiebuf[toff + gi] = hv.lab[off + (int64_t)c * HUB_CHUNK + j];
-                }
+        if (rec) {  // the same number of iterations in every lane
+            const long long off = (long long)b + v;
+            for (int32_t j0 = 0; j0 < nfin; j0 += 32) {
+                const int32_t j = j0 + lane, gi = before + j;  // 0 is the holder
+                if (j < nfin && gi > 0) a.tiebuf[off + gi] = fin_list[j];
             }
         }
-        __syncthreads();
-        // clean for the next sweep: bits, chunk maxima, own-community count
-        for (int64_t w = off / 32 + tid; w < (off + (int64_t)nch * HUB_CHUNK) / 32; w += BT) hv.bits[w] = 0u;
-        for (int32_t c = tid; c < nch; c += BT) hv.cmax[c0 + c] = ORD_NONE;
-        if (tid == 0) hv.cf[h] = 0;
         __syncthreads();
     }
 }
@@ -1718,125 +1610,6 @@ static void launch_thread(pcd_graph *g, const SweepArgs &a, const R &rule, int b
     prof_mark(g->ctx, name, st);
 }
 
-static HubView hub_view(pcd_graph *g) {
-    return HubView{g->hub_lab,   g->hub_key,   g->hub_bits,  g->hub_cmax,  g->hub_cnf,   g->hub_chunk,
-                   g->hub_choff, g->hub_item,  g->hub_cf,    g->hub_count, g->hub_chunks, g->hub_items};
-}
-
-__global__ void k_hub_degrees(const int32_t *__restrict__ indices, const int32_t *__restrict__ list, int64_t count,
-                              int32_t *deg) {
-    for (int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; h < count; h += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t v = list[h];
-        deg[h] = indices[v + 1] - indices[v];
-    }
-}
-
-__global__ void k_hub_chunk_map(const int32_t *__restrict__ choff, int32_t count, int32_t *chunk) {
-    for (int64_t h = blockIdx.x; h < count; h += gridDim.x)
-        for (int32_t c = choff[h] + threadIdx.x; c < choff[h + 1]; c += blockDim.x) chunk[c] = (int32_t)h;
-}
-
-__global__ void k_fill_i64(long long *p, int64_t n, long long x) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        p[i] = x;
-}
-
-static void hub_free(pcd_graph *g, cudaStream_t st) {
-    for (void *p : {(void *)g->hub_lab, (void *)g->hub_key, (void *)g->hub_bits, (void *)g->hub_cmax,
-                    (void *)g->hub_cnf, (void *)g->hub_chunk, (void *)g->hub_choff, (void *)g->hub_item,
-                    (void *)g->hub_cf})
-        if (p) cudaFreeAsync(p, st);
-    g->hub_lab = nullptr;
-    g->hub_key = nullptr;
-    g->hub_bits = nullptr;
-    g->hub_cmax = nullptr;
-    g->hub_cnf = nullptr;
-    g->hub_chunk = nullptr;
-    g->hub_choff = nullptr;
-    g->hub_item = nullptr;
-    g->hub_cf = nullptr;
-    g->dev_bytes -= g->hub_bytes;
-    g->hub_bytes = 0;
-    g->hub_cap_chunks = g->hub_cap_hubs = 0;
-}
-
-void hub_release(pcd_graph *g, cudaStream_t st) { hub_free(g, st); }
-
-// The hub list's layout: hub h owns chunks [choff[h], choff[h+1]) and part
-// items [item[h], item[h+1]).  The arrays grow (never shrink) with the hub
-// class; between sweeps hub_bits is zero, hub_cmax is ORD_NONE and hub_cf is
-// zero (the order pass restores that after each sweep).
-pcd_status hub_layout(pcd_graph *g, cudaStream_t st) {
-    pcd_ctx *ctx = g->ctx;
-    const int64_t H = g->bin_off[BIN_HUB + 1] - g->bin_off[BIN_HUB];
-    g->hub_count = 0;
-    g->hub_chunks = 0;
-    g->hub_items = 0;
-    if (H <= 0) return PCD_OK;
-    int32_t *d_deg = nullptr;
-    if (cudaMallocAsync(&d_deg, sizeof(int32_t) * (size_t)H, st) != cudaSuccess)
-        return check_cuda(ctx, cudaGetLastError(), "hub layout");
-    k_hub_degrees<<<cap_grid((H + 255) / 256, (int64_t)ctx->num_sms * 4), 256, 0, st>>>(
-        g->indices, g->bin_list + g->bin_off[BIN_HUB], H, d_deg);
-    std::vector<int32_t> deg((size_t)H), choff((size_t)H + 1), item((size_t)H + 1);
-    cudaMemcpyAsync(deg.data(), d_deg, sizeof(int32_t) * (size_t)H, cudaMemcpyDeviceToHost, st);
-    cudaFreeAsync(d_deg, st);
-    pcd_status s = check_cuda(ctx, cudaStreamSynchronize(st), "hub layout");
-    if (s != PCD_OK) return s;
-    int64_t ch = 0, it = 0;
-    for (int64_t h = 0; h < H; ++h) {
-        choff[(size_t)h] = (int32_t)ch;
-        item[(size_t)h] = (int32_t)it;
-        const int64_t d = deg[(size_t)h];
-        ch += (d + HUB_CHUNK - 1) / HUB_CHUNK;
-        it += std::max<int64_t>(1, (d + HUB_PART_LABELS - 1) / HUB_PART_LABELS);
-    }
-    choff[(size_t)H] = (int32_t)ch;
-    item[(size_t)H] = (int32_t)it;
-    if (ch > g->hub_cap_chunks || H > g->hub_cap_hubs) {
-        hub_free(g, st);
-        const int64_t pos = ch * HUB_CHUNK;
-        size_t bytes = 0;
-        auto al = [&](void **p, size_t b) {
-            if (s != PCD_OK) return;
-            if (cudaMallocAsync(p, b, st) != cudaSuccess) {
-                *p = nullptr;
-                s = check_cuda(ctx, cudaGetLastError(), "hub arrays");
-            }
-            bytes += b;
-        };
-        al((void **)&g->hub_lab, sizeof(int32_t) * (size_t)pos);
-        al((void **)&g->hub_key, sizeof(long long) * (size_t)pos);
-        al((void **)&g->hub_bits, sizeof(uint32_t) * (size_t)(pos / 32));
-        al((void **)&g->hub_cmax, sizeof(long long) * (size_t)ch);
-        al((void **)&g->hub_cnf, sizeof(int32_t) * (size_t)ch);
-        al((void **)&g->hub_chunk, sizeof(int32_t) * (size_t)ch);
-        al((void **)&g->hub_choff, sizeof(int32_t) * (size_t)(H + 1));
-        al((void **)&g->hub_item, sizeof(int32_t) * (size_t)(H + 1));
-        al((void **)&g->hub_cf, sizeof(int32_t) * (size_t)H);
-        g->hub_bytes = bytes;
-        g->dev_bytes += bytes;
-        if (s != PCD_OK) {
-            hub_free(g, st);
-            return s;
-        }
-        g->hub_cap_chunks = ch;
-        g->hub_cap_hubs = H;
-        cudaMemsetAsync(g->hub_bits, 0, sizeof(uint32_t) * (size_t)(pos / 32), st);
-        k_fill_i64<<<cap_grid((ch + 255) / 256, (int64_t)ctx->num_sms * 4), 256, 0, st>>>(g->hub_cmax, ch, ORD_NONE);
-        cudaMemsetAsync(g->hub_cf, 0, sizeof(int32_t) * (size_t)H, st);
-    }
-    cudaMemcpyAsync(g->hub_choff, choff.data(), sizeof(int32_t) * (size_t)(H + 1), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(g->hub_item, item.data(), sizeof(int32_t) * (size_t)(H + 1), cudaMemcpyHostToDevice, st);
-    k_hub_chunk_map<<<cap_grid(H, (int64_t)ctx->num_sms * 4), 256, 0, st>>>(g->hub_choff, (int32_t)H, g->hub_chunk);
-    s = check_cuda(ctx, cudaStreamSynchronize(st), "hub layout");
-    if (s != PCD_OK) return s;
-    g->hub_count = (int32_t)H;
-    g->hub_chunks = (int32_t)ch;
-    g->hub_items = (int32_t)it;
-    return PCD_OK;
-}
-
 // The degree classes of one sweep are independent (each reads only the old
 // labels and writes its own vertices' outputs), so they run concurrently:
 // hubs, the large-block and the block classes each on a side stream forked
@@ -1850,24 +1623,17 @@ static int launch_bins_rule(pcd_graph *g, const SweepArgs &a, const R &rule, cud
     cudaStream_t side[pcd_ctx::kSide];
     const bool forked = g->ctx->class_streams && side_fork(g->ctx, pcd_ctx::kSide, side) == PCD_OK;
     cudaStream_t s_hub = forked ? side[0] : st, s_bl = forked ? side[1] : st, s_b = forked ? side[2] : st;
-    if (g->hub_count > 0) {
-        // hubs: gather, part histograms (1024-thread blocks, one per SM, items
-        // from a queue), ordered pass (a block per hub)
-        const HubView hv = hub_view(g);
-        const int32_t *hl = L + g->bin_off[BIN_HUB];
-        const int sms = g->ctx->num_sms;
-        k_hub_gather<<<cap_grid(g->hub_chunks, (int64_t)sms * 8), 256, 0, s_hub>>>(a, hv, hl);
-        prof_mark(g->ctx, "sweep.hub_gather", s_hub);
-        const size_t smem = 3ull * HUB_TABLE_CAP * sizeof(int32_t);
-        cudaFuncSetAttribute(k_hub_parts<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        int per_sm = 1;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hub_parts<R>, 1024, smem);
-        k_hub_parts<R><<<cap_grid(g->hub_items, (int64_t)sms * std::max(1, per_sm)), 1024, smem, s_hub>>>(a, rule, hv,
-                                                                                                       hl);
-        prof_mark(g->ctx, "sweep.hub_parts", s_hub);
-        k_hub_order<R><<<cap_grid(g->hub_count, (int64_t)sms * 2), 1024, 0, s_hub>>>(a, rule, hv, hl);
-        launches += 3;
-        prof_mark(g->ctx, "sweep.hub_order", s_hub);
+    if ((c = g->bin_off[BIN_HUB + 1] - g->bin_off[BIN_HUB]) > 0) {
+        // hubs: 1024-thread blocks (one per SM), shared tables filled part by
+        // part, position arrays in per-block slices of hub_scratch
+        constexpr int32_t cap = HUB_TABLE_CAP;
+        const size_t smem = 3ull * cap * sizeof(int32_t);
+        cudaFuncSetAttribute(k_prop_hub_parts<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_prop_hub_parts<R><<<cap_grid(c, g->hub_blocks), 1024, smem, s_hub>>>(
+            a, rule, L + g->bin_off[BIN_HUB], c, cap, HUB_PART_LABELS, g->hub_scratch, hub_stride(g->max_deg),
+            g->max_deg);
+        ++launches;
+        prof_mark(g->ctx, "sweep.hub", s_hub);
     }
     // warp and block classes: one launch per degree sub-range, tables sized to
     // its largest degree, larger sub-ranges first
