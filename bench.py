@@ -115,6 +115,12 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def tune_cache() -> str:
+    import tempfile
+
+    return os.path.join(tempfile.gettempdir(), "pcd_bench_tuning.json")
+
+
 def max_over_ranks(dist, x: float, device) -> float:
     """The job's time is its slowest rank's: max of x over the ranks (x itself
     without a process group)."""
@@ -307,7 +313,7 @@ def batch_cpu_baseline(voff, ind, adj, idx, sched, budget_s):
     return len(done) / sec, len(done), sec, threads
 
 
-def batched_leg(args, ctx, dev):
+def batched_leg(args, ctx, dev, strategy=None, frac=None):
     """Many-graph workload: the log-normal batch of SBMs, every graph run
     through the reference driver's schedule (singleton start, stop test,
     final labels and score).  Batched = one packed batch through
@@ -328,13 +334,30 @@ def batched_leg(args, ctx, dev):
     N = int(voff[-1])
     M = int(d_ind[-1].item()) // 2
     log(f"[bench] batch: {Gn} SBM graphs, n={N} m={M} ({time.time() - t0:.1f}s)")
-    sched = {"metric": args.batch_metric, "strategy": args.batch_strategy, "frac": args.batch_frac,
+    sched = {"metric": args.batch_metric,
+             "strategy": args.batch_strategy if strategy is None else strategy,
+             "frac": args.batch_frac if frac is None else frac,
              "rounds": 1, "n_iter": args.batch_iters, "threshold": args.batch_threshold}
     rule = pcd.parse_metric(sched["metric"])
     h_labels = torch.empty(N, dtype=torch.int32).pin_memory()
+    tuned = None
+    if args.tune:
+        import tune
+
+        Bt = pcd.Batch.from_device(ctx, voff, d_ind.data_ptr(), d_adj.data_ptr())
+        tr = tune.tune_batch(Bt, rule, sched["frac"], d_ind.cpu().numpy(), cache_path=tune_cache(), retune=True)
+        Bt.free()
+        tuned = {k: tr[k] for k in ("bins", "hub_part", "ms", "default_ms")}
+        tuned["note"] = "ms: the batch's first propagation step, best tuned vs default classes"
+
+    def configure(B):
+        if tuned:
+            B.set_bins(tuned["bins"])
+            B.set_hub_part(tuned["hub_part"])
 
     def batched_job():
         B = pcd.Batch.from_device(ctx, voff, d_ind.data_ptr(), d_adj.data_ptr())
+        configure(B)
         scores, iters = B.run(rule, sched["strategy"], sched["frac"], sched["rounds"], sched["n_iter"],
                               sched["threshold"], True)
         B.get_labels_ptr(h_labels.data_ptr())
@@ -358,6 +381,7 @@ def batched_leg(args, ctx, dev):
     torch.cuda.synchronize()
     t = time.perf_counter()
     B = pcd.Batch.from_host_ptr(ctx, voff, h_ind.data_ptr(), h_adj.data_ptr())
+    configure(B)
     s3, _ = B.run(rule, sched["strategy"], sched["frac"], sched["rounds"], sched["n_iter"], sched["threshold"],
                   True)
     B.get_labels_ptr(h_labels.data_ptr())
@@ -414,6 +438,7 @@ def batched_leg(args, ctx, dev):
         "speedup_vs_plain": batched_gps / plain_gps,
         "iterations_max": int(iters.max()), "iterations_mean": float(iters.mean()),
         "identical_to_plain": True,
+        "tuning": tuned,
         "cpu_baseline": cpu,
     }
 
@@ -562,11 +587,15 @@ def serve_pool(dev):
 
 def served_leg(args, dev):
     """Requests arrive as a Poisson stream (seed 5): 90% SBM, 9% power-law, 1%
-    R-MAT s22, each Modularity or CPM(0.01) with the reference's default stop
-    test (-s 0 -t 0, frac 1.0).  Served: pcd.Server (batches under a 150 GB
-    HBM budget).  Plain: the same requests in arrival order through the
-    single-graph path, one at a time (FIFO queue: latency = wait + service).
-    Every served result must equal the plain one."""
+    R-MAT s22, each Modularity or CPM(0.01), -s 0 -f 1.0 with the iteration
+    count pinned (-n, default 20: under CPM an R-MAT graph's score never turns
+    positive, so a -t 0 stop test would run it to the iteration cap).
+    Served: pcd.Server with continuous batching (graphs join and leave running
+    batches between iterations, under a 150 GB HBM budget).  Plain: the same
+    requests in arrival order through the single-graph path, one at a time
+    (FIFO queue: latency = wait + service).  Arrival rates are multiples of the
+    plain path's capacity (1 / mean service time), from well below it to well
+    above it.  Every served result must equal the plain one."""
     import numpy as np
 
     import pcd
@@ -582,6 +611,7 @@ def served_leg(args, dev):
         g = pool[int(rng.integers(len(pool)))]
         reqs.append((g, "mod" if rng.random() < 0.5 else "cpm-0.01"))
         kinds.append("sbm" if u < 0.90 else ("powerlaw" if u < 0.99 else "rmat22"))
+    n_iter = args.serve_iters
     gaps = rng.exponential(1.0, size=len(reqs))
     edges = sum(len(g[1]) // 2 for g, _ in reqs)
 
@@ -590,12 +620,12 @@ def served_leg(args, dev):
     plain = []
     for g, metric in reqs[:3]:  # warm-up
         G = pcd.Graph.from_csr(ctx, g[0], g[1])
-        pcd.run(G, pcd.parse_metric(metric), 0, 1.0, 1, -1, 0.0, 0)
+        pcd.run(G, pcd.parse_metric(metric), 0, 1.0, 1, n_iter, 0.0, 0)
         G.free()
     for g, metric in reqs:
         t = time.perf_counter()
         G = pcd.Graph.from_csr(ctx, g[0], g[1])
-        res = pcd.run(G, pcd.parse_metric(metric), 0, 1.0, 1, -1, 0.0, 0)
+        res = pcd.run(G, pcd.parse_metric(metric), 0, 1.0, 1, n_iter, 0.0, 0)
         G.free()
         plain.append((time.perf_counter() - t, res))
     ctx.close()
@@ -605,9 +635,12 @@ def served_leg(args, dev):
         return {k: round(float(np.percentile(x, q)) * 1000.0, 3) for k, q in (("p50", 50), ("p90", 90), ("p99", 99))} | \
                {"max": round(float(np.max(x)) * 1000.0, 3)}
 
+    plain_capacity = 1.0 / float(np.mean(service))
+    rates = [m * plain_capacity for m in args.serve_rate_multiples] if not args.serve_rates else args.serve_rates
     out = {"requests": len(reqs), "edges": int(edges),
            "mix": "90% SBM n~LogUniform[1e3, 5e4] (64-graph pool), 9% power-law n in {1e5, 2.5e5, 6e5}, "
-                  "1% R-MAT s22; mod or cpm-0.01 each with p 1/2; -s 0 -f 1.0 -t 0 from singletons",
+                  f"1% R-MAT s22; mod or cpm-0.01 each with p 1/2; -s 0 -f 1.0 -n {n_iter} from singletons",
+           "plain_capacity_graphs_per_s": plain_capacity,
            "hbm_budget_bytes": 150 * 10**9, "rates": [],
            "plain_service_by_type": {k: {"requests": int(sum(1 for x in kinds if x == k)),
                                          "mean_ms": round(1000.0 * float(np.mean([service[i] for i in range(len(reqs))
@@ -616,24 +649,27 @@ def served_leg(args, dev):
                                                                            for i in range(len(reqs))
                                                                            if kinds[i] == k]))}
                                      for k in ("sbm", "powerlaw", "rmat22") if k in kinds}}
-    for rate in args.serve_rates:
-        arrival = np.cumsum(gaps / rate)
+    for rate in rates:
+        # each rate serves the first `cnt` requests: about serve_seconds of arrivals
+        cnt = int(min(len(reqs), max(100, rate * args.serve_seconds)))
+        sub = reqs[:cnt]
+        arrival = np.cumsum(gaps[:cnt] / rate)
         # plain FIFO queue
-        fin = np.zeros(len(reqs))
+        fin = np.zeros(cnt)
         prev = 0.0
-        for k in range(len(reqs)):
+        for k in range(cnt):
             prev = max(arrival[k], prev) + service[k]
             fin[k] = prev
         plain_lat = fin - arrival
         with pcd.Server(device=0, workers=args.serve_workers, max_batch_graphs=256,
-                        hbm_budget_bytes=150 * 10**9, max_wait_ms=2.0) as srv:
+                        hbm_budget_bytes=150 * 10**9, max_wait_ms=2.0, continuous=True) as srv:
             tickets = []
             start = time.perf_counter()
-            for k, (g, metric) in enumerate(reqs):
+            for k, (g, metric) in enumerate(sub):
                 delay = start + arrival[k] - time.perf_counter()
                 if delay > 0:
                     time.sleep(delay)
-                tickets.append(srv.submit(g[0], g[1], pcd.parse_metric(metric), 0, 1.0, 1, -1, 0.0))
+                tickets.append(srv.submit(g[0], g[1], pcd.parse_metric(metric), 0, 1.0, 1, n_iter, 0.0))
             lat, same = [], 0
             for k, t in enumerate(tickets):
                 r = srv.wait(t)
@@ -642,15 +678,19 @@ def served_leg(args, dev):
                 same += int(np.array_equal(r.labels, p.labels) and r.score == p.score and r.iterations == p.iterations)
             wall = time.perf_counter() - start
             st = srv.stats()
-        assert same == len(reqs), f"{len(reqs) - same} served results differ from the plain path"
+        assert same == cnt, f"{cnt - same} served results differ from the plain path"
         lat = np.array(lat)
         out["rates"].append({
             "arrival_rate": rate,
-            "served": {"graphs_per_s": len(reqs) / wall, "latency_ms": pct(lat), "batches": st["batches"],
+            "rate_vs_plain_capacity": rate / plain_capacity,
+            "requests": cnt,
+            "served": {"graphs_per_s": cnt / wall, "latency_ms": pct(lat), "batches": st["batches"],
                        "mean_batch_graphs": st["batched_graphs"] / max(1, st["batches"]),
+                       "admitted_into_running_batches": st["admitted_running"],
+                       "returned_while_batch_ran_on": st["released_early"],
                        "hbm_peak_estimated_bytes": st["bytes_peak"], "hbm_batch_measured_peak_bytes":
                            st["bytes_measured_peak"], "estimate_exceeded": st["estimate_exceeded"]},
-            "plain": {"graphs_per_s": len(reqs) / float(fin[-1]), "latency_ms": pct(plain_lat)},
+            "plain": {"graphs_per_s": cnt / float(fin[-1]), "latency_ms": pct(plain_lat)},
             "identical_to_plain": True,
         })
         log(f"[bench] served at {rate}/s: {out['rates'][-1]['served']['graphs_per_s']:.0f} graphs/s, "
@@ -831,6 +871,7 @@ def main():
     ap.add_argument("--bins", default="", help="degree classes, 7 comma-separated bounds (default: library's)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of the timed sweeps")
+    ap.add_argument("--tune", type=int, default=1, help="1: autotune degree classes and hub part size first")
     ap.add_argument("--batch-graphs", type=int, default=4096, help="0: skip the many-graph workload")
     ap.add_argument("--batch-reps", type=int, default=2)
     ap.add_argument("--batch-plain-stride", type=int, default=8)
@@ -847,7 +888,11 @@ def main():
     ap.add_argument("--pl-wcc-iters", type=int, default=2, help="WCC schedule iterations on the power-law graph")
     ap.add_argument("--pl-reps", type=int, default=5, help="timed repetitions of each first sweep")
     ap.add_argument("--serve-requests", type=int, default=600, help="0: skip the served workload")
-    ap.add_argument("--serve-rates", type=float, nargs="+", default=[200.0, 2000.0])
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[],
+                    help="arrival rates (graphs/s); default: --serve-rate-multiples of the plain capacity")
+    ap.add_argument("--serve-rate-multiples", type=float, nargs="+", default=[0.25, 1.0, 4.0, 16.0])
+    ap.add_argument("--serve-iters", type=int, default=20, help="-n of every served request")
+    ap.add_argument("--serve-seconds", type=float, default=15.0, help="arrival span per rate (bounds the requests)")
     ap.add_argument("--serve-workers", type=int, default=4)
     args = ap.parse_args()
 
@@ -890,9 +935,19 @@ def main():
     d_adj = torch.from_numpy(adj).to(dev)
     torch.cuda.synchronize()
     G = pcd.Graph.from_device(ctx, n, m, d_ind.data_ptr(), d_adj.data_ptr())
+    rule = pcd.ModularityRule()
+    tuning = None
     if args.bins:
         G.set_bins([int(x) for x in args.bins.split(",")])
-    rule = pcd.ModularityRule()
+    elif args.tune:
+        import tune
+
+        # degree classes and hub part size timed on this graph (outside the timed region)
+        tr = tune.tune_graph(G, rule, cache_path=tune_cache(), retune=True, indices=ind)
+        tuning = {k: tr[k] for k in ("bins", "hub_part", "ms", "default_ms", "signature")}
+        tuning["candidates_timed"] = len(tr.get("timings", []))
+        tuning["note"] = "ms: the schedule's first two sweeps, best tuned vs default classes"
+        log(f"[bench] tuning: {json.dumps(tuning)}")
     sweep = pcd.PropagationRefinement(1.0)
     # The reference schedule (-s 0, frac 1.0): the start partition and rand_r
     # seed of each of its first S sweeps, kept on the device.
@@ -1005,11 +1060,14 @@ def main():
                "note": "each step: pcd_load_csr from pinned host CSR (validation, degree bins, buffers), "
                        "pcd_labels_set, pcd_refine, pcd_labels_get, pcd_graph_free"}
 
-    batched = None
+    batched = batched_s2 = None
     if args.batch_graphs > 0:
         del d_ind, d_adj
         torch.cuda.empty_cache()
         batched = batched_leg(args, ctx, dev)
+        torch.cuda.empty_cache()
+        # alternating propagation and merging: merge iterations in the timed region
+        batched_s2 = batched_leg(args, ctx, dev, strategy=2, frac=1.0)
 
     converted = None
     if args.convert:
@@ -1070,6 +1128,7 @@ def main():
             "parity": parity,
             "e2e": e2e,
             "batched": batched,
+            "batched_s2": batched_s2,
             "served": served,
             "powerlaw": powerlaw,
             "convert": converted,
@@ -1080,6 +1139,7 @@ def main():
             "per_sweep_ms": [round(statistics.mean(sweep_ms[j::args.sweeps]), 3)
                              for j in range(min(args.sweeps, len(sweep_ms)))],
             "bins": bins_now,
+            "tuning": tuning,
             "sweep_info": {"draws": info.draws, "fp64_recheck_vertices": info.fallback,
                            "tie_replays": info.resolved},
             "wall_s_timed": wall,

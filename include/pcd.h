@@ -101,15 +101,23 @@ pcd_status pcd_load_csr_device(pcd_ctx *ctx, int32_t n, int32_t m, const int32_t
                                const int32_t *d_adj, pcd_graph **out);
 pcd_status pcd_graph_free(pcd_graph *g);
 
-/* Degree classes of the sweep kernels: vertices of degree <= max_deg[i] (and
- * above max_deg[i-1]) run in class i: 0..3 groups of 4/8/16/32 lanes per
- * vertex, 4 a warp per vertex, 5 a 256-thread block, 6 a 1024-thread block
- * with a shared-memory table, and everything above max_deg[6] a 1024-thread
- * block with its table in HBM.  Bounds must be non-decreasing and at most
- * {4, 8, 16, 32, 256, 2048, 8192} (the kernels' capacities).  Results do not
- * depend on the classes; the autotuner and the tests move them. */
+/* No counterpart in the reference (its GPU path sorts all edges at once).
+ * Degree classes of the sweep kernels: vertices of degree <= max_deg[i] (and
+ * above max_deg[i-1]) run in class i: 0..3 one thread per vertex with the row
+ * in registers (up to 4/8/16/32 neighbours), 4 a warp per vertex, 5 a
+ * 256-thread block, 6 a 512- or 1024-thread block (shared-memory tables sized
+ * to each degree sub-range), and everything above max_deg[6] the hub kernel
+ * (1024-thread blocks, labels split into hash parts).  Bounds must be
+ * non-decreasing and at most {4, 8, 16, 32, 256, 2048, 8192} (the kernels'
+ * capacities).  Results do not depend on the classes; the autotuner
+ * (par-cd_gb300/tune.py) and the tests move them. */
 pcd_status pcd_graph_set_bins(pcd_graph *g, const int32_t max_deg[7]);
 pcd_status pcd_graph_get_bins(pcd_graph *g, int32_t max_deg[7], int64_t counts[8]);
+/* No counterpart in the reference.  Distinct labels per hash part of the hub
+ * kernel (default 6144, range [1024, 8192]: a part must fit half of the
+ * 16384-slot shared table).  Results do not depend on it; the autotuner moves
+ * it. */
+pcd_status pcd_graph_set_hub_part(pcd_graph *g, int32_t labels);
 
 /* Device memory a graph or batch holds right now (every buffer libpcd
  * allocated for it, merge buffers and seed tables included).  No counterpart
@@ -277,6 +285,13 @@ typedef struct pcd_serve_config {
     int32_t use_cuda_graph;     /* passed to pcd_batch_run */
     int64_t small_graph_edges;  /* size classes by adjacency entries: small <= this,   */
     int64_t large_graph_edges;  /* medium <= this, large above (one graph per batch)   */
+    int32_t continuous;         /* 1: a batch runs iteration by iteration; a graph whose
+                                 * schedule ends returns at that iteration and leaves,
+                                 * queued requests of the same schedule and size class
+                                 * join between iterations as slots and memory free up
+                                 * (for -s 2 at even iterations, so that all graphs of a
+                                 * batch sweep alike).  0: each batch runs to its end
+                                 * through pcd_batch_run (CUDA-graph iterations). */
 } pcd_serve_config;
 typedef struct pcd_serve_stats {
     int64_t submitted, completed, failed, batches, batched_graphs, queue_len;
@@ -284,6 +299,8 @@ typedef struct pcd_serve_stats {
     int64_t bytes_peak;          /* largest estimated total in flight so far   */
     int64_t bytes_measured_peak; /* largest pcd_graph_device_bytes of a batch  */
     int64_t estimate_exceeded;   /* batches that held more than their estimate */
+    int64_t admitted_running;    /* requests that joined a batch already running */
+    int64_t released_early;      /* requests returned while their batch ran on   */
 } pcd_serve_stats;
 typedef struct pcd_serve_timing {
     double queue_ms;        /* submit -> its batch started */

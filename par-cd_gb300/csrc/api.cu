@@ -583,6 +583,14 @@ pcd_status pcd_graph_set_bins(pcd_graph *g, const int32_t max_deg[7]) {
     return check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "set_bins");
 }
 
+pcd_status pcd_graph_set_hub_part(pcd_graph *g, int32_t labels) {
+    if (!g) return PCD_ERR_INVALID_ARGUMENT;
+    if (labels < 1024 || labels > HUB_TABLE_CAP / 2)
+        return set_error(g->ctx, PCD_ERR_INVALID_ARGUMENT, "hub part size out of range [1024, 8192]");
+    g->hub_part_labels = labels;
+    return PCD_OK;
+}
+
 pcd_status pcd_graph_get_bins(pcd_graph *g, int32_t max_deg[7], int64_t counts[8]) {
     if (!g) return PCD_ERR_INVALID_ARGUMENT;
     for (int i = 0; i < 7; ++i)

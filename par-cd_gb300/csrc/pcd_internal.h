@@ -108,6 +108,7 @@ struct pcd_graph {
     // keys, labels and (position, label) buckets of the row being refined)
     int32_t *hub_scratch = nullptr;
     int32_t hub_blocks = 0;
+    int32_t hub_part_labels = 6144;  // distinct labels per hash part (pcd_graph_set_hub_part)
     size_t hub_bytes = 0;
     size_t dev_bytes = 0;             // device memory held through dev_alloc and the hub slices
     // degree bins

@@ -1630,7 +1630,7 @@ static int launch_bins_rule(pcd_graph *g, const SweepArgs &a, const R &rule, cud
         const size_t smem = 3ull * cap * sizeof(int32_t);
         cudaFuncSetAttribute(k_prop_hub_parts<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_prop_hub_parts<R><<<cap_grid(c, g->hub_blocks), 1024, smem, s_hub>>>(
-            a, rule, L + g->bin_off[BIN_HUB], c, cap, HUB_PART_LABELS, g->hub_scratch, hub_stride(g->max_deg),
+            a, rule, L + g->bin_off[BIN_HUB], c, cap, g->hub_part_labels, g->hub_scratch, hub_stride(g->max_deg),
             g->max_deg);
         ++launches;
         prof_mark(g->ctx, "sweep.hub", s_hub);

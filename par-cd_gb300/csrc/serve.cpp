@@ -56,6 +56,18 @@ struct Request {
     int32_t iterations = 0;
     int64_t batch_graphs = 0;
     int32_t cls = 0;  // size class: 0 small, 1 medium, 2 large (runs alone)
+    pcd_rand seeds{};  // the reference driver's rand() stream after the singleton partition's n draws
+};
+
+// A graph's place in a continuously running batch: its own iteration count,
+// previous score and seed stream, and its labels across batch rebuilds.
+struct Slot {
+    std::shared_ptr<Request> r;
+    int32_t it = 0;
+    double prev = 0.0;
+    bool fresh = true;   // still at its singleton start
+    bool gone = false;   // returned; still in the device batch until the next rebuild
+    std::vector<int32_t> labels;
 };
 
 bool same_schedule(const pcd_schedule &a, const pcd_schedule &b) {
@@ -101,7 +113,252 @@ struct pcd_server {
     void worker_main();
     bool take_batch(std::vector<std::shared_ptr<Request>> &batch, int64_t &bytes);
     void run_batch(pcd_ctx *ctx, std::vector<std::shared_ptr<Request>> &batch, int64_t bytes);
+    void run_continuous(pcd_ctx *ctx, std::vector<std::shared_ptr<Request>> &batch, int64_t bytes);
+    // requests of `like`'s schedule and size class that fit beside `held`
+    // (caps, HBM budget); removed from the queue.  Caller holds `mu`.
+    std::vector<std::shared_ptr<Request>> admit(const std::vector<std::shared_ptr<Request>> &held,
+                                                const Request &like);
+    void finish(Request &r, pcd_status st, Clock::time_point t_done, int64_t batch_graphs);
 };
+
+std::vector<std::shared_ptr<Request>> pcd_server::admit(const std::vector<std::shared_ptr<Request>> &held,
+                                                        const Request &like) {
+    std::vector<std::shared_ptr<Request>> out;
+    const int32_t cap = like.cls == 2 ? 1 : cfg.max_batch_graphs;
+    if ((int32_t)held.size() >= cap || queue.empty()) return out;
+    int64_t edges = 0;
+    for (const auto &r : held) edges += 2ll * r->m;
+    std::vector<std::shared_ptr<Request>> trial = held;
+    const int64_t others = in_flight - estimate(held);  // what the other batches hold
+    for (const auto &r : queue) {
+        if ((int32_t)trial.size() >= cap) break;
+        if (r->cls != like.cls || !same_schedule(r->sched, like.sched)) continue;
+        if (edges + 2ll * r->m > cfg.max_batch_edges) break;
+        trial.push_back(r);
+        if (estimate(trial) > cfg.hbm_budget_bytes - others) {
+            trial.pop_back();
+            break;
+        }
+        edges += 2ll * r->m;
+        out.push_back(r);
+    }
+    if (!out.empty()) {
+        std::deque<std::shared_ptr<Request>> rest;
+        size_t j = 0;
+        for (const auto &r : queue) {
+            if (j < out.size() && r == out[j])
+                ++j;
+            else
+                rest.push_back(r);
+        }
+        queue.swap(rest);
+        stats.queue_len = (int64_t)queue.size();
+    }
+    return out;
+}
+
+void pcd_server::finish(Request &r, pcd_status st, Clock::time_point t_done, int64_t batch_graphs) {
+    r.status = st;
+    r.t_done = t_done;
+    r.batch_graphs = batch_graphs;
+    if (st == PCD_OK)
+        ++stats.completed;
+    else
+        ++stats.failed;
+    std::vector<int32_t>().swap(r.indices);
+    std::vector<int32_t>().swap(r.adj);
+    r.done = true;
+}
+
+// Continuous batching: the batch runs the driver loop (src/main.cpp:226-266)
+// iteration by iteration on the host, every graph with its own iteration
+// count, previous score and seed stream: compress and score the batch, stop
+// test per graph, then one propagation or merge step of the whole batch with
+// each graph's next seed.  A graph whose schedule ends is returned at once;
+// at an iteration boundary the batch is rebuilt without the returned graphs
+// and with queued requests of the same schedule and size class (new graphs
+// start from singletons at their own iteration 0; under -s 2 they join only
+// when the batch's next step is a propagation, so that every graph of a
+// batch takes the same kind of step).  Each graph's labels, scores and
+// iteration count are exactly those of running it alone.
+void pcd_server::run_continuous(pcd_ctx *ctx, std::vector<std::shared_ptr<Request>> &batch, int64_t bytes) {
+    const pcd_schedule sched = batch.front()->sched;
+    const int32_t cap_it = sched.n_iter >= 0 ? sched.n_iter : 1000;  // threshold mode stops at 1000 iterations
+    std::vector<Slot> slots;
+    const auto t_start = Clock::now();
+    for (auto &r : batch) {
+        Slot sl;
+        sl.r = r;
+        r->t_start = t_start;
+        slots.push_back(std::move(sl));
+    }
+    int64_t held_bytes = bytes;  // this batch's share of in_flight
+    pcd_graph *b = nullptr;
+    bool rebuild = true;
+    pcd_status st = PCD_OK;
+    std::vector<int32_t> voff, all_labels;
+    std::vector<double> scores;
+    auto free_batch = [&]() {
+        if (!b) return;
+        int64_t held = 0;
+        pcd_graph_device_bytes(b, &held);
+        pcd_graph_free(b);
+        b = nullptr;
+        std::lock_guard<std::mutex> lock(mu);
+        stats.bytes_measured_peak = std::max(stats.bytes_measured_peak, held);
+        if (held > held_bytes) ++stats.estimate_exceeded;
+    };
+    while (st == PCD_OK) {
+        if (rebuild) {  // pack the graphs still running (returned ones leave here)
+            free_batch();
+            slots.erase(std::remove_if(slots.begin(), slots.end(), [](const Slot &x) { return x.gone; }),
+                        slots.end());
+            if (slots.empty()) break;
+            const int32_t G = (int32_t)slots.size();
+            voff.assign((size_t)G + 1, 0);
+            int64_t nnz = 0;
+            for (int32_t i = 0; i < G; ++i) {
+                voff[(size_t)i + 1] = voff[(size_t)i] + slots[(size_t)i].r->n;
+                nnz += 2ll * slots[(size_t)i].r->m;
+            }
+            const int32_t N = voff[(size_t)G];
+            std::vector<int32_t> ind((size_t)N + 1), adj((size_t)std::max<int64_t>(nnz, 1)), lab((size_t)N);
+            int64_t e0 = 0;
+            for (int32_t i = 0; i < G; ++i) {
+                const Slot &sl = slots[(size_t)i];
+                const Request &r = *sl.r;
+                for (int32_t v = 0; v < r.n; ++v) {
+                    ind[(size_t)voff[(size_t)i] + v] = (int32_t)(e0 + r.indices[(size_t)v]);
+                    lab[(size_t)voff[(size_t)i] + v] = sl.fresh ? v : sl.labels[(size_t)v];
+                }
+                if (r.m) std::memcpy(adj.data() + e0, r.adj.data(), sizeof(int32_t) * 2 * (size_t)r.m);
+                e0 += 2ll * r.m;
+            }
+            ind[(size_t)N] = (int32_t)e0;
+            st = pcd_batch_load(ctx, G, voff.data(), ind.data(), adj.data(), &b);
+            if (st == PCD_OK) st = pcd_batch_labels_set(b, lab.data());
+            if (st != PCD_OK) break;
+            rebuild = false;
+        }
+        const int32_t G = (int32_t)slots.size();
+        scores.assign((size_t)G, 0.0);
+        st = pcd_batch_score(b, &sched.rule, scores.data());
+        if (st != PCD_OK) break;
+        // the reference's stop test (src/main.cpp:241-242), per graph
+        std::vector<int32_t> fin;
+        int32_t live = 0, step_it = 0;
+        for (int32_t i = 0; i < G; ++i) {
+            const Slot &sl = slots[(size_t)i];
+            if (sl.gone) continue;
+            const double sc = scores[(size_t)i];
+            const bool done = sched.n_iter != -1 ? sl.it >= sched.n_iter
+                                                 : ((sl.prev > 0 && sc > 0 && sc / sl.prev - 1 <= sched.threshold) ||
+                                                    sl.it >= cap_it - 1);
+            if (done) {
+                fin.push_back(i);
+            } else {
+                ++live;
+                step_it = sl.it;  // every live graph of the batch has the same parity
+            }
+        }
+        bool have_labels = false;
+        if (!fin.empty()) {  // return finished graphs now
+            all_labels.assign((size_t)voff[(size_t)G], 0);
+            st = pcd_batch_labels_get(b, all_labels.data());
+            if (st != PCD_OK) break;
+            have_labels = true;
+            const auto t_done = Clock::now();
+            std::lock_guard<std::mutex> lock(mu);
+            for (int32_t i : fin) {
+                Slot &sl = slots[(size_t)i];
+                Request &r = *sl.r;
+                r.labels.assign(all_labels.begin() + voff[(size_t)i], all_labels.begin() + voff[(size_t)i + 1]);
+                r.score = scores[(size_t)i];
+                r.iterations = sl.it;
+                if (live > 0) ++stats.released_early;
+                finish(r, PCD_OK, t_done, G);
+                sl.gone = true;
+            }
+            cv_done.notify_all();
+            cv_work.notify_all();
+        }
+        // queued requests of this schedule and size class join between
+        // iterations (under -s 2 only before a propagation step)
+        std::vector<std::shared_ptr<Request>> joined;
+        const bool prop_next = sched.strategy == 0 || (sched.strategy == 2 && step_it % 2 == 0);
+        if (live > 0 && (sched.strategy != 2 || prop_next)) {
+            std::lock_guard<std::mutex> lock(mu);
+            std::vector<std::shared_ptr<Request>> held;
+            for (const Slot &sl : slots)
+                if (!sl.gone) held.push_back(sl.r);
+            joined = admit(held, *held.front());
+            std::vector<std::shared_ptr<Request>> now = held;
+            now.insert(now.end(), joined.begin(), joined.end());
+            const int64_t est = estimate(now);
+            in_flight += est - held_bytes;
+            held_bytes = est;
+            stats.bytes_in_flight = in_flight;
+            stats.bytes_peak = std::max(stats.bytes_peak, in_flight);
+            stats.admitted_running += (int64_t)joined.size();
+            stats.batched_graphs += (int64_t)joined.size();
+        }
+        if (live == 0) break;
+        int32_t gone = 0;
+        for (const Slot &sl : slots) gone += sl.gone ? 1 : 0;
+        if (!joined.empty() || 4 * gone >= G) {
+            // rebuild: running graphs keep their labels, newcomers start from
+            // singletons; the next pass scores and stop-tests everyone (the
+            // same outcome again for the running graphs)
+            if (!have_labels) {
+                all_labels.assign((size_t)voff[(size_t)G], 0);
+                st = pcd_batch_labels_get(b, all_labels.data());
+                if (st != PCD_OK) break;
+            }
+            for (int32_t i = 0; i < G; ++i) {
+                Slot &sl = slots[(size_t)i];
+                if (sl.gone) continue;
+                sl.labels.assign(all_labels.begin() + voff[(size_t)i], all_labels.begin() + voff[(size_t)i + 1]);
+                sl.fresh = false;
+            }
+            const auto t_join = Clock::now();
+            for (auto &r : joined) {
+                Slot sl;
+                sl.r = r;
+                r->t_start = t_join;
+                slots.push_back(std::move(sl));
+            }
+            rebuild = true;
+            continue;
+        }
+        // one step of the batch, every live graph with its own next seed
+        // (returned graphs still in the batch step too; their results are unused)
+        std::vector<uint32_t> seeds((size_t)G, 0u);
+        for (int32_t i = 0; i < G; ++i)
+            if (!slots[(size_t)i].gone) seeds[(size_t)i] = (uint32_t)pcd_rand_next(&slots[(size_t)i].r->seeds);
+        const bool merge = sched.strategy == 1 || (sched.strategy == 2 && step_it % 2 == 1);
+        st = merge ? pcd_batch_merge(b, &sched.rule, sched.rounds, seeds.data())
+                   : pcd_batch_refine(b, &sched.rule, sched.frac, seeds.data());
+        if (st != PCD_OK) break;
+        for (int32_t i = 0; i < G; ++i) {
+            Slot &sl = slots[(size_t)i];
+            if (sl.gone) continue;
+            sl.prev = scores[(size_t)i];
+            ++sl.it;
+        }
+    }
+    free_batch();
+    std::lock_guard<std::mutex> lock(mu);
+    for (Slot &sl : slots)
+        if (!sl.gone) finish(*sl.r, st == PCD_OK ? PCD_ERR_CUDA : st, Clock::now(), (int64_t)slots.size());
+    if (batch.front()->cls > 0) --big_in_flight;
+    in_flight -= held_bytes;
+    stats.bytes_in_flight = in_flight;
+    ++stats.batches;
+    stats.batched_graphs += (int64_t)batch.size();
+    cv_done.notify_all();
+    cv_work.notify_all();
+}
+
 
 // Forms the next batch, or returns false when stopping with an empty queue.
 // Requests too large for the whole budget fail here.  A batch holds one size
@@ -280,7 +537,10 @@ void pcd_server::worker_main() {
         cudaStream_t want = s_hi ? (batch.front()->cls == 0 ? s_hi : s_lo) : nullptr;
         if (want != cur && pcd_set_stream(ctx, want) == PCD_OK) cur = want;
         ctx->grid_scale = batch.front()->cls == 0 ? 1 : 8;  // long runs release SMs block by block
-        run_batch(ctx, batch, bytes);
+        if (cfg.continuous)
+            run_continuous(ctx, batch, bytes);
+        else
+            run_batch(ctx, batch, bytes);
     }
     pcd_set_stream(ctx, nullptr);
     if (s_hi) cudaStreamDestroy(s_hi);
@@ -352,6 +612,10 @@ pcd_status pcd_serve_submit(pcd_server *s, int32_t n, int32_t m, const int32_t *
     r->cls = 2ll * m <= s->cfg.small_graph_edges ? 0 : (2ll * m <= s->cfg.large_graph_edges ? 1 : 2);
     r->indices.assign(indices, indices + n + 1);
     r->adj.assign(adj, adj + 2 * (size_t)m);
+    // the driver's rand() stream: create_singleton_partition draws n values
+    // first, then every refinement draws its seed (src/framework.cpp:14-24)
+    pcd_rand_seed(&r->seeds, 1);
+    pcd_rand_skip(&r->seeds, n);
     {
         std::lock_guard<std::mutex> lock(s->mu);
         if (s->stopping) return PCD_ERR_INVALID_ARGUMENT;

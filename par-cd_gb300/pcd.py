@@ -54,13 +54,14 @@ class _Schedule(C.Structure):
 class _ServeConfig(C.Structure):
     _fields_ = [("device", C.c_int32), ("workers", C.c_int32), ("max_batch_graphs", C.c_int32),
                 ("max_batch_edges", C.c_int64), ("hbm_budget_bytes", C.c_int64), ("max_wait_ms", C.c_double),
-                ("use_cuda_graph", C.c_int32), ("small_graph_edges", C.c_int64), ("large_graph_edges", C.c_int64)]
+                ("use_cuda_graph", C.c_int32), ("small_graph_edges", C.c_int64), ("large_graph_edges", C.c_int64),
+                ("continuous", C.c_int32)]
 
 
 class _ServeStats(C.Structure):
     _fields_ = [(nm, C.c_int64) for nm in ("submitted", "completed", "failed", "batches", "batched_graphs",
                                            "queue_len", "bytes_in_flight", "bytes_peak", "bytes_measured_peak",
-                                           "estimate_exceeded")]
+                                           "estimate_exceeded", "admitted_running", "released_early")]
 
 
 class _ServeTiming(C.Structure):
@@ -98,6 +99,7 @@ def _load() -> C.CDLL:
         "pcd_profile_enable": ([vp, i32], i32),
         "pcd_graph_set_bins": ([vp, C.POINTER(i32)], i32),
         "pcd_graph_get_bins": ([vp, C.POINTER(i32), C.POINTER(i64)], i32),
+        "pcd_graph_set_hub_part": ([vp, i32], i32),
         "pcd_profile_read": ([vp, C.POINTER(C.c_char_p), C.POINTER(dbl), i32], i32),
         "pcd_batch_load": ([vp, i32, vp, vp, vp, C.POINTER(vp)], i32),
         "pcd_batch_load_device": ([vp, i32, vp, vp, vp, C.POINTER(vp)], i32),
@@ -370,6 +372,10 @@ class Graph:
     def set_bins(self, max_deg):
         arr = (C.c_int32 * 7)(*[int(x) for x in max_deg])
         self.ctx._check(LIB.pcd_graph_set_bins(self.h, arr))
+
+    def set_hub_part(self, labels: int):
+        """Distinct labels per hash part of the hub kernel."""
+        self.ctx._check(LIB.pcd_graph_set_hub_part(self.h, int(labels)))
 
     def get_bins(self):
         md = (C.c_int32 * 7)()
@@ -664,6 +670,19 @@ class Batch:
         self.ctx._check(LIB.pcd_batch_compress(self.h, _ptr(k)))
         return k
 
+    def set_bins(self, max_deg):
+        arr = (C.c_int32 * 7)(*[int(x) for x in max_deg])
+        self.ctx._check(LIB.pcd_graph_set_bins(self.h, arr))
+
+    def set_hub_part(self, labels: int):
+        self.ctx._check(LIB.pcd_graph_set_hub_part(self.h, int(labels)))
+
+    def get_bins(self):
+        md = (C.c_int32 * 7)()
+        cnt = (C.c_int64 * 8)()
+        self.ctx._check(LIB.pcd_graph_get_bins(self.h, md, cnt))
+        return list(md), list(cnt)
+
     def stats(self):
         """Per-graph statistics: a list of (sizes, int_volume, ext_volume),
         graph g's communities numbered from 0 as in that graph alone."""
@@ -730,9 +749,10 @@ class Server:
 
     def __init__(self, device: int = 0, workers: int = 2, max_batch_graphs: int = 256,
                  max_batch_edges: int = 1 << 28, hbm_budget_bytes: int = 150 * 10**9, max_wait_ms: float = 2.0,
-                 cuda_graph: bool = False, small_graph_edges: int = 1 << 20, large_graph_edges: int = 1 << 24):
+                 cuda_graph: bool = False, small_graph_edges: int = 1 << 20, large_graph_edges: int = 1 << 24,
+                 continuous: bool = True):
         cfg = _ServeConfig(device, workers, max_batch_graphs, max_batch_edges, hbm_budget_bytes, max_wait_ms,
-                           1 if cuda_graph else 0, small_graph_edges, large_graph_edges)
+                           1 if cuda_graph else 0, small_graph_edges, large_graph_edges, 1 if continuous else 0)
         self.h = C.c_void_p()
         st = LIB.pcd_serve_start(C.byref(cfg), C.byref(self.h))
         if st:

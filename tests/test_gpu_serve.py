@@ -2,6 +2,7 @@
 through the single-graph path, whatever it was batched with, and batches are
 admitted only within the device-memory budget."""
 import threading
+import time
 
 import numpy as np
 import pytest
@@ -46,14 +47,15 @@ def _alone(ctx, ind, adj, sched):
     return res
 
 
-def test_served_results_equal_each_graph_alone(ctx):
+@pytest.mark.parametrize("continuous", [True, False], ids=["continuous", "whole-batch"])
+def test_served_results_equal_each_graph_alone(ctx, continuous):
     import pcd
 
     gs = _graphs()
     reqs = [(i, SCHEDULES[(i * 7 + j) % len(SCHEDULES)]) for j in range(3) for i in range(len(gs))]
     rng = np.random.default_rng(3)
     rng.shuffle(reqs)
-    with pcd.Server(workers=3, max_batch_graphs=8, max_wait_ms=1.0) as srv:
+    with pcd.Server(workers=3, max_batch_graphs=8, max_wait_ms=1.0, continuous=continuous) as srv:
         tickets = []
         # submitted from two threads at once, as a server front end would
         lock = threading.Lock()
@@ -79,6 +81,35 @@ def test_served_results_equal_each_graph_alone(ctx):
         assert np.array_equal(res.labels, ref.labels), (i, sched)
         assert res.score == ref.score and res.iterations == ref.iterations, (i, sched)
         assert res.latency_ms >= res.queue_ms >= 0.0
+
+
+@pytest.mark.parametrize("strategy", [0, 2])
+def test_requests_join_and_leave_a_running_batch(ctx, strategy):
+    """Continuous batching: requests that arrive while a batch runs join it
+    between iterations, graphs whose schedule ends return while the others
+    run on, and every result is the graph's result alone."""
+    import pcd
+
+    gs = _graphs()
+    sched = ("mod", strategy, 1.0, 1, 60, 0.0)
+    metric, _, frac, rounds, n_iter, thr = sched
+    first = len(gs) - 2  # rmat12: the batch the later requests join
+    order = [first] + list(range(8))
+    with pcd.Server(workers=1, max_batch_graphs=16, max_wait_ms=0.0) as srv:
+        tickets = []
+        for k, i in enumerate(order):
+            tickets.append((srv.submit(gs[i][0], gs[i][1], pcd.parse_metric(metric), strategy, frac, rounds,
+                                       n_iter, thr), i))
+            time.sleep(0.02 if k == 0 else 0.004)
+        results = [(srv.wait(t), i) for t, i in tickets]
+        st = srv.stats()
+    assert st["completed"] == len(order) and st["failed"] == 0
+    assert st["admitted_running"] > 0, st
+    assert st["released_early"] > 0, st
+    for res, i in results:
+        ref = _alone(ctx, gs[i][0], gs[i][1], sched)
+        assert np.array_equal(res.labels, ref.labels), i
+        assert res.score == ref.score and res.iterations == ref.iterations, i
 
 
 def test_admission_respects_the_budget_and_rejects_oversized_requests():
