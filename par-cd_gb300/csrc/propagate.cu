@@ -259,6 +259,47 @@ __device__ __forceinline__ K kmax(K a, K b) {
     return a > b ? a : b;
 }
 
+// Per-warp results of a block, combined by every warp from one shared load
+// per lane and a shuffle scan (rather than every thread reading all NW
+// entries).  carry: the maximum of `init` and the maxima of the warps before
+// `wid`; mreal: the maximum over all warps.
+template <class PK, int NW>
+__device__ __forceinline__ void warp_carry_in(const typename PK::K *s_agg, int wid, int lane, typename PK::K &carry,
+                                              typename PK::K &mreal) {
+    static_assert(NW <= 32, "one lane per warp");
+    using K = typename PK::K;
+    K inc = lane < NW ? s_agg[lane] : PK::ident();
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const K y = __shfl_up_sync(FULL, inc, o);
+        if (lane >= o) inc = kmax(inc, y);
+    }
+    mreal = __shfl_sync(FULL, inc, 31);
+    const K before = __shfl_sync(FULL, inc, wid > 0 ? wid - 1 : 0);
+    carry = wid > 0 ? kmax(PK::init(), before) : PK::init();
+}
+
+// tt: the sum of the warps' tie counts (mod 2^32); nf: the final-level
+// candidates of all warps; before: those of the warps before `wid`; hw: the
+// first warp with one (-1: none).
+template <int NW>
+__device__ __forceinline__ void warp_totals(const uint32_t *s_t, const int32_t *s_nfin, int wid, int lane,
+                                            uint32_t &tt, int32_t &nf, int32_t &before, int32_t &hw) {
+    const uint32_t t = lane < NW ? s_t[lane] : 0u;
+    const int32_t c = lane < NW ? s_nfin[lane] : 0;
+    tt = __reduce_add_sync(FULL, t);
+    int32_t inc = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int32_t y = __shfl_up_sync(FULL, inc, o);
+        if (lane >= o) inc += y;
+    }
+    nf = __shfl_sync(FULL, inc, 31);
+    before = __shfl_sync(FULL, inc - c, wid);
+    const unsigned nz = __ballot_sync(FULL, c > 0);
+    hw = nz ? __ffs(nz) - 1 : -1;
+}
+
 // ---------------------------------------------------------------------------
 // warp per vertex (deg <= WCAP): adjacency in chunks of 32 in order; lanes
 // holding the same label are merged with match_any and the lowest lane (the
@@ -408,7 +449,13 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
         const int32_t holder = has ? ties[0] : -1;
         const int32_t r = has ? nfin - 1 : 0;
         int32_t dec = DEC_AMBIGUOUS;
-        if (!amb) dec = vr.decide(has ? PK::raw_level(mreal) : R::initial(), has, v, d, curr, curr_freq, a.cm);
+        if constexpr (R::kExactInt) {  // integer decision: cheaper in every lane than a broadcast
+            if (!amb) dec = vr.decide(has ? PK::raw_level(mreal) : R::initial(), has, v, d, curr, curr_freq, a.cm);
+        } else {  // FP64 leave gain: one lane evaluates it, the warp takes its decision
+            if (!amb && lane == 0)
+                dec = vr.decide(has ? PK::raw_level(mreal) : R::initial(), has, v, d, curr, curr_freq, a.cm);
+            dec = __shfl_sync(FULL, dec, 0);
+        }
         if (dec == DEC_AMBIGUOUS) {
             if (lane == 0) push_ambiguous(a, v, d);
             continue;
@@ -887,13 +934,8 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
         for (int o = 16; o; o >>= 1) wmax = kmax(wmax, __shfl_xor_sync(FULL, wmax, o));
         if (lane == 0) s_agg[wid] = wmax;
         __syncthreads();
-        K carry = PK::init(), mreal = PK::ident();
-#pragma unroll
-        for (int w2 = 0; w2 < NW; ++w2) {
-            const K x = s_agg[w2];
-            if (w2 < wid) carry = kmax(carry, x);
-            mreal = kmax(mreal, x);
-        }
+        K carry, mreal;
+        warp_carry_in<PK, NW>(s_agg, wid, lane, carry, mreal);
         const auto lfin = PK::level(kmax(PK::init(), mreal));
         // S: ordered ties, final-level candidates, table clearing
         uint32_t t = 0;
@@ -936,16 +978,9 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
         }
         __syncthreads();
         // every warp: the same totals and decision
-        uint32_t tt = 0;
-        int32_t nf = 0, before = 0, hw = -1;
-#pragma unroll
-        for (int w2 = 0; w2 < NW; ++w2) {
-            const int32_t c = s_nfin[w2];
-            tt += s_t[w2];
-            if (w2 < wid) before += c;
-            if (hw < 0 && c > 0) hw = w2;
-            nf += c;
-        }
+        uint32_t tt;
+        int32_t nf, before, hw;
+        warp_totals<NW>(s_t, s_nfin, wid, lane, tt, nf, before, hw);
         const bool has_best = mreal != PK::ident() && PK::level(mreal) > PK::level(PK::init());
         // the holder is the first final-level candidate: entry 0 of the first
         // range that has one (that range's warp has not overwritten it: only
@@ -953,9 +988,17 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
         const int32_t holder = has_best ? pos_slot[hw * span] : -1;
         const int32_t r = has_best ? nf - 1 : 0;
         int32_t dec = DEC_AMBIGUOUS;
-        if (!s_amb) {
-            const typename R::Key best = has_best ? PK::raw_level(mreal) : R::initial();
-            dec = vr.decide(best, has_best, v, d, curr, s_curr_freq, a.cm);
+        if constexpr (R::kExactInt) {  // integer decision: cheaper in every lane than a broadcast
+            if (!s_amb) {
+                const typename R::Key best = has_best ? PK::raw_level(mreal) : R::initial();
+                dec = vr.decide(best, has_best, v, d, curr, s_curr_freq, a.cm);
+            }
+        } else {  // FP64 leave gain: one lane per warp evaluates it
+            if (!s_amb && lane == 0) {
+                const typename R::Key best = has_best ? PK::raw_level(mreal) : R::initial();
+                dec = vr.decide(best, has_best, v, d, curr, s_curr_freq, a.cm);
+            }
+            dec = __shfl_sync(FULL, dec, 0);
         }
         const bool rec = dec == DEC_MOVE && r > 0;
         if (tid == 0) {
@@ -1160,12 +1203,8 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
         for (int o = 16; o; o >>= 1) wmax = kmax(wmax, __shfl_xor_sync(FULL, wmax, o));
         if (lane == 0) s_agg[wid] = wmax;
         __syncthreads();
-        K carry = PK::init(), mreal = PK::ident();
-        for (int w2 = 0; w2 < NW; ++w2) {
-            const K x = s_agg[w2];
-            if (w2 < wid) carry = kmax(carry, x);
-            mreal = kmax(mreal, x);
-        }
+        K carry, mreal;
+        warp_carry_in<PK, NW>(s_agg, wid, lane, carry, mreal);
         const auto lfin = PK::level(kmax(PK::init(), mreal));
         uint32_t t = 0;
         int32_t nfin = 0;
@@ -1203,22 +1242,24 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
             if (amb) s_amb = 1;
         }
         __syncthreads();
-        uint32_t tt = 0;
-        int32_t nf = 0, before = 0, hw = -1;
-        for (int w2 = 0; w2 < NW; ++w2) {
-            const int32_t c = s_nfin[w2];
-            tt += s_t[w2];
-            if (w2 < wid) before += c;
-            if (hw < 0 && c > 0) hw = w2;
-            nf += c;
-        }
+        uint32_t tt;
+        int32_t nf, before, hw;
+        warp_totals<NW>(s_t, s_nfin, wid, lane, tt, nf, before, hw);
         const bool has_best = mreal != PK::ident() && PK::level(mreal) > PK::level(PK::init());
         const int32_t holder = has_best && hw >= 0 ? pos_lab[hw * span] : -1;
         const int32_t r = has_best ? nf - 1 : 0;
         int32_t dec = DEC_AMBIGUOUS;
-        if (!s_amb) {
-            const typename R::Key best = has_best ? PK::raw_level(mreal) : R::initial();
-            dec = vr.decide(best, has_best, v, d, curr, s_curr_freq, a.cm);
+        if constexpr (R::kExactInt) {  // integer decision: cheaper in every lane than a broadcast
+            if (!s_amb) {
+                const typename R::Key best = has_best ? PK::raw_level(mreal) : R::initial();
+                dec = vr.decide(best, has_best, v, d, curr, s_curr_freq, a.cm);
+            }
+        } else {  // FP64 leave gain: one lane per warp evaluates it
+            if (!s_amb && lane == 0) {
+                const typename R::Key best = has_best ? PK::raw_level(mreal) : R::initial();
+                dec = vr.decide(best, has_best, v, d, curr, s_curr_freq, a.cm);
+            }
+            dec = __shfl_sync(FULL, dec, 0);
         }
         const bool rec = dec == DEC_MOVE && r > 0;
         if (tid == 0) {
