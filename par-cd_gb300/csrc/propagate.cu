@@ -1101,11 +1101,12 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                 l[u] = p < d ? a.g.adj[b + p] : -1;
             }
 #pragma unroll
+            for (int u = 0; u < 4; ++u) l[u] = l[u] >= 0 ? a.labels[l[u]] : -1;  // four gathers in flight
+#pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int32_t p = p0 + u * BT + tid;
                 int32_t pt = -1 - lane;
                 if (p < d) {
-                    l[u] = a.labels[l[u]];
                     pos_lab[p] = l[u];
                     pos_key[p] = PK::ident();
                     pt = (int32_t)hub_part(hash_label(l[u]), parts);
@@ -1148,11 +1149,17 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
             const int32_t i0 = s_start[part], i1 = s_start[part + 1];
             int32_t ts = 64;
             while (ts < 2 * (i1 - i0) && ts < table_cap) ts <<= 1;
-            // histogram of this part's labels
-            for (int32_t j0 = i0; j0 < i1; j0 += BT) {
-                const int32_t j = j0 + tid;
-                const int2 e = j < i1 ? bucket[j] : make_int2(-1, -2);
-                const int32_t p = e.x, l = e.y;
+            // histogram of this part's labels, four bucket entries in flight per thread
+            for (int32_t j0 = i0; j0 < i1; j0 += 4 * BT) {
+              int2 eq[4];
+#pragma unroll
+              for (int u = 0; u < 4; ++u) {
+                  const int32_t j = j0 + u * BT + tid;
+                  eq[u] = j < i1 ? bucket[j] : make_int2(-1, -2);
+              }
+#pragma unroll
+              for (int u = 0; u < 4; ++u) {
+                const int32_t p = eq[u].x, l = eq[u].y;
                 if (p >= 0) {
                     uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
                     int32_t probes = 0;
@@ -1172,24 +1179,42 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                         atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);  // a part overfilled the table
                     }
                 }
+              }
             }
             __syncthreads();
-            // slot walk: each label's key at its first position; the slot is cleared
-            for (int32_t i = tid; i < ts; i += BT) {
-                const int32_t l = keys[i];
-                if (l != -1) {
-                    const int32_t k = cnts[i];
-                    const uint32_t p = first[i];
-                    if (l == curr) {
-                        s_curr_freq = k;
-                    } else {
-                        Tag tag{0, 0};
-                        const typename R::Key raw = vr.join(v, d, l, k, a.cm, tag);
-                        if (R::usable(raw)) pos_key[p] = PK::make(raw, k);
+            // slot walk: each label's key at its first position; the slot is
+            // cleared.  Four slots per thread at a time, so that their
+            // community statistics gathers (in join) are in flight together.
+            for (int32_t i0 = tid; i0 < ts; i0 += 4 * BT) {
+                int32_t lw[4], kw[4];
+                uint32_t pw[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int32_t i = i0 + u * BT;
+                    lw[u] = i < ts ? keys[i] : -1;
+                    kw[u] = 0;
+                    pw[u] = 0;
+                    if (lw[u] != -1) {
+                        kw[u] = cnts[i];
+                        pw[u] = first[i];
+                        keys[i] = -1;
+                        cnts[i] = 0;
+                        first[i] = 0xffffffffu;
                     }
-                    keys[i] = -1;
-                    cnts[i] = 0;
-                    first[i] = 0xffffffffu;
+                }
+                typename R::Key raw[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    Tag tag{0, 0};
+                    raw[u] = lw[u] != -1 && lw[u] != curr ? vr.join(v, d, lw[u], kw[u], a.cm, tag) : R::identity();
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (lw[u] == -1) continue;
+                    if (lw[u] == curr)
+                        s_curr_freq = kw[u];
+                    else if (R::usable(raw[u]))
+                        pos_key[pw[u]] = PK::make(raw[u], kw[u]);
                 }
             }
             __syncthreads();
@@ -1210,30 +1235,40 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
         int32_t nfin = 0;
         bool amb = false;
         int32_t *fin_list = pos_lab + lo;  // entries already read are overwritten
-        for (int32_t base = lo; base < hi; base += 32) {
-            const int32_t p = base + lane;
-            const K key = p < hi ? pos_key[p] : PK::ident();
-            const bool cand = key != PK::ident();
-            const int32_t l = cand ? pos_lab[p] : -1;
-            __syncwarp();
-            const bool fin = cand && PK::level(key) == lfin;
-            const unsigned fm = __ballot_sync(FULL, fin);
-            if (fin) fin_list[nfin + __popc(fm & lanemask_lt())] = l;
-            nfin += __popc(fm);
-            if (!__any_sync(FULL, cand && PK::level(key) >= PK::level(carry))) continue;
-            K inc = key;
+        constexpr int UO = 4;  // 32-position steps whose loads are issued together
+        for (int32_t base0 = lo; base0 < hi; base0 += 32 * UO) {
+            K kq[UO];
+            int32_t lq[UO];
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const K y = __shfl_up_sync(FULL, inc, o);
-                if (lane >= o) inc = kmax(inc, y);
+            for (int u = 0; u < UO; ++u) {
+                const int32_t p = base0 + 32 * u + lane;
+                kq[u] = p < hi ? pos_key[p] : PK::ident();
+                lq[u] = p < hi ? pos_lab[p] : -1;
             }
-            K ex = __shfl_up_sync(FULL, inc, 1);
-            if (lane == 0) ex = PK::ident();
-            const K pre = kmax(carry, ex);
-            const bool tie = cand && PK::level(key) == PK::level(pre);
-            if (tie && PK::tie_ambiguous(key, pre)) amb = true;
-            t += __popc(__ballot_sync(FULL, tie));
-            carry = kmax(carry, __shfl_sync(FULL, inc, 31));
+            __syncwarp();  // these steps' labels are read before fin_list overwrites read entries
+#pragma unroll
+            for (int u = 0; u < UO; ++u) {
+                const K key = kq[u];
+                const bool cand = key != PK::ident();
+                const bool fin = cand && PK::level(key) == lfin;
+                const unsigned fm = __ballot_sync(FULL, fin);
+                if (fin) fin_list[nfin + __popc(fm & lanemask_lt())] = lq[u];
+                nfin += __popc(fm);
+                if (!__any_sync(FULL, cand && PK::level(key) >= PK::level(carry))) continue;
+                K inc = key;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const K y = __shfl_up_sync(FULL, inc, o);
+                    if (lane >= o) inc = kmax(inc, y);
+                }
+                K ex = __shfl_up_sync(FULL, inc, 1);
+                if (lane == 0) ex = PK::ident();
+                const K pre = kmax(carry, ex);
+                const bool tie = cand && PK::level(key) == PK::level(pre);
+                if (tie && PK::tie_ambiguous(key, pre)) amb = true;
+                t += __popc(__ballot_sync(FULL, tie));
+                carry = kmax(carry, __shfl_sync(FULL, inc, 31));
+            }
         }
         amb = __any_sync(FULL, amb);
         if (lane == 0) {
