@@ -115,21 +115,21 @@ struct pcd_server {
     void run_batch(pcd_ctx *ctx, std::vector<std::shared_ptr<Request>> &batch, int64_t bytes);
     void run_continuous(pcd_ctx *ctx, std::vector<std::shared_ptr<Request>> &batch, int64_t bytes);
     // requests of `like`'s schedule and size class that fit beside `held`
-    // (caps, HBM budget); removed from the queue.  Caller holds `mu`.
+    // (caps, HBM budget, with `others` bytes held by the other batches);
+    // removed from the queue.  Caller holds `mu`.
     std::vector<std::shared_ptr<Request>> admit(const std::vector<std::shared_ptr<Request>> &held,
-                                                const Request &like);
+                                                const Request &like, int64_t others);
     void finish(Request &r, pcd_status st, Clock::time_point t_done, int64_t batch_graphs);
 };
 
 std::vector<std::shared_ptr<Request>> pcd_server::admit(const std::vector<std::shared_ptr<Request>> &held,
-                                                        const Request &like) {
+                                                        const Request &like, int64_t others) {
     std::vector<std::shared_ptr<Request>> out;
     const int32_t cap = like.cls == 2 ? 1 : cfg.max_batch_graphs;
     if ((int32_t)held.size() >= cap || queue.empty()) return out;
     int64_t edges = 0;
     for (const auto &r : held) edges += 2ll * r->m;
     std::vector<std::shared_ptr<Request>> trial = held;
-    const int64_t others = in_flight - estimate(held);  // what the other batches hold
     for (const auto &r : queue) {
         if ((int32_t)trial.size() >= cap) break;
         if (r->cls != like.cls || !same_schedule(r->sched, like.sched)) continue;
@@ -286,25 +286,28 @@ void pcd_server::run_continuous(pcd_ctx *ctx, std::vector<std::shared_ptr<Reques
         // iterations (under -s 2 only before a propagation step)
         std::vector<std::shared_ptr<Request>> joined;
         const bool prop_next = sched.strategy == 0 || (sched.strategy == 2 && step_it % 2 == 0);
+        int32_t gone = 0;
+        for (const Slot &sl : slots) gone += sl.gone ? 1 : 0;
         if (live > 0 && (sched.strategy != 2 || prop_next)) {
             std::lock_guard<std::mutex> lock(mu);
             std::vector<std::shared_ptr<Request>> held;
             for (const Slot &sl : slots)
                 if (!sl.gone) held.push_back(sl.r);
-            joined = admit(held, *held.front());
-            std::vector<std::shared_ptr<Request>> now = held;
-            now.insert(now.end(), joined.begin(), joined.end());
-            const int64_t est = estimate(now);
-            in_flight += est - held_bytes;
-            held_bytes = est;
-            stats.bytes_in_flight = in_flight;
-            stats.bytes_peak = std::max(stats.bytes_peak, in_flight);
+            // the device batch holds held_bytes until it is rebuilt
+            joined = admit(held, *held.front(), in_flight - held_bytes);
+            if (!joined.empty() || 4 * gone >= G) {  // the batch is rebuilt below
+                std::vector<std::shared_ptr<Request>> now = held;
+                now.insert(now.end(), joined.begin(), joined.end());
+                const int64_t est = estimate(now);
+                in_flight += est - held_bytes;
+                held_bytes = est;
+                stats.bytes_in_flight = in_flight;
+                stats.bytes_peak = std::max(stats.bytes_peak, in_flight);
+            }
             stats.admitted_running += (int64_t)joined.size();
             stats.batched_graphs += (int64_t)joined.size();
         }
         if (live == 0) break;
-        int32_t gone = 0;
-        for (const Slot &sl : slots) gone += sl.gone ? 1 : 0;
         if (!joined.empty() || 4 * gone >= G) {
             // rebuild: running graphs keep their labels, newcomers start from
             // singletons; the next pass scores and stop-tests everyone (the

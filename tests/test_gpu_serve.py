@@ -106,6 +106,10 @@ def test_requests_join_and_leave_a_running_batch(ctx, strategy):
     assert st["completed"] == len(order) and st["failed"] == 0
     assert st["admitted_running"] > 0, st
     assert st["released_early"] > 0, st
+    # a batch is charged what its device copy holds, returned graphs included
+    # until the rebuild that drops them
+    assert st["estimate_exceeded"] == 0, st
+    assert 0 < st["bytes_measured_peak"] <= st["bytes_peak"], st
     for res, i in results:
         ref = _alone(ctx, gs[i][0], gs[i][1], sched)
         assert np.array_equal(res.labels, ref.labels), i
