@@ -192,7 +192,11 @@ void pcd_server::run_continuous(pcd_ctx *ctx, std::vector<std::shared_ptr<Reques
         r->t_start = t_start;
         slots.push_back(std::move(sl));
     }
-    int64_t held_bytes = bytes;  // this batch's share of in_flight
+    // held_bytes: this batch's share of in_flight.  It grows when requests
+    // join (reserved at admission) and shrinks only once the old device copy
+    // is freed.  batch_bytes: the estimate of the copy on the device now;
+    // next_bytes: the estimate of the copy the next rebuild loads.
+    int64_t held_bytes = bytes, batch_bytes = bytes, next_bytes = bytes;
     pcd_graph *b = nullptr;
     bool rebuild = true;
     pcd_status st = PCD_OK;
@@ -206,11 +210,19 @@ void pcd_server::run_continuous(pcd_ctx *ctx, std::vector<std::shared_ptr<Reques
         b = nullptr;
         std::lock_guard<std::mutex> lock(mu);
         stats.bytes_measured_peak = std::max(stats.bytes_measured_peak, held);
-        if (held > held_bytes) ++stats.estimate_exceeded;
+        if (held > batch_bytes) ++stats.estimate_exceeded;
     };
     while (st == PCD_OK) {
         if (rebuild) {  // pack the graphs still running (returned ones leave here)
             free_batch();
+            if (next_bytes < held_bytes) {  // the old copy is gone: release the difference
+                std::lock_guard<std::mutex> lock(mu);
+                in_flight -= held_bytes - next_bytes;
+                held_bytes = next_bytes;
+                stats.bytes_in_flight = in_flight;
+                cv_work.notify_all();
+            }
+            batch_bytes = next_bytes;
             slots.erase(std::remove_if(slots.begin(), slots.end(), [](const Slot &x) { return x.gone; }),
                         slots.end());
             if (slots.empty()) break;
@@ -288,21 +300,26 @@ void pcd_server::run_continuous(pcd_ctx *ctx, std::vector<std::shared_ptr<Reques
         const bool prop_next = sched.strategy == 0 || (sched.strategy == 2 && step_it % 2 == 0);
         int32_t gone = 0;
         for (const Slot &sl : slots) gone += sl.gone ? 1 : 0;
-        if (live > 0 && (sched.strategy != 2 || prop_next)) {
+        if (live > 0) {
             std::lock_guard<std::mutex> lock(mu);
             std::vector<std::shared_ptr<Request>> held;
             for (const Slot &sl : slots)
                 if (!sl.gone) held.push_back(sl.r);
-            // the device batch holds held_bytes until it is rebuilt
-            joined = admit(held, *held.front(), in_flight - held_bytes);
+            // the other batches hold in_flight - held_bytes; the copy of this
+            // one stays on the device until the rebuild below frees it, so a
+            // joining request is charged on top of held_bytes when the new
+            // estimate exceeds it
+            if (sched.strategy != 2 || prop_next) joined = admit(held, *held.front(), in_flight - held_bytes);
             if (!joined.empty() || 4 * gone >= G) {  // the batch is rebuilt below
                 std::vector<std::shared_ptr<Request>> now = held;
                 now.insert(now.end(), joined.begin(), joined.end());
-                const int64_t est = estimate(now);
-                in_flight += est - held_bytes;
-                held_bytes = est;
-                stats.bytes_in_flight = in_flight;
-                stats.bytes_peak = std::max(stats.bytes_peak, in_flight);
+                next_bytes = estimate(now);
+                if (next_bytes > held_bytes) {
+                    in_flight += next_bytes - held_bytes;
+                    held_bytes = next_bytes;
+                    stats.bytes_in_flight = in_flight;
+                    stats.bytes_peak = std::max(stats.bytes_peak, in_flight);
+                }
             }
             stats.admitted_running += (int64_t)joined.size();
             stats.batched_graphs += (int64_t)joined.size();
