@@ -1059,6 +1059,33 @@ def main():
                "ms_per_step": 1000.0 * sec / args.e2e_steps,
                "note": "each step: pcd_load_csr from pinned host CSR (validation, degree bins, buffers), "
                        "pcd_labels_set, pcd_refine, pcd_labels_get, pcd_graph_free"}
+        # where one more step's time goes: device spans of the load and of the
+        # refine call (CUDA events), host time of the calls around them
+        ctx.profile(True)
+        ph = {}
+        t0 = time.perf_counter()
+        g2 = pcd.Graph.from_host_ptr(ctx, n, m, h_ind.data_ptr(), h_adj.data_ptr())
+        ph["load (host)"] = time.perf_counter() - t0
+        for nm, ms in ctx.profile_read():
+            ph[nm] = ph.get(nm, 0.0) + ms / 1000.0
+        t0 = time.perf_counter()
+        g2.set_labels_ptr(h_lab.data_ptr())
+        ph["labels_set (host)"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        sweep.refine(g2, rule, seeds[0])
+        ctx.synchronize()
+        ph["refine (host)"] = time.perf_counter() - t0
+        for nm, ms in ctx.profile_read():
+            key = "refine." + nm if nm == "compress+stats" else "refine.sweep"
+            ph[key] = ph.get(key, 0.0) + ms / 1000.0
+        t0 = time.perf_counter()
+        g2.get_labels_ptr(h_out.data_ptr())
+        ph["labels_get (host)"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        g2.free()
+        ph["free (host)"] = time.perf_counter() - t0
+        ctx.profile(False)
+        e2e["phases_ms"] = {k: round(1000.0 * v, 3) for k, v in ph.items()}
 
     batched = batched_s2 = None
     if args.batch_graphs > 0:

@@ -191,8 +191,8 @@ pcd_status pcd_sweep_info_get(pcd_graph *g, pcd_sweep_info *info);
 
 /* Per-phase device timing (the reference's CudaTimer spans,
  * src/cuda-common.cuh:253-316): while enabled, pcd_refine / pcd_merge /
- * pcd_compress record CUDA events between their kernel groups on the
- * context's stream.  pcd_profile_read synchronises and writes up to `cap`
+ * pcd_compress / pcd_load_csr record CUDA events between their kernel groups
+ * on the context's stream.  pcd_profile_read synchronises and writes up to `cap`
  * (phase name, milliseconds) pairs of the most recent call; returns the number
  * of phases (or -1 on error).  Names are static strings. */
 pcd_status pcd_profile_enable(pcd_ctx *ctx, int32_t on);

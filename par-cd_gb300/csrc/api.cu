@@ -38,14 +38,6 @@ pcd_status dev_alloc(pcd_graph *g, void **p, size_t bytes) {
     return PCD_OK;
 }
 
-__global__ void k_degree_max(const int32_t *indices, int32_t n, int32_t *out) {
-    int32_t mx = 0;
-    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
-        mx = max(mx, indices[v + 1] - indices[v]);
-    mx = __reduce_max_sync(0xffffffffu, mx);
-    if ((threadIdx.x & 31) == 0) atomicMax(out, mx);
-}
-
 // one more event of the pool recorded on st; returns its index (-1 on failure)
 static int32_t prof_record(pcd_ctx *ctx, cudaStream_t st) {
     if (ctx->prof_used == ctx->prof_pool.size()) {
@@ -311,6 +303,8 @@ pcd_status pcd_destroy(pcd_ctx *ctx) {
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     for (auto &e : ctx->ev_join)
         if (e) cudaEventDestroy(e);
+    for (auto &e : ctx->ev_copy)
+        if (e) cudaEventDestroy(e);
     if (ctx->own_stream) {
         cudaStreamSynchronize(ctx->own_stream);
         cudaStreamDestroy(ctx->own_stream);
@@ -387,28 +381,10 @@ static pcd_status ensure_hub_scratch(pcd_graph *g) {
     return PCD_OK;
 }
 
-static pcd_status graph_setup(pcd_ctx *ctx, pcd_graph *g) {
+// Partition state and sweep scratch sized by n and 2m: allocated before the
+// copies, so that the side stream of graph_setup may use them.
+static pcd_status alloc_state(pcd_ctx *ctx, pcd_graph *g) {
     const int64_t n = g->n, nn = std::max<int64_t>(n, 1);
-    cudaStream_t st = ctx->stream;
-    // validation + max degree
-    int32_t *flag = nullptr;
-    TRY(dev_alloc(g, (void **)&flag, 2 * sizeof(int32_t)));
-    CK(cudaMemsetAsync(flag, 0, 2 * sizeof(int32_t), st), "memset");
-    if (n > 0) {
-        launch_validate(g->indices, g->adj, g->n, g->m, flag, st);
-        k_degree_max<<<std::max(1, std::min<int>((int)((n + 255) / 256), ctx->num_sms * 8)), 256, 0, st>>>(
-            g->indices, g->n, flag + 1);
-    }
-    int32_t h[2] = {0, 0};
-    CK(cudaMemcpyAsync(h, flag, sizeof h, cudaMemcpyDeviceToHost, st), "validate");
-    CK(cudaStreamSynchronize(st), "validate");
-    if (h[0]) {
-        char buf[128];
-        snprintf(buf, sizeof buf, "graph arrays are not a valid CSR (flags 0x%x: 1 span, 2 offsets, 4 rows)", h[0]);
-        return set_error(ctx, PCD_ERR_FORMAT, buf);
-    }
-    g->max_deg = h[1];
-    // partition state and sweep scratch
     TRY(dev_alloc(g, (void **)&g->labels, sizeof(int32_t) * nn));
     TRY(dev_alloc(g, (void **)&g->labels_alt, sizeof(int32_t) * nn));
     TRY(dev_alloc(g, (void **)&g->first, sizeof(int32_t) * nn));
@@ -433,6 +409,39 @@ static pcd_status graph_setup(pcd_ctx *ctx, pcd_graph *g) {
     TRY(dev_alloc(g, (void **)&g->d_score, 64));
     TRY(dev_alloc(g, (void **)&g->bin_list, sizeof(int32_t) * nn));
     g->h_ctr = ctx->h_ctr;  // pinned, one per context (calls on a context come from one thread)
+    return PCD_OK;
+}
+
+// After the row offsets have arrived, while the neighbour array is still in
+// flight on the context's stream in `nch` pieces ([cut[k], cut[k + 1]),
+// piece k complete at ctx->ev_copy[k]): on `side`, the offsets, the largest
+// degree, the degree classes, then the rows of each piece as it lands; on the
+// context's stream, behind the copy, the counters and the FP64 re-evaluation
+// tables.  `flag` holds two zeroed words.  The caller joins `side` back into
+// the context's stream.
+static pcd_status graph_setup(pcd_ctx *ctx, pcd_graph *g, int32_t *flag, cudaStream_t side, const int64_t *cut,
+                              int nch) {
+    const int64_t n = g->n;
+    cudaStream_t st = ctx->stream;
+    if (n > 0) launch_check_offsets(g->indices, g->n, g->m, flag, side);
+    int32_t h[2] = {0, 0};
+    CK(cudaMemcpyAsync(h, flag, sizeof h, cudaMemcpyDeviceToHost, side), "validate");
+    CK(cudaStreamSynchronize(side), "validate");
+    if (h[0]) {
+        char buf[128];
+        snprintf(buf, sizeof buf, "graph arrays are not a valid CSR (flags 0x%x: 1 span, 2 offsets, 4 rows)", h[0]);
+        return set_error(ctx, PCD_ERR_FORMAT, buf);
+    }
+    g->max_deg = h[1];
+    g->bins = BinConfig{{4, 8, 16, 32, 256, 2048, 8192}};
+    if (n > 0) launch_bins(g, side);
+    prof_mark(ctx, "load.bins", side);
+    CK(cudaGetLastError(), "degree classes");
+    for (int k = 0; k < nch; ++k) {
+        CK(cudaStreamWaitEvent(side, ctx->ev_copy[k], 0), "validate");
+        if (n > 0) launch_validate_rows(g, flag, k ? cut[k] : -1, cut[k + 1], side);
+    }
+    // the context's stream, behind the copy
     CK(cudaMemsetAsync(g->ctr, 0, sizeof(DevCounters), st), "memset");
     // FP64 re-evaluation tables: one HBM slice per block, empty between uses
     // (keys -1, counts 0, first positions 0xffffffff; position arrays need no init)
@@ -448,14 +457,21 @@ static pcd_status graph_setup(pcd_ctx *ctx, pcd_graph *g) {
         CK(cudaMemsetAsync(base + slots, 0, sizeof(int32_t) * (size_t)slots, st), "fallback scratch");
         CK(cudaMemsetAsync(base + 2 * slots, 0xff, sizeof(int32_t) * (size_t)slots, st), "fallback scratch");
     }
-    // degree bins, then the hub slices (the same tables plus labels and counts by position)
-    g->bins = BinConfig{{4, 8, 16, 32, 256, 2048, 8192}};
-    if (n > 0) launch_bins(g, st);
+    prof_mark(ctx, "load.state", st);
+    // the rows' verdict (a copy to pageable memory returns once it is done)
+    prof_mark(ctx, "load.validate", side);
+    CK(cudaMemcpyAsync(h, flag, sizeof(int32_t), cudaMemcpyDeviceToHost, side), "validate");
+    CK(cudaStreamSynchronize(side), "validate");
+    if (h[0]) {
+        char buf[128];
+        snprintf(buf, sizeof buf, "graph arrays are not a valid CSR (flags 0x%x: 1 span, 2 offsets, 4 rows)", h[0]);
+        return set_error(ctx, PCD_ERR_FORMAT, buf);
+    }
+    // the hub slices (the same tables plus labels and counts by position)
     TRY(ensure_hub_scratch(g));
     // initial labels: singletons 0..n-1 (already compressed)
     g->k = g->n;
     g->compressed = false;
-    CK(cudaStreamSynchronize(st), "graph setup");
     return PCD_OK;
 }
 
@@ -486,17 +502,42 @@ static pcd_status load_common(pcd_ctx *ctx, int32_t n, int32_t m, const int32_t 
     g->n = n;
     g->m = m;
     g->nnz = 2 * (int64_t)m;
+    prof_begin(ctx, ctx->stream);
+    cudaStream_t st = ctx->stream, side = nullptr;
+    int32_t *flag = nullptr;
     pcd_status s = dev_alloc(g, (void **)&g->indices, sizeof(int32_t) * ((size_t)n + 1));
     if (s == PCD_OK) s = dev_alloc(g, (void **)&g->adj, sizeof(int32_t) * (size_t)std::max<int64_t>(g->nnz, 1));
+    if (s == PCD_OK) s = dev_alloc(g, (void **)&flag, 2 * sizeof(int32_t));
+    if (s == PCD_OK) s = alloc_state(ctx, g);
+    if (s == PCD_OK) s = check_cuda(ctx, cudaMemsetAsync(flag, 0, 2 * sizeof(int32_t), st), "memset");
     if (s == PCD_OK)
-        s = check_cuda(ctx, cudaMemcpyAsync(g->indices, indices, sizeof(int32_t) * ((size_t)n + 1), kind, ctx->stream),
+        s = check_cuda(ctx, cudaMemcpyAsync(g->indices, indices, sizeof(int32_t) * ((size_t)n + 1), kind, st),
                        "copy indices");
-    if (s == PCD_OK && g->nnz)
-        s = check_cuda(ctx, cudaMemcpyAsync(g->adj, adj, sizeof(int32_t) * (size_t)g->nnz, kind, ctx->stream),
-                       "copy adj");
-    if (s == PCD_OK) s = graph_setup(ctx, g);
+    // the side stream starts behind the allocations and the row offsets
+    if (s == PCD_OK) s = side_fork(ctx, 1, &side);
+    const bool forked = s == PCD_OK;
+    // the neighbour array in pieces of about 256 MB (16-byte boundaries), an
+    // event after each
+    int64_t cut[pcd_ctx::kCopyChunks + 1] = {0};
+    const int nch = (int)std::min<int64_t>(pcd_ctx::kCopyChunks, std::max<int64_t>(1, (4 * g->nnz) >> 28));
+    for (int k = 1; k < nch; ++k) cut[k] = (g->nnz * k / nch) & ~3ll;
+    cut[nch] = g->nnz;
+    for (int k = 0; k < nch && s == PCD_OK; ++k) {
+        if (!ctx->ev_copy[k])
+            s = check_cuda(ctx, cudaEventCreateWithFlags(&ctx->ev_copy[k], cudaEventDisableTiming), "copy events");
+        if (s == PCD_OK && cut[k + 1] > cut[k])
+            s = check_cuda(ctx,
+                           cudaMemcpyAsync(g->adj + cut[k], adj + cut[k], sizeof(int32_t) * (size_t)(cut[k + 1] - cut[k]),
+                                           kind, st),
+                           "copy adj");
+        if (s == PCD_OK) s = check_cuda(ctx, cudaEventRecord(ctx->ev_copy[k], st), "copy events");
+    }
+    if (s == PCD_OK) prof_mark(ctx, "load.copy", st);
+    if (s == PCD_OK) s = graph_setup(ctx, g, flag, side, cut, nch);
+    if (forked) side_join(ctx, 1);
     if (s == PCD_OK && n > 0) {
         k_iota<<<std::max(1, std::min<int>((n + 255) / 256, ctx->num_sms * 8)), 256, 0, ctx->stream>>>(g->labels, n);
+        prof_mark(ctx, "load.labels", ctx->stream);
         s = check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "init labels");
     }
     if (s != PCD_OK) {

@@ -128,7 +128,13 @@ __global__ void k_stats_thread(const int32_t *__restrict__ indices, const int32_
             int32_t v = list[idx];
             l = labels[v];
             int32_t b = indices[v], e = indices[v + 1];
-            for (int32_t j = b; j < e; ++j) di += (labels[adj[j]] == l);
+            for (int32_t j = b; j < e; j += 4) {  // four gathers in flight
+                int32_t u[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) u[k] = j + k < e ? adj[j + k] : -1;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) di += u[k] >= 0 && labels[u[k]] == l;
+            }
             de = (e - b) - di;
         }
         add_stats(l, di, de, sizes, intv, extv, vol, valid, wsh);
@@ -136,6 +142,7 @@ __global__ void k_stats_thread(const int32_t *__restrict__ indices, const int32_
 }
 
 // Warp per vertex for the larger degrees; lane 0 adds the vertex's counts.
+// Neighbour ids are >= 0 in a validated graph, so -1 marks a lane past the row.
 __global__ void k_stats_warp(const int32_t *__restrict__ indices, const int32_t *__restrict__ adj,
                              const int32_t *__restrict__ labels, const int32_t *__restrict__ list,
                              int64_t count, int32_t *sizes, int32_t *intv, int32_t *extv, int32_t *vol) {
@@ -147,7 +154,13 @@ __global__ void k_stats_warp(const int32_t *__restrict__ indices, const int32_t 
         int32_t l = labels[v];
         int32_t b = indices[v], e = indices[v + 1];
         int32_t di = 0;
-        for (int32_t j = b + lane; j < e; j += 32) di += (labels[adj[j]] == l);
+        for (int32_t j = b + lane; j < e; j += 4 * 32) {  // four gathers in flight per lane
+            int32_t u[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) u[k] = j + 32 * k < e ? adj[j + 32 * k] : -1;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) di += u[k] >= 0 && labels[u[k]] == l;
+        }
 #pragma unroll
         for (int d = 16; d; d >>= 1) di += __shfl_xor_sync(FULL, di, d);
         if (lane == 0) {
@@ -369,37 +382,147 @@ int launch_score(pcd_graph *g, int32_t kind, double lambda, double *d_out, cudaS
 }
 
 // ---------------------------------------------------------------------------
-// CSR validation: offsets monotone and spanning [0, 2m], neighbours in range,
-// rows strictly increasing (sorted, no duplicates), no loops.
+// CSR validation in two parts.  The row offsets alone (monotone, spanning
+// [0, 2m]; flag bits 1 and 2) and the largest degree need only `indices`, so
+// they run while the neighbour array is still being copied; the rows
+// (neighbours in range, strictly increasing, no loops; bit 4) follow once it
+// has arrived, and only over offsets that passed.
 // ---------------------------------------------------------------------------
-__global__ void k_validate(const int32_t *__restrict__ indices, const int32_t *__restrict__ adj, int32_t n,
-                           int32_t m, int32_t *flag) {
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    if (warp == 0 && lane == 0) {
-        if (indices[0] != 0 || (int64_t)indices[n] != 2 * (int64_t)m) atomicOr(flag, 1);
+__global__ void k_check_offsets(const int32_t *__restrict__ indices, int32_t n, int32_t m, int32_t *flag) {
+    int32_t bad = 0, mx = 0;
+    const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t0 == 0 && (indices[0] != 0 || (int64_t)indices[n] != 2 * (int64_t)m)) bad |= 1;
+    for (int64_t v = t0; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t b = indices[v], e = indices[v + 1];
+        if (b > e || b < 0 || (int64_t)e > 2 * (int64_t)m) bad |= 2;
+        mx = max(mx, e - b);
     }
-    for (int64_t v = warp; v < n; v += nwarps) {
-        int32_t b = indices[v], e = indices[v + 1];
-        if (b > e || b < 0 || (int64_t)e > 2 * (int64_t)m) {
-            if (lane == 0) atomicOr(flag, 2);
-            continue;
-        }
-        bool bad = false;
-        for (int32_t j = b + lane; j < e; j += 32) {
-            int32_t u = adj[j];
-            bad |= (u < 0 || u >= n || u == (int32_t)v);
-            if (j > b) bad |= (adj[j - 1] >= u);
-        }
-        if (__any_sync(FULL, bad) && lane == 0) atomicOr(flag, 4);
+    bad = __reduce_or_sync(FULL, bad);
+    mx = __reduce_max_sync(FULL, mx);
+    if ((threadIdx.x & 31) == 0) {
+        if (bad) atomicOr(flag, bad);
+        atomicMax(flag + 1, mx);
     }
 }
 
-int launch_validate(const int32_t *indices, const int32_t *adj, int32_t n, int32_t m, int32_t *d_flag,
-                    cudaStream_t st) {
-    k_validate<<<grid_for((int64_t)n * 32, 256), 256, 0, st>>>(indices, adj, n, m, d_flag);
+// Rows (bit 4 of flag), by degree class from the class lists (bin_list), so
+// that no thread walks a long row alone: a thread per row up to 32 neighbours,
+// a warp per row up to 2048, a 512-thread block per longer row; four loads in
+// flight per thread.  Within a row the neighbours must increase strictly, lie
+// in [0, n) and differ from the row's vertex.  One launch checks the rows
+// whose end offset lies in (lo, hi]: the neighbour array arrives in pieces,
+// and a row is checked once its last neighbour has.  The offsets have passed
+// k_check_offsets.
+__global__ void k_validate_thread(const int32_t *__restrict__ indices, const int32_t *__restrict__ adj, int32_t n,
+                                  const int32_t *__restrict__ list, int64_t count, int64_t lo, int64_t hi,
+                                  int32_t *flag) {
+    bool bad = false;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t v = list[i];
+        const int32_t e = indices[v + 1];
+        if (e <= lo || e > hi) continue;
+        const int32_t b = indices[v];
+        int32_t prev = -1;  // ids are >= 0, so the first neighbour always exceeds it
+        for (int32_t j = b; j < e; j += 4) {
+            int32_t u[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) u[k] = j + k < e ? adj[j + k] : INT_MAX;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (j + k < e) {
+                    bad |= u[k] < 0 || u[k] >= n || u[k] == v || u[k] <= prev;
+                    prev = u[k];
+                }
+            }
+        }
+    }
+    if (__any_sync(FULL, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 4);
+}
+
+// `nw` warps walk row [b, e) of vertex v in 32-entry chunks (chunk c of the
+// row to warp c % nw); the neighbour before each lane's entry comes from the
+// lane below, or from memory for lane 0.
+__device__ __forceinline__ bool check_row_warps(const int32_t *__restrict__ adj, int32_t n, int32_t v, int32_t b,
+                                                int32_t e, int wid, int nw, int lane) {
+    bool bad = false;
+    for (int64_t c0 = (int64_t)b + 32 * wid; c0 < e; c0 += 4ll * 32 * nw) {
+        int32_t u[4], p0[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int64_t c = c0 + 32ll * nw * k, j = c + lane;
+            u[k] = j < e ? adj[j] : 0;
+            p0[k] = lane == 0 && c < e && c > b ? adj[c - 1] : -1;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int64_t j = c0 + 32ll * nw * k + lane;
+            int32_t prev = __shfl_up_sync(FULL, u[k], 1);
+            if (lane == 0) prev = p0[k];
+            if (j < e) bad |= u[k] < 0 || u[k] >= n || u[k] == v || (j > b && prev >= u[k]);
+        }
+    }
+    return bad;
+}
+
+__global__ void k_validate_warp(const int32_t *__restrict__ indices, const int32_t *__restrict__ adj, int32_t n,
+                                const int32_t *__restrict__ list, int64_t count, int64_t lo, int64_t hi,
+                                int32_t *flag) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    bool bad = false;
+    for (int64_t i = warp; i < count; i += nwarps) {
+        const int32_t v = list[i];
+        const int32_t e = indices[v + 1];
+        if (e <= lo || e > hi) continue;
+        bad |= check_row_warps(adj, n, v, indices[v], e, 0, 1, lane);
+    }
+    if (__any_sync(FULL, bad) && lane == 0) atomicOr(flag, 4);
+}
+
+__global__ void __launch_bounds__(512) k_validate_block(const int32_t *__restrict__ indices,
+                                                        const int32_t *__restrict__ adj, int32_t n,
+                                                        const int32_t *__restrict__ list, int64_t count,
+                                                        int64_t lo, int64_t hi, int32_t *flag) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    bool bad = false;
+    for (int64_t i = blockIdx.x; i < count; i += gridDim.x) {
+        const int32_t v = list[i];
+        const int32_t e = indices[v + 1];
+        if (e <= lo || e > hi) continue;
+        bad |= check_row_warps(adj, n, v, indices[v], e, wid, 16, lane);
+    }
+    if (__any_sync(FULL, bad) && lane == 0) atomicOr(flag, 4);
+}
+
+int launch_check_offsets(const int32_t *indices, int32_t n, int32_t m, int32_t *d_flag, cudaStream_t st) {
+    k_check_offsets<<<grid_for(std::max<int64_t>(n, 1), 256), 256, 0, st>>>(indices, n, m, d_flag);
     return 1;
+}
+
+int launch_validate_rows(pcd_graph *g, int32_t *d_flag, int64_t lo, int64_t hi, cudaStream_t st) {
+    int launches = 0;
+    const int64_t nt = g->bin_off[BIN_WARP] - g->bin_off[0];
+    const int64_t nw = g->bin_off[BIN_BLOCK_L] - g->bin_off[BIN_WARP];
+    const int64_t nb = g->bin_off[NBINS] - g->bin_off[BIN_BLOCK_L];
+    if (nt > 0) {
+        k_validate_thread<<<grid_for(nt, 256), 256, 0, st>>>(g->indices, g->adj, g->n, g->bin_list + g->bin_off[0],
+                                                              nt, lo, hi, d_flag);
+        ++launches;
+    }
+    if (nw > 0) {
+        k_validate_warp<<<grid_for(nw * 32, 256), 256, 0, st>>>(g->indices, g->adj, g->n,
+                                                                 g->bin_list + g->bin_off[BIN_WARP], nw, lo, hi,
+                                                                 d_flag);
+        ++launches;
+    }
+    if (nb > 0) {
+        const unsigned blocks = (unsigned)std::min<int64_t>(nb, (int64_t)g->ctx->num_sms * 4);
+        k_validate_block<<<blocks, 512, 0, st>>>(g->indices, g->adj, g->n, g->bin_list + g->bin_off[BIN_BLOCK_L], nb,
+                                                 lo, hi, d_flag);
+        ++launches;
+    }
+    return launches;
 }
 
 // ---------------------------------------------------------------------------

@@ -38,6 +38,10 @@ struct pcd_ctx {
     int32_t side_prio = 0;
     cudaEvent_t ev_fork = nullptr;
     cudaEvent_t ev_join[kSide] = {nullptr, nullptr, nullptr};
+    // a graph load copies the neighbour array in up to kCopyChunks pieces and
+    // records one of these after each, so its rows are checked as they arrive
+    static constexpr int kCopyChunks = 8;
+    cudaEvent_t ev_copy[kCopyChunks] = {};
     pcd::DevCounters *h_ctr = nullptr;  // pinned copy of a graph's counters (shared by its graphs)
     // multiplies the resident-block caps of the sweep grids: above 1 the warp,
     // block and thread classes launch more blocks than fit at once, so blocks
@@ -150,8 +154,12 @@ pcd_status dev_alloc(pcd_graph *g, void **p, size_t bytes);
 int launch_compress(pcd_graph *g, cudaStream_t st);   // relabel + stats; k to ctr->k
 int launch_stats(pcd_graph *g, cudaStream_t st);
 int launch_score(pcd_graph *g, int32_t kind, double lambda, double *d_out, cudaStream_t st);
-int launch_validate(const int32_t *indices, const int32_t *adj, int32_t n, int32_t m,
-                    int32_t *d_flag, cudaStream_t st);
+// CSR checks: offsets (flag bits 1, 2) and the largest degree (d_flag[1]) from
+// `indices` alone; then the rows (bit 4), over offsets that passed
+int launch_check_offsets(const int32_t *indices, int32_t n, int32_t m, int32_t *d_flag, cudaStream_t st);
+// by degree class (needs the bins): the rows whose last neighbour lies in
+// (lo, hi] of the neighbour array (rows ending at 0 with lo < 0)
+int launch_validate_rows(pcd_graph *g, int32_t *d_flag, int64_t lo, int64_t hi, cudaStream_t st);
 // fills bin_list, bin_off, subs (syncs); active_only (batches): vertices of
 // graphs whose schedule has finished are left out of every class
 int launch_bins(pcd_graph *g, cudaStream_t st, bool active_only = false);

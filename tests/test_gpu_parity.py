@@ -201,6 +201,24 @@ def test_edge_cases(ctx, port):
         pcd.Graph.from_csr(ctx, np.array([0, 2, 2], np.int32), np.array([1, 1], np.int32))  # duplicate
     with pytest.raises(pcd.PcdError):
         pcd.Graph.from_csr(ctx, np.array([0, 1, 2], np.int32), np.array([1, 5], np.int32))  # out of range
+    with pytest.raises(pcd.PcdError):
+        pcd.Graph.from_csr(ctx, np.array([0, 3, 2, 4], np.int32), np.array([1, 2, 3, 0], np.int32))  # offsets fall
+    with pytest.raises(pcd.PcdError):
+        pcd.Graph.from_csr(ctx, np.array([0, 1, 2, 2], np.int32), np.array([1, 0, 2, 1], np.int32))  # span < 2m
+    # rows longer than 16 neighbours are checked by a whole warp: a star of 20
+    # leaves whose centre row carries one fault at a time
+    leaves = np.arange(1, 21, dtype=np.int32)
+    ind_star = np.concatenate([[0, 20], 20 + np.arange(1, 21)]).astype(np.int32)
+    for centre, what in ((np.r_[leaves[:4], leaves[3], leaves[5:]], "duplicate"),
+                         (np.r_[leaves[:10], 0, leaves[11:]], "loop"),
+                         (np.r_[leaves[:10], 25, leaves[11:]], "out of range"),
+                         (np.r_[leaves[10:], leaves[:10]], "unsorted")):
+        adj_star = np.concatenate([centre, np.zeros(20, np.int32)]).astype(np.int32)
+        with pytest.raises(pcd.PcdError, match="not a valid CSR"):
+            pcd.Graph.from_csr(ctx, ind_star, adj_star)  # the centre row has a `what`
+    G = pcd.Graph.from_csr(ctx, ind_star, np.concatenate([leaves, np.zeros(20, np.int32)]).astype(np.int32))
+    assert G.n == 21
+    G.free()
     G = pcd.Graph.from_csr(ctx, np.array([0, 1, 2], np.int32), np.array([1, 0], np.int32))
     with pytest.raises(pcd.PcdError):
         G.labels = np.array([0, 7], np.int32)
