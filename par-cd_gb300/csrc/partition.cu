@@ -267,6 +267,7 @@ int launch_compress(pcd_graph *g, cudaStream_t st) {
                                                         g->batch->cgid, g->batch->gK, g->ctr);
         ++launches;
     }
+    prof_mark(g->ctx, "compress", st);
     launches += launch_stats(g, st);
     return launches;
 }
