@@ -1076,7 +1076,7 @@ def main():
         ctx.synchronize()
         ph["refine (host)"] = time.perf_counter() - t0
         for nm, ms in ctx.profile_read():
-            key = "refine." + nm if nm in ("compress", "stats") else "refine.sweep"
+            key = "refine." + nm if nm == "compress" or nm.startswith("stats") else "refine.sweep"
             ph[key] = ph.get(key, 0.0) + ms / 1000.0
         t0 = time.perf_counter()
         g2.get_labels_ptr(h_out.data_ptr())

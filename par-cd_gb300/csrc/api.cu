@@ -691,7 +691,6 @@ pcd_status pcd_compress(pcd_graph *g, int32_t *num_labels) {
     int launches = 0;
     if (!g->compressed) prof_begin(g->ctx, g->ctx->stream);
     TRY(ensure_compressed(g, &launches));
-    if (launches) prof_mark(g->ctx, "stats", g->ctx->stream);
     g->info.kernels_total += launches;
     if (num_labels) {
         TRY(sync_and_check(g));
@@ -755,7 +754,6 @@ pcd_status pcd_refine(pcd_graph *g, const pcd_rule *rule, double frac, uint32_t 
     int launches = 0;
     prof_begin(g->ctx, g->ctx->stream);
     TRY(ensure_compressed(g, &launches));
-    if (launches) prof_mark(g->ctx, "stats", g->ctx->stream);
     if (g->n > 0) {
         launches += launch_refine(g, rule->kind, rule->lambda, frac, seed, g->ctx->stream);
         std::swap(g->labels, g->labels_alt);
@@ -774,7 +772,6 @@ pcd_status pcd_merge(pcd_graph *g, const pcd_rule *rule, int32_t rounds, uint32_
     int launches = 0;
     prof_begin(g->ctx, g->ctx->stream);
     TRY(ensure_compressed(g, &launches));
-    if (launches) prof_mark(g->ctx, "stats", g->ctx->stream);
     if (g->n > 0) {
         TRY(run_merge(g, rule->kind, rule->lambda, rounds, seed, g->ctx->stream, &launches));
         std::swap(g->labels, g->labels_alt);

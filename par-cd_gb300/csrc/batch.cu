@@ -311,7 +311,6 @@ static pcd_status batch_step(pcd_graph *g, const pcd_rule *rule, bool merge, dou
     int launches = 0;
     prof_begin(ctx, ctx->stream);
     TRY(ensure_compressed(g, &launches));
-    if (launches) prof_mark(ctx, "stats", ctx->stream);
     g->labels_vertex_space = false;
     CK(cudaMemcpyAsync(g->batch->gseed, seeds, sizeof(uint32_t) * g->batch->G, cudaMemcpyHostToDevice, ctx->stream),
        "seeds");

@@ -173,25 +173,28 @@ __global__ void k_stats_warp(const int32_t *__restrict__ indices, const int32_t 
     }
 }
 
-// Block per vertex for rows above 2048 neighbours (the largest rows would
-// otherwise keep one warp busy for the whole pass): 512 threads with four
-// label gathers in flight each, one set of atomics per vertex.
-__global__ void __launch_bounds__(512) k_stats_block(const int32_t *__restrict__ indices,
-                                                     const int32_t *__restrict__ adj,
-                                                     const int32_t *__restrict__ labels,
-                                                     const int32_t *__restrict__ list, int64_t count, int32_t *sizes,
-                                                     int32_t *intv, int32_t *extv, int32_t *vol) {
-    __shared__ int32_t part[16];
+// Block per vertex for rows above 2048 neighbours (one warp would walk them
+// alone): BT threads with four label gathers in flight each, one set of
+// atomics per vertex.  (256-thread blocks for 257..2048 were slower than a
+// warp per row there.)
+template <int BT>
+__global__ void __launch_bounds__(BT) k_stats_block(const int32_t *__restrict__ indices,
+                                                    const int32_t *__restrict__ adj,
+                                                    const int32_t *__restrict__ labels,
+                                                    const int32_t *__restrict__ list, int64_t count, int32_t *sizes,
+                                                    int32_t *intv, int32_t *extv, int32_t *vol) {
+    constexpr int NW = BT / 32;
+    __shared__ int32_t part[NW];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int64_t idx = blockIdx.x; idx < count; idx += gridDim.x) {
         const int32_t v = list[idx];
         const int32_t l = labels[v];
         const int32_t b = indices[v], e = indices[v + 1];
         int32_t di = 0;
-        for (int32_t j0 = b + (int32_t)threadIdx.x; j0 < e; j0 += 4 * 512) {
+        for (int32_t j0 = b + (int32_t)threadIdx.x; j0 < e; j0 += 4 * BT) {
             int32_t u[4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) u[k] = j0 + k * 512 < e ? adj[j0 + k * 512] : -1;
+            for (int k = 0; k < 4; ++k) u[k] = j0 + k * BT < e ? adj[j0 + k * BT] : -1;
 #pragma unroll
             for (int k = 0; k < 4; ++k) di += u[k] >= 0 && labels[u[k]] == l;
         }
@@ -200,7 +203,7 @@ __global__ void __launch_bounds__(512) k_stats_block(const int32_t *__restrict__
         __syncthreads();
         if (threadIdx.x == 0) {
             int32_t t = 0;
-            for (int w = 0; w < 16; ++w) t += part[w];
+            for (int w = 0; w < NW; ++w) t += part[w];
             atomicAdd(sizes + l, 1);
             atomicAdd(intv + l, t);
             atomicAdd(extv + l, (e - b) - t);
@@ -222,6 +225,7 @@ int launch_stats(pcd_graph *g, cudaStream_t st) {
         k_stats_thread<<<grid_for(nt, 256), 256, 0, st>>>(g->indices, g->adj, g->labels,
                                                            g->bin_list + g->bin_off[0], nt, g->sizes,
                                                            g->intv, g->extv, g->vol);
+        prof_mark(g->ctx, "stats.thread", st);
         ++launches;
     }
     int64_t nw = g->bin_off[BIN_BLOCK_L] - g->bin_off[BIN_WARP];
@@ -229,13 +233,16 @@ int launch_stats(pcd_graph *g, cudaStream_t st) {
         k_stats_warp<<<grid_for(nw * 32, 256), 256, 0, st>>>(g->indices, g->adj, g->labels,
                                                              g->bin_list + g->bin_off[BIN_WARP], nw, g->sizes,
                                                              g->intv, g->extv, g->vol);
+        prof_mark(g->ctx, "stats.warp", st);
         ++launches;
     }
-    int64_t nb = g->bin_off[NBINS] - g->bin_off[BIN_BLOCK_L];
-    if (nb > 0) {
-        const unsigned blocks = (unsigned)std::min<int64_t>(nb, (int64_t)g->ctx->num_sms * 4);
-        k_stats_block<<<blocks, 512, 0, st>>>(g->indices, g->adj, g->labels, g->bin_list + g->bin_off[BIN_BLOCK_L], nb,
-                                             g->sizes, g->intv, g->extv, g->vol);
+    int64_t nl = g->bin_off[NBINS] - g->bin_off[BIN_BLOCK_L];
+    if (nl > 0) {
+        const unsigned blocks = (unsigned)std::min<int64_t>(nl, (int64_t)g->ctx->num_sms * 4);
+        k_stats_block<512><<<blocks, 512, 0, st>>>(g->indices, g->adj, g->labels,
+                                                   g->bin_list + g->bin_off[BIN_BLOCK_L], nl, g->sizes, g->intv,
+                                                   g->extv, g->vol);
+        prof_mark(g->ctx, "stats.block_l", st);
         ++launches;
     }
     return launches;
