@@ -112,10 +112,15 @@ __device__ __forceinline__ void add_stats(int32_t l, int32_t di, int32_t de, int
     __syncwarp();
 }
 
+// `singles`: the partition has one vertex per community (k == n right after a
+// compress; see launch_stats), so no neighbour shares a vertex's label (the
+// graph has no loops) and the neighbour labels need not be read.
 __global__ void k_stats_thread(const int32_t *__restrict__ indices, const int32_t *__restrict__ adj,
                                const int32_t *__restrict__ labels, const int32_t *__restrict__ list,
-                               int64_t count, int32_t *sizes, int32_t *intv, int32_t *extv, int32_t *vol) {
+                               int64_t count, int32_t *sizes, int32_t *intv, int32_t *extv, int32_t *vol,
+                               const int32_t *k_dev, int32_t n_all) {
     __shared__ int2 sh[1024];
+    const bool singles = k_dev && *k_dev == n_all;
     int2 *wsh = sh + (threadIdx.x & ~31u);
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t start = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -128,7 +133,7 @@ __global__ void k_stats_thread(const int32_t *__restrict__ indices, const int32_
             int32_t v = list[idx];
             l = labels[v];
             int32_t b = indices[v], e = indices[v + 1];
-            for (int32_t j = b; j < e; j += 4) {  // four gathers in flight
+            for (int32_t j = b; j < (singles ? b : e); j += 4) {  // four gathers in flight
                 int32_t u[4];
 #pragma unroll
                 for (int k = 0; k < 4; ++k) u[k] = j + k < e ? adj[j + k] : -1;
@@ -145,8 +150,10 @@ __global__ void k_stats_thread(const int32_t *__restrict__ indices, const int32_
 // Neighbour ids are >= 0 in a validated graph, so -1 marks a lane past the row.
 __global__ void k_stats_warp(const int32_t *__restrict__ indices, const int32_t *__restrict__ adj,
                              const int32_t *__restrict__ labels, const int32_t *__restrict__ list,
-                             int64_t count, int32_t *sizes, int32_t *intv, int32_t *extv, int32_t *vol) {
+                             int64_t count, int32_t *sizes, int32_t *intv, int32_t *extv, int32_t *vol,
+                             const int32_t *k_dev, int32_t n_all) {
     const int lane = threadIdx.x & 31;
+    const bool singles = k_dev && *k_dev == n_all;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t idx = warp; idx < count; idx += nwarps) {
@@ -154,7 +161,7 @@ __global__ void k_stats_warp(const int32_t *__restrict__ indices, const int32_t 
         int32_t l = labels[v];
         int32_t b = indices[v], e = indices[v + 1];
         int32_t di = 0;
-        for (int32_t j = b + lane; j < e; j += 4 * 32) {  // four gathers in flight per lane
+        for (int32_t j = b + lane; j < (singles ? b : e); j += 4 * 32) {  // four gathers in flight per lane
             int32_t u[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) u[k] = j + 32 * k < e ? adj[j + 32 * k] : -1;
@@ -182,8 +189,10 @@ __global__ void __launch_bounds__(BT) k_stats_block(const int32_t *__restrict__ 
                                                     const int32_t *__restrict__ adj,
                                                     const int32_t *__restrict__ labels,
                                                     const int32_t *__restrict__ list, int64_t count, int32_t *sizes,
-                                                    int32_t *intv, int32_t *extv, int32_t *vol) {
+                                                    int32_t *intv, int32_t *extv, int32_t *vol,
+                                                    const int32_t *k_dev, int32_t n_all) {
     constexpr int NW = BT / 32;
+    const bool singles = k_dev && *k_dev == n_all;
     __shared__ int32_t part[NW];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int64_t idx = blockIdx.x; idx < count; idx += gridDim.x) {
@@ -191,7 +200,7 @@ __global__ void __launch_bounds__(BT) k_stats_block(const int32_t *__restrict__ 
         const int32_t l = labels[v];
         const int32_t b = indices[v], e = indices[v + 1];
         int32_t di = 0;
-        for (int32_t j0 = b + (int32_t)threadIdx.x; j0 < e; j0 += 4 * BT) {
+        for (int32_t j0 = b + (int32_t)threadIdx.x; j0 < (singles ? b : e); j0 += 4 * BT) {
             int32_t u[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) u[k] = j0 + k * BT < e ? adj[j0 + k * BT] : -1;
@@ -213,8 +222,12 @@ __global__ void __launch_bounds__(BT) k_stats_block(const int32_t *__restrict__ 
     }
 }
 
-int launch_stats(pcd_graph *g, cudaStream_t st) {
+// after_compress: ctr->k holds the community count of the current labels
+// (launch_compress has just set it), so a partition of single vertices can be
+// recognised on the device; other callers pass false.
+int launch_stats(pcd_graph *g, cudaStream_t st, bool after_compress) {
     int launches = 0;
+    const int32_t *k_dev = after_compress ? &g->ctr->k : nullptr;
     size_t bytes = sizeof(int32_t) * (size_t)(g->n > 0 ? g->n : 1);
     cudaMemsetAsync(g->sizes, 0, bytes, st);
     cudaMemsetAsync(g->intv, 0, bytes, st);
@@ -224,7 +237,7 @@ int launch_stats(pcd_graph *g, cudaStream_t st) {
     if (nt > 0) {
         k_stats_thread<<<grid_for(nt, 256), 256, 0, st>>>(g->indices, g->adj, g->labels,
                                                            g->bin_list + g->bin_off[0], nt, g->sizes,
-                                                           g->intv, g->extv, g->vol);
+                                                           g->intv, g->extv, g->vol, k_dev, g->n);
         prof_mark(g->ctx, "stats.thread", st);
         ++launches;
     }
@@ -232,7 +245,7 @@ int launch_stats(pcd_graph *g, cudaStream_t st) {
     if (nw > 0) {
         k_stats_warp<<<grid_for(nw * 32, 256), 256, 0, st>>>(g->indices, g->adj, g->labels,
                                                              g->bin_list + g->bin_off[BIN_WARP], nw, g->sizes,
-                                                             g->intv, g->extv, g->vol);
+                                                             g->intv, g->extv, g->vol, k_dev, g->n);
         prof_mark(g->ctx, "stats.warp", st);
         ++launches;
     }
@@ -241,7 +254,7 @@ int launch_stats(pcd_graph *g, cudaStream_t st) {
         const unsigned blocks = (unsigned)std::min<int64_t>(nl, (int64_t)g->ctx->num_sms * 4);
         k_stats_block<512><<<blocks, 512, 0, st>>>(g->indices, g->adj, g->labels,
                                                    g->bin_list + g->bin_off[BIN_BLOCK_L], nl, g->sizes, g->intv,
-                                                   g->extv, g->vol);
+                                                   g->extv, g->vol, k_dev, g->n);
         prof_mark(g->ctx, "stats.block_l", st);
         ++launches;
     }
@@ -275,7 +288,7 @@ int launch_compress(pcd_graph *g, cudaStream_t st) {
         ++launches;
     }
     prof_mark(g->ctx, "compress", st);
-    launches += launch_stats(g, st);
+    launches += launch_stats(g, st, true);
     return launches;
 }
 

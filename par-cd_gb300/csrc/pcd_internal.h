@@ -152,7 +152,7 @@ pcd_status dev_alloc(pcd_graph *g, void **p, size_t bytes);
 
 // partition.cu
 int launch_compress(pcd_graph *g, cudaStream_t st);   // relabel + stats; k to ctr->k
-int launch_stats(pcd_graph *g, cudaStream_t st);
+int launch_stats(pcd_graph *g, cudaStream_t st, bool after_compress = false);
 int launch_score(pcd_graph *g, int32_t kind, double lambda, double *d_out, cudaStream_t st);
 // CSR checks: offsets (flag bits 1, 2) and the largest degree (d_flag[1]) from
 // `indices` alone; then the rows (bit 4), over offsets that passed
