@@ -15,7 +15,7 @@ Lines printed (rank 0, one JSON line):
              stream the kernels run on, max over ranks
   e2e        the same metric through the C ABI with HOST buffers: every step
              loads the CSR from pinned host memory, sets the start labels,
-             sweeps, and reads the labels back
+             sweeps, and reads the labels back (the same cycle of sweeps)
   roofline   the sweep's dominant kernel against the measured HBM copy peak
   cpu_baseline  the oracle (C restatement of the reference, OpenMP) on the
              host cores, on the same graph
@@ -866,7 +866,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scale", type=int, default=24)
     ap.add_argument("--edge-factor", type=int, default=16)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5, help="e2e steps (cycling through the same sweeps)")
     ap.add_argument("--sweeps", type=int, default=5, help="cycle through the first S sweeps of the schedule")
     ap.add_argument("--bins", default="", help="degree classes, 7 comma-separated bounds (default: library's)")
     ap.add_argument("--no-cpu", action="store_true")
@@ -1006,12 +1006,15 @@ def main():
     value = world * m * args.steps / (total_ms / 1e3)
     assert np.array_equal(G.labels, results[last]), "sweep result changed between identical steps"
 
-    # per-phase profile of one more step (events between kernel groups)
+    # per-phase profile: every sweep of the cycle once more (events between
+    # kernel groups), averaged, so that the classes add up to the timed mean
+    # (the first sweep, from the singleton partition, differs from the rest)
     ctx.profile(True)
-    step(0)
     phases = {}
-    for nm, ms in ctx.profile_read():  # a class may run as several launches (degree sub-ranges)
-        phases[nm] = phases.get(nm, 0.0) + ms
+    for i in range(args.sweeps):
+        step(i)
+        for nm, ms in ctx.profile_read():  # a class may run as several launches (degree sub-ranges)
+            phases[nm] = phases.get(nm, 0.0) + ms / args.sweeps
     ctx.profile(False)
     info = G.info()
     bins_now = G.get_bins()
@@ -1033,57 +1036,69 @@ def main():
     if args.e2e_steps > 0:
         h_ind = torch.from_numpy(ind).pin_memory()
         h_adj = torch.from_numpy(adj).pin_memory()
-        h_lab = starts[0].cpu().pin_memory()
+        # the same cycle of sweeps as the resident steps: step i starts from
+        # sweep (i mod S)'s start partition with that sweep's seed
+        h_labs = [starts[j].cpu().pin_memory() for j in range(args.sweeps)]
         h_out = torch.empty(n, dtype=torch.int32).pin_memory()
         G.free()
         torch.cuda.empty_cache()
 
-        def e2e_step():
+        def e2e_step(i):
+            j = i % args.sweeps
             g2 = pcd.Graph.from_host_ptr(ctx, n, m, h_ind.data_ptr(), h_adj.data_ptr())
-            g2.set_labels_ptr(h_lab.data_ptr())
-            sweep.refine(g2, rule, seeds[0])
+            g2.set_labels_ptr(h_labs[j].data_ptr())
+            sweep.refine(g2, rule, seeds[j])
             g2.get_labels_ptr(h_out.data_ptr())
             g2.free()
+            return j
 
-        e2e_step()
-        assert np.array_equal(h_out.numpy(), results[0]), "end-to-end result differs from the resident run"
+        for i in range(args.sweeps):  # warm-up, and every sweep's labels against the resident run
+            j = e2e_step(i)
+            assert np.array_equal(h_out.numpy(), results[j]), f"end-to-end sweep {j} differs from the resident run"
         if dist:
             dist.barrier()
         t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
-            e2e_step()
+        for i in range(args.e2e_steps):
+            e2e_step(i)
         sec = time.perf_counter() - t0
         sec = max_over_ranks(dist, sec, dev)
         e2e = {"value": world * m * args.e2e_steps / sec, "unit": "edges/s",
                "h2d_bytes_per_step": int(4 * (n + 1) + 8 * m + 4 * n), "d2h_bytes_per_step": int(4 * n),
                "ms_per_step": 1000.0 * sec / args.e2e_steps,
                "note": "each step: pcd_load_csr from pinned host CSR (validation, degree bins, buffers), "
-                       "pcd_labels_set, pcd_refine, pcd_labels_get, pcd_graph_free"}
-        # where one more step's time goes: device spans of the load and of the
-        # refine call (CUDA events), host time of the calls around them
+                       "pcd_labels_set (the start partition of sweep i mod S), pcd_refine, pcd_labels_get, "
+                       "pcd_graph_free; the same cycle of sweeps as value"}
+        # where a step's time goes, averaged over one more cycle of the sweeps:
+        # device spans of the load and of the refine call (CUDA events), host
+        # time of the calls around them
         ctx.profile(True)
         ph = {}
-        t0 = time.perf_counter()
-        g2 = pcd.Graph.from_host_ptr(ctx, n, m, h_ind.data_ptr(), h_adj.data_ptr())
-        ph["load (host)"] = time.perf_counter() - t0
-        for nm, ms in ctx.profile_read():
-            ph[nm] = ph.get(nm, 0.0) + ms / 1000.0
-        t0 = time.perf_counter()
-        g2.set_labels_ptr(h_lab.data_ptr())
-        ph["labels_set (host)"] = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        sweep.refine(g2, rule, seeds[0])
-        ctx.synchronize()
-        ph["refine (host)"] = time.perf_counter() - t0
-        for nm, ms in ctx.profile_read():
-            key = "refine." + nm if nm == "compress" or nm.startswith("stats") else "refine.sweep"
-            ph[key] = ph.get(key, 0.0) + ms / 1000.0
-        t0 = time.perf_counter()
-        g2.get_labels_ptr(h_out.data_ptr())
-        ph["labels_get (host)"] = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        g2.free()
-        ph["free (host)"] = time.perf_counter() - t0
+        S = args.sweeps
+
+        def add(key, sec):
+            ph[key] = ph.get(key, 0.0) + sec / S
+
+        for j in range(S):
+            t0 = time.perf_counter()
+            g2 = pcd.Graph.from_host_ptr(ctx, n, m, h_ind.data_ptr(), h_adj.data_ptr())
+            add("load (host)", time.perf_counter() - t0)
+            for nm, ms in ctx.profile_read():
+                add(nm, ms / 1000.0)
+            t0 = time.perf_counter()
+            g2.set_labels_ptr(h_labs[j].data_ptr())
+            add("labels_set (host)", time.perf_counter() - t0)
+            t0 = time.perf_counter()
+            sweep.refine(g2, rule, seeds[j])
+            ctx.synchronize()
+            add("refine (host)", time.perf_counter() - t0)
+            for nm, ms in ctx.profile_read():
+                add("refine." + nm if nm == "compress" or nm.startswith("stats") else "refine.sweep", ms / 1000.0)
+            t0 = time.perf_counter()
+            g2.get_labels_ptr(h_out.data_ptr())
+            add("labels_get (host)", time.perf_counter() - t0)
+            t0 = time.perf_counter()
+            g2.free()
+            add("free (host)", time.perf_counter() - t0)
         ctx.profile(False)
         e2e["phases_ms"] = {k: round(1000.0 * v, 3) for k, v in ph.items()}
 
@@ -1163,6 +1178,7 @@ def main():
             "gpu_launches": int(launches),
             "clocks": clk,
             "phases_ms": {nm: round(ms, 4) for nm, ms in phases.items()},
+            "phases_over": f"mean of the cycle's {args.sweeps} sweeps (CUDA events between kernel groups)",
             "per_sweep_ms": [round(statistics.mean(sweep_ms[j::args.sweeps]), 3)
                              for j in range(min(args.sweeps, len(sweep_ms)))],
             "bins": bins_now,

@@ -150,10 +150,19 @@ __device__ __forceinline__ long long alloc_ties_warp(const SweepArgs &a, int32_t
 // tied with the final holder (a bit mask).  No lane talks to another, so a
 // warp analyses 32 vertices at once.
 // ---------------------------------------------------------------------------
+// True when every vertex is its own community: k == n, set by the compress
+// that precedes every sweep (the first sweep of every schedule from the
+// singleton partition).  A row's labels are then distinct (rows hold no
+// duplicate neighbours), each counted once, and a label's first occurrence is
+// its row position, so the kernels score the row as it stands, without a
+// histogram.  The flag is the same for every thread of a launch.
+__device__ __forceinline__ bool singleton_partition(const SweepArgs &a) { return a.ctr->k == a.g.n; }
+
 template <class R, int MAXD>
 __global__ void __launch_bounds__(256) k_prop_thread(SweepArgs a, R rule, const int32_t *__restrict__ list,
                                                      int64_t count) {
     using Key = typename R::Key;
+    const bool singles = singleton_partition(a);
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < count;
          idx += (int64_t)gridDim.x * blockDim.x) {
         const int32_t v = list[idx];
@@ -170,13 +179,15 @@ __global__ void __launch_bounds__(256) k_prop_thread(SweepArgs a, R rule, const 
             cnt[j] = 1;
         }
         uint32_t later = 0;  // bit j: lab[j] occurred at an earlier position
+        if (!singles) {
 #pragma unroll
-        for (int j = 1; j < MAXD; ++j) {
+            for (int j = 1; j < MAXD; ++j) {
 #pragma unroll
-            for (int i = 0; i < j; ++i) {
-                const bool e = lab[i] == lab[j];
-                cnt[i] += e ? 1 : 0;
-                later |= e ? (1u << j) : 0u;
+                for (int i = 0; i < j; ++i) {
+                    const bool e = lab[i] == lab[j];
+                    cnt[i] += e ? 1 : 0;
+                    later |= e ? (1u << j) : 0u;
+                }
             }
         }
         Key best = R::initial();
@@ -334,6 +345,7 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     if (count_dev) count = *count_dev;
+    const bool singles = singleton_partition(a);
     for (int64_t idx = gw; idx < count; idx += nw) {
         const int32_t v = list[idx];
         const int32_t b = a.g.indices[v], e = a.g.indices[v + 1], d = e - b;
@@ -343,12 +355,21 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
             if (lane == 0) push_ambiguous(a, v, d);
             continue;
         }
+        int32_t nc = 0;
+        if (singles) {  // the row as it stands: every position a candidate of count 1
+            for (int32_t i = lane; i < d; i += 32) {
+                clab[i] = a.labels[a.g.adj[b + i]];
+                ccnt[i] = 1;
+            }
+            nc = d;
+            __syncwarp();
+        }
         int32_t ts = 64;
         while (ts < 2 * d) ts <<= 1;
-        for (int i = lane; i < ts; i += 32) keys[i] = -1;
+        if (!singles)
+            for (int i = lane; i < ts; i += 32) keys[i] = -1;
         __syncwarp();
-        int32_t nc = 0;
-        for (int32_t base = b; base < e; base += 32) {
+        for (int32_t base = b; base < (singles ? b : e); base += 32) {
             const int32_t j = base + lane;
             const bool valid = j < e;
             const int32_t l = valid ? a.labels[a.g.adj[j]] : -2;
@@ -844,6 +865,7 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
     __shared__ int32_t s_nfin[NW];
     __shared__ int32_t s_amb, s_curr_freq;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const bool singles = singleton_partition(a);
     for (int32_t i = tid; i < table_cap; i += BT) {
         keys[i] = -1;
         cnts[i] = 0;
@@ -869,8 +891,9 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
             s_amb = 0;
             s_curr_freq = 0;
         }
-        // H: histogram, four gathers in flight per thread
-        for (int32_t p0 = 0; p0 < d; p0 += BT * 4) {
+        // H: histogram, four gathers in flight per thread (none for a
+        // partition of single vertices: K reads the row as it stands)
+        for (int32_t p0 = 0; p0 < (singles ? 0 : d); p0 += BT * 4) {
             int32_t lab[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
@@ -914,10 +937,10 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
             slot[i] = -1;
             lab[i] = -1;
             if (p < hi) {
-                const int32_t h = pos_slot[p];
-                if (h >= 0 && first[h] == (uint32_t)p) {
+                const int32_t h = singles ? -1 : pos_slot[p];
+                if (singles || (h >= 0 && first[h] == (uint32_t)p)) {
                     slot[i] = h;
-                    const int32_t l = keys[h], k = cnts[h];
+                    const int32_t l = singles ? a.labels[a.g.adj[b + p]] : keys[h], k = singles ? 1 : cnts[h];
                     lab[i] = l;
                     if (l == curr) {
                         s_curr_freq = k;
@@ -1058,6 +1081,7 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
     __shared__ int32_t s_amb, s_curr_freq;
     __shared__ int32_t s_vi[2];  // by iteration parity: a slot is rewritten only after every thread read it
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const bool singles = singleton_partition(a);
     K *pos_key = reinterpret_cast<K *>(gscratch + (int64_t)blockIdx.x * gstride);
     int32_t *pos_lab = reinterpret_cast<int32_t *>(pos_key + pos_cap);
     // (position, label) grouped by part; starts on an 8-byte boundary whatever pos_cap is
@@ -1102,6 +1126,25 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u) l[u] = l[u] >= 0 ? a.labels[l[u]] : -1;  // four gathers in flight
+            if (singles) {  // every position is its label's first, count 1: its key at once
+                typename R::Key raw[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    Tag tag{0, 0};
+                    const int32_t p = p0 + u * BT + tid;
+                    raw[u] = p < d && l[u] != curr ? vr.join(v, d, l[u], 1, a.cm, tag) : R::identity();
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int32_t p = p0 + u * BT + tid;
+                    if (p < d) {
+                        pos_lab[p] = l[u];
+                        pos_key[p] = l[u] != curr && R::usable(raw[u]) ? PK::make(raw[u], 1) : PK::ident();
+                        if (l[u] == curr) s_curr_freq = 1;
+                    }
+                }
+                continue;
+            }
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int32_t p = p0 + u * BT + tid;
@@ -1116,108 +1159,110 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
             }
         }
         __syncthreads();
-        if (wid == 0) {  // exclusive scan of the part sizes
-            int32_t carry = 0;
-            for (int32_t i0 = 0; i0 < parts; i0 += 32) {
-                const int32_t i = i0 + lane;
-                const int32_t c = i < parts ? s_cur[i] : 0;
-                int32_t inc = c;
+        if (!singles) {  // parts: sizes, buckets, histograms and the slot walk
+            if (wid == 0) {  // exclusive scan of the part sizes
+                int32_t carry = 0;
+                for (int32_t i0 = 0; i0 < parts; i0 += 32) {
+                    const int32_t i = i0 + lane;
+                    const int32_t c = i < parts ? s_cur[i] : 0;
+                    int32_t inc = c;
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int32_t y = __shfl_up_sync(FULL, inc, o);
-                    if (lane >= o) inc += y;
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int32_t y = __shfl_up_sync(FULL, inc, o);
+                        if (lane >= o) inc += y;
+                    }
+                    if (i < parts) s_start[i] = carry + inc - c;
+                    carry += __shfl_sync(FULL, inc, 31);
                 }
-                if (i < parts) s_start[i] = carry + inc - c;
-                carry += __shfl_sync(FULL, inc, 31);
+                if (lane == 0) s_start[parts] = carry;
             }
-            if (lane == 0) s_start[parts] = carry;
-        }
-        __syncthreads();
-        for (int32_t i = tid; i < parts; i += BT) s_cur[i] = s_start[i];
-        __syncthreads();
-        for (int32_t p0 = 0; p0 < d; p0 += BT) {  // positions into their part's bucket
-            const int32_t p = p0 + tid;
-            const int32_t pt = p < d ? (int32_t)hub_part(hash_label(pos_lab[p]), parts) : -1 - lane;
-            const unsigned peers = __match_any_sync(FULL, pt);
-            int32_t base = 0;
-            if (p < d && lane == __ffs(peers) - 1) base = atomicAdd(&s_cur[pt], __popc(peers));
-            base = __shfl_sync(FULL, base, __ffs(peers) - 1);
-            if (p < d) bucket[base + __popc(peers & lanemask_lt())] = make_int2(p, pos_lab[p]);
-        }
-        __syncthreads();
-        for (int32_t part = 0; part < parts; ++part) {
-            const int32_t i0 = s_start[part], i1 = s_start[part + 1];
-            int32_t ts = 64;
-            while (ts < 2 * (i1 - i0) && ts < table_cap) ts <<= 1;
-            // histogram of this part's labels, four bucket entries in flight per thread
-            for (int32_t j0 = i0; j0 < i1; j0 += 4 * BT) {
-              int2 eq[4];
+            __syncthreads();
+            for (int32_t i = tid; i < parts; i += BT) s_cur[i] = s_start[i];
+            __syncthreads();
+            for (int32_t p0 = 0; p0 < d; p0 += BT) {  // positions into their part's bucket
+                const int32_t p = p0 + tid;
+                const int32_t pt = p < d ? (int32_t)hub_part(hash_label(pos_lab[p]), parts) : -1 - lane;
+                const unsigned peers = __match_any_sync(FULL, pt);
+                int32_t base = 0;
+                if (p < d && lane == __ffs(peers) - 1) base = atomicAdd(&s_cur[pt], __popc(peers));
+                base = __shfl_sync(FULL, base, __ffs(peers) - 1);
+                if (p < d) bucket[base + __popc(peers & lanemask_lt())] = make_int2(p, pos_lab[p]);
+            }
+            __syncthreads();
+            for (int32_t part = 0; part < parts; ++part) {
+                const int32_t i0 = s_start[part], i1 = s_start[part + 1];
+                int32_t ts = 64;
+                while (ts < 2 * (i1 - i0) && ts < table_cap) ts <<= 1;
+                // histogram of this part's labels, four bucket entries in flight per thread
+                for (int32_t j0 = i0; j0 < i1; j0 += 4 * BT) {
+                  int2 eq[4];
 #pragma unroll
-              for (int u = 0; u < 4; ++u) {
-                  const int32_t j = j0 + u * BT + tid;
-                  eq[u] = j < i1 ? bucket[j] : make_int2(-1, -2);
-              }
+                  for (int u = 0; u < 4; ++u) {
+                      const int32_t j = j0 + u * BT + tid;
+                      eq[u] = j < i1 ? bucket[j] : make_int2(-1, -2);
+                  }
 #pragma unroll
-              for (int u = 0; u < 4; ++u) {
-                const int32_t p = eq[u].x, l = eq[u].y;
-                if (p >= 0) {
-                    uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
-                    int32_t probes = 0;
-                    for (; probes < ts; ++probes) {
-                        const int32_t kk = keys[h];
-                        if (kk == l) break;
-                        if (kk == -1) {
-                            const int32_t old = atomicCAS(&keys[h], -1, l);
-                            if (old == -1 || old == l) break;
+                  for (int u = 0; u < 4; ++u) {
+                    const int32_t p = eq[u].x, l = eq[u].y;
+                    if (p >= 0) {
+                        uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
+                        int32_t probes = 0;
+                        for (; probes < ts; ++probes) {
+                            const int32_t kk = keys[h];
+                            if (kk == l) break;
+                            if (kk == -1) {
+                                const int32_t old = atomicCAS(&keys[h], -1, l);
+                                if (old == -1 || old == l) break;
+                            }
+                            h = (h + 1) & (uint32_t)(ts - 1);
                         }
-                        h = (h + 1) & (uint32_t)(ts - 1);
+                        if (probes < ts) {
+                            atomicAdd(&cnts[h], 1);
+                            atomicMin(&first[h], (uint32_t)p);
+                        } else {
+                            atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);  // a part overfilled the table
+                        }
                     }
-                    if (probes < ts) {
-                        atomicAdd(&cnts[h], 1);
-                        atomicMin(&first[h], (uint32_t)p);
-                    } else {
-                        atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);  // a part overfilled the table
+                  }
+                }
+                __syncthreads();
+                // slot walk: each label's key at its first position; the slot is
+                // cleared.  Four slots per thread at a time, so that their
+                // community statistics gathers (in join) are in flight together.
+                for (int32_t i0 = tid; i0 < ts; i0 += 4 * BT) {
+                    int32_t lw[4], kw[4];
+                    uint32_t pw[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int32_t i = i0 + u * BT;
+                        lw[u] = i < ts ? keys[i] : -1;
+                        kw[u] = 0;
+                        pw[u] = 0;
+                        if (lw[u] != -1) {
+                            kw[u] = cnts[i];
+                            pw[u] = first[i];
+                            keys[i] = -1;
+                            cnts[i] = 0;
+                            first[i] = 0xffffffffu;
+                        }
+                    }
+                    typename R::Key raw[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        Tag tag{0, 0};
+                        raw[u] = lw[u] != -1 && lw[u] != curr ? vr.join(v, d, lw[u], kw[u], a.cm, tag) : R::identity();
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        if (lw[u] == -1) continue;
+                        if (lw[u] == curr)
+                            s_curr_freq = kw[u];
+                        else if (R::usable(raw[u]))
+                            pos_key[pw[u]] = PK::make(raw[u], kw[u]);
                     }
                 }
-              }
+                __syncthreads();
             }
-            __syncthreads();
-            // slot walk: each label's key at its first position; the slot is
-            // cleared.  Four slots per thread at a time, so that their
-            // community statistics gathers (in join) are in flight together.
-            for (int32_t i0 = tid; i0 < ts; i0 += 4 * BT) {
-                int32_t lw[4], kw[4];
-                uint32_t pw[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int32_t i = i0 + u * BT;
-                    lw[u] = i < ts ? keys[i] : -1;
-                    kw[u] = 0;
-                    pw[u] = 0;
-                    if (lw[u] != -1) {
-                        kw[u] = cnts[i];
-                        pw[u] = first[i];
-                        keys[i] = -1;
-                        cnts[i] = 0;
-                        first[i] = 0xffffffffu;
-                    }
-                }
-                typename R::Key raw[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    Tag tag{0, 0};
-                    raw[u] = lw[u] != -1 && lw[u] != curr ? vr.join(v, d, lw[u], kw[u], a.cm, tag) : R::identity();
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    if (lw[u] == -1) continue;
-                    if (lw[u] == curr)
-                        s_curr_freq = kw[u];
-                    else if (R::usable(raw[u]))
-                        pos_key[pw[u]] = PK::make(raw[u], kw[u]);
-                }
-            }
-            __syncthreads();
         }
         // ordered pass over the keyed positions, one contiguous range per warp
         const int32_t span = ((d + NW - 1) / NW + 31) & ~31;
