@@ -155,7 +155,9 @@ __device__ __forceinline__ long long alloc_ties_warp(const SweepArgs &a, int32_t
 // singleton partition).  A row's labels are then distinct (rows hold no
 // duplicate neighbours), each counted once, and a label's first occurrence is
 // its row position, so the kernels score the row as it stands, without a
-// histogram.  The flag is the same for every thread of a launch.
+// histogram.  Compress numbers communities by their first vertex, so every
+// label is then its vertex's id and a neighbour's label needs no gather.
+// The flag is the same for every thread of a launch.
 __device__ __forceinline__ bool singleton_partition(const SweepArgs &a) { return a.ctr->k == a.g.n; }
 
 template <class R, int MAXD>
@@ -175,7 +177,7 @@ __global__ void __launch_bounds__(256) k_prop_thread(SweepArgs a, R rule, const 
         for (int j = 0; j < MAXD; ++j) lab[j] = j < d ? a.g.adj[b + j] : -1;
 #pragma unroll
         for (int j = 0; j < MAXD; ++j) {
-            lab[j] = j < d ? a.labels[lab[j]] : -2 - j;  // distinct negative fillers never match
+            lab[j] = j < d ? (singles ? lab[j] : a.labels[lab[j]]) : -2 - j;  // distinct negative fillers never match
             cnt[j] = 1;
         }
         uint32_t later = 0;  // bit j: lab[j] occurred at an earlier position
@@ -358,7 +360,7 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
         int32_t nc = 0;
         if (singles) {  // the row as it stands: every position a candidate of count 1
             for (int32_t i = lane; i < d; i += 32) {
-                clab[i] = a.labels[a.g.adj[b + i]];
+                clab[i] = a.g.adj[b + i];
                 ccnt[i] = 1;
             }
             nc = d;
@@ -940,7 +942,7 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
                 const int32_t h = singles ? -1 : pos_slot[p];
                 if (singles || (h >= 0 && first[h] == (uint32_t)p)) {
                     slot[i] = h;
-                    const int32_t l = singles ? a.labels[a.g.adj[b + p]] : keys[h], k = singles ? 1 : cnts[h];
+                    const int32_t l = singles ? a.g.adj[b + p] : keys[h], k = singles ? 1 : cnts[h];
                     lab[i] = l;
                     if (l == curr) {
                         s_curr_freq = k;
@@ -1124,8 +1126,10 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                 const int32_t p = p0 + u * BT + tid;
                 l[u] = p < d ? a.g.adj[b + p] : -1;
             }
+            if (!singles) {
 #pragma unroll
-            for (int u = 0; u < 4; ++u) l[u] = l[u] >= 0 ? a.labels[l[u]] : -1;  // four gathers in flight
+                for (int u = 0; u < 4; ++u) l[u] = l[u] >= 0 ? a.labels[l[u]] : -1;  // four gathers in flight
+            }
             if (singles) {  // every position is its label's first, count 1: its key at once
                 typename R::Key raw[4];
 #pragma unroll
