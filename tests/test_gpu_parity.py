@@ -260,6 +260,50 @@ def test_every_kernel_class_matches_oracle(ctx, port, bins, gname, metric):
         assert bad.size == 0, f"sweep {a.it}: {bad.size} vertices differ, first {bad[:6]}"
 
 
+@pytest.mark.parametrize("bins", BIN_LAYOUTS, ids=lambda b: "-".join(map(str, b)))
+def test_singleton_partitions_match_oracle(ctx, port, bins):
+    """Partitions of single vertices (k = n after compress) take the sweep
+    path without histograms and the statistics without neighbour reads.
+    Besides the start of every schedule they arise from any labeling with
+    all labels distinct: a permutation of the ids, NEW_LABEL everywhere.
+    Propagation (frac 1.0 and 0.6) and merge sweeps, every rule (WCC from
+    singletons too), vertices forced into each kernel class, against the
+    oracle."""
+    import oracle
+    import pcd
+
+    g = golden_graph("rmat12")
+    port.load(g.indices, g.adj)
+    port.count_triangles()
+    G = pcd.Graph.from_csr(ctx, g.indices, g.adj)
+    G.set_bins(bins)
+    rng = np.random.default_rng(23)
+    starts = {"permutation": rng.permutation(g.n).astype(np.int32), "new labels": np.full(g.n, -1, np.int32)}
+    for metric in ("mod", "cpm-0.01", "wcc"):
+        rule = pcd.parse_metric(metric)
+        rk, lam = oracle.parse_rule(metric)
+        for name, lab in starts.items():
+            comp, k = port.compress(lab)
+            assert k == g.n
+            st = port.stats(comp)
+            G.labels = lab
+            assert G.compress() == g.n
+            s, i, e = G.stats()
+            assert np.array_equal(s, st.sizes) and np.array_equal(i, st.int_volume) and np.array_equal(e, st.ext_volume)
+            for frac in (1.0, 0.6):
+                seed = int(rng.integers(0, 2**31))
+                G.labels = lab
+                pcd.PropagationRefinement(frac).refine(G, rule, seed)
+                want = port.refine_prop(rk, lam, comp, frac, seed=seed, st=st)
+                bad = np.nonzero(G.labels != want)[0]
+                assert bad.size == 0, f"{metric} {name} frac {frac}: {bad.size} differ, first {bad[:6]}"
+            seed = int(rng.integers(0, 2**31))
+            G.labels = lab
+            pcd.MergingRefinement(1).refine(G, rule, seed)
+            assert np.array_equal(G.labels, port.refine_merge(rk, lam, comp, 1, seed=seed, st=st)), (metric, name)
+    G.free()
+
+
 def test_larger_rmat_sweeps_match_oracle(ctx, port):
     """R-MAT scale 16 (hubs above 8192 neighbours only appear at larger
     scales; the layouts above cover that class on small graphs)."""
