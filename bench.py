@@ -1043,31 +1043,83 @@ def main():
         G.free()
         torch.cuda.empty_cache()
 
-        def e2e_step(i):
+        def e2e_step(i, c=None, out=None, copy_lock=None, times=None):
             j = i % args.sweeps
-            g2 = pcd.Graph.from_host_ptr(ctx, n, m, h_ind.data_ptr(), h_adj.data_ptr())
+            out = h_out if out is None else out
+            t0 = time.perf_counter()
+            if copy_lock is None:
+                g2 = pcd.Graph.from_host_ptr(c or ctx, n, m, h_ind.data_ptr(), h_adj.data_ptr())
+            else:
+                with copy_lock:  # one copy over the host link at a time
+                    g2 = pcd.Graph.from_host_ptr(c, n, m, h_ind.data_ptr(), h_adj.data_ptr())
+            t1 = time.perf_counter()
             g2.set_labels_ptr(h_labs[j].data_ptr())
             sweep.refine(g2, rule, seeds[j])
-            g2.get_labels_ptr(h_out.data_ptr())
+            g2.get_labels_ptr(out.data_ptr())
             g2.free()
+            if times is not None:
+                times.append((t1 - t0, time.perf_counter() - t1))
             return j
+
+        # Steps on W contexts at once, one host thread per context (as the
+        # serving workers run), loads taken one at a time: while one graph is
+        # copied from the host, the other context refines the previous one
+        # (double buffering).  Step i runs on context i mod W; `check`
+        # compares every step's labels with the resident run's.
+        def e2e_run(steps, ctxs, check=False, times=None):
+            outs = [torch.empty(n, dtype=torch.int32).pin_memory() for _ in ctxs]
+            errors = []
+            copy_lock = threading.Lock() if len(ctxs) > 1 else None
+
+            def worker(w):
+                try:
+                    for i in range(w, steps, len(ctxs)):
+                        j = e2e_step(i, ctxs[w], outs[w], copy_lock, times)
+                        if check and not np.array_equal(outs[w].numpy(), results[j]):
+                            raise AssertionError(f"end-to-end sweep {j} differs from the resident run")
+                except BaseException as exc:  # re-raised on the main thread
+                    errors.append(exc)
+
+            threads = [threading.Thread(target=worker, args=(w,)) for w in range(len(ctxs))]
+            t0 = time.perf_counter()
+            for t in threads:
+                t.start()
+            for t in threads:
+                t.join()
+            sec = time.perf_counter() - t0
+            if errors:
+                raise errors[0]
+            return sec
 
         for i in range(args.sweeps):  # warm-up, and every sweep's labels against the resident run
             j = e2e_step(i)
             assert np.array_equal(h_out.numpy(), results[j]), f"end-to-end sweep {j} differs from the resident run"
+        ctx2 = pcd.Context(local)
+        pipe = [ctx, ctx2]
+        e2e_run(2 * args.sweeps, pipe, check=True)  # warm-up of the second context, checked
         if dist:
             dist.barrier()
-        t0 = time.perf_counter()
-        for i in range(args.e2e_steps):
-            e2e_step(i)
-        sec = time.perf_counter() - t0
+        sec_serial = e2e_run(args.e2e_steps, [ctx])
+        if dist:
+            dist.barrier()
+        pipe_times = []
+        sec = e2e_run(args.e2e_steps, pipe, times=pipe_times)
         sec = max_over_ranks(dist, sec, dev)
+        sec_serial = max_over_ranks(dist, sec_serial, dev)
         e2e = {"value": world * m * args.e2e_steps / sec, "unit": "edges/s",
                "h2d_bytes_per_step": int(4 * (n + 1) + 8 * m + 4 * n), "d2h_bytes_per_step": int(4 * n),
                "ms_per_step": 1000.0 * sec / args.e2e_steps,
+               "contexts": len(pipe),
+               "pipelined_host_ms": {"load (copy lock held)": round(1000.0 * statistics.mean(t[0] for t in pipe_times), 3),
+                                     "labels, refine, read-back, free": round(
+                                         1000.0 * statistics.mean(t[1] for t in pipe_times), 3)},
+               "serial": {"value": world * m * args.e2e_steps / sec_serial, "ms_per_step":
+                          1000.0 * sec_serial / args.e2e_steps},
                "note": "each step: pcd_load_csr from pinned host CSR (validation, degree bins, buffers), "
                        "pcd_labels_set (the start partition of sweep i mod S), pcd_refine, pcd_labels_get, "
-                       "pcd_graph_free; the same cycle of sweeps as value"}
+                       "pcd_graph_free; the same cycle of sweeps as value; steps on two contexts driven by "
+                       "two host threads, one load at a time, so one step's copy overlaps the other's refine "
+                       "(serial: one context)"}
         # where a step's time goes, averaged over one more cycle of the sweeps:
         # device spans of the load and of the refine call (CUDA events), host
         # time of the calls around them
@@ -1101,6 +1153,7 @@ def main():
             add("free (host)", time.perf_counter() - t0)
         ctx.profile(False)
         e2e["phases_ms"] = {k: round(1000.0 * v, 3) for k, v in ph.items()}
+        ctx2.close()
 
     batched = batched_s2 = None
     if args.batch_graphs > 0:

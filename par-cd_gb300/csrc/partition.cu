@@ -555,54 +555,111 @@ __device__ __forceinline__ int32_t bin_of(int32_t d, const BinConfig &b) {
     return NBINS - 1;
 }
 
-struct SubFlag {
-    const int32_t *indices;
-    BinConfig cfg;
-    int32_t bin, lo, hi;
-    const int32_t *vgid, *gdone;  // batch, active graphs only: vertices of finished graphs are left out
-    __device__ bool in(int64_t v) const {
-        const int32_t d = indices[v + 1] - indices[v];
-        return d > lo && d <= hi && bin_of(d, cfg) == bin && (!gdone || !gdone[vgid[v]]);
-    }
-    __device__ uint32_t operator()(int64_t v) const { return in(v) ? 1u : 0u; }
-};
-
-struct SubStore {
-    SubFlag f;
-    int32_t *out;
-    __device__ void operator()(int64_t v, uint32_t x, uint32_t) const {
-        if (f.in(v)) out[x] = (int32_t)v;
-    }
-};
-
 constexpr int MAX_SUBS = 16;
+constexpr int BIN_TILE = 256;  // vertices per block of the count and scatter passes
 struct SubBounds {
     int32_t count;
     int32_t lo[MAX_SUBS], hi[MAX_SUBS];
 };
 
-// the largest degree in each sub-range (sizes the shared tables of its launch)
-__global__ void k_sub_maxdeg(const int32_t *__restrict__ indices, int32_t n, SubBounds sb, int32_t *out,
-                             const int32_t *__restrict__ vgid, const int32_t *__restrict__ gdone) {
-    __shared__ int32_t sm[MAX_SUBS];
-    if (threadIdx.x < MAX_SUBS) sm[threadIdx.x] = 0;
-    __syncthreads();
-    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-        if (gdone && gdone[vgid[v]]) continue;
-        const int32_t d = indices[v + 1] - indices[v];
-        for (int s = 0; s < sb.count; ++s)
-            if (d > sb.lo[s] && d <= sb.hi[s]) {
-                atomicMax(&sm[s], d);
-                break;
-            }
+// The sub-range of vertex v (degree class cut at powers of two), or -1 when v
+// is left out (a batch's finished graph).
+__device__ __forceinline__ int sub_of(const int32_t *__restrict__ indices, int64_t v, const SubBounds &sb,
+                                      const int32_t *__restrict__ vgid, const int32_t *__restrict__ gdone,
+                                      int32_t &d) {
+    d = indices[v + 1] - indices[v];
+    if (gdone && gdone[vgid[v]]) return -1;
+    for (int s = 0; s < sb.count; ++s)
+        if (d > sb.lo[s] && d <= sb.hi[s]) return s;
+    return -1;
+}
+
+// Per tile of BIN_TILE vertices: its count in every sub-range (written
+// sub-major, cnt[s * ntiles + tile], so one exclusive scan gives every tile's
+// place in the class list) and the largest degree of every sub-range.
+__global__ void __launch_bounds__(BIN_TILE) k_bins_count(const int32_t *__restrict__ indices, int32_t n,
+                                                         SubBounds sb, const int32_t *__restrict__ vgid,
+                                                         const int32_t *__restrict__ gdone, int64_t ntiles,
+                                                         uint32_t *cnt, int32_t *maxdeg) {
+    __shared__ uint32_t c[MAX_SUBS];
+    __shared__ int32_t mx[MAX_SUBS];
+    if (threadIdx.x < MAX_SUBS) {
+        c[threadIdx.x] = 0;
+        mx[threadIdx.x] = 0;
     }
     __syncthreads();
-    if (threadIdx.x < MAX_SUBS && sm[threadIdx.x] > 0) atomicMax(&out[threadIdx.x], sm[threadIdx.x]);
+    const int64_t v = blockIdx.x * (int64_t)BIN_TILE + threadIdx.x;
+    if (v < n) {
+        int32_t d;
+        const int sv = sub_of(indices, v, sb, vgid, gdone, d);
+        if (sv >= 0) {
+            atomicAdd(&c[sv], 1u);
+            atomicMax(&mx[sv], d);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < sb.count) {
+        cnt[threadIdx.x * ntiles + blockIdx.x] = c[threadIdx.x];
+        if (mx[threadIdx.x] > 0) atomicMax(&maxdeg[threadIdx.x], mx[threadIdx.x]);
+    }
 }
+
+// Each vertex to its place: the tile's offset in its sub-range, plus the
+// vertices of the same sub-range before it in the tile (warps in order, lanes
+// in order), so every class list is in vertex order.
+__global__ void __launch_bounds__(BIN_TILE) k_bins_scatter(const int32_t *__restrict__ indices, int32_t n,
+                                                           SubBounds sb, const int32_t *__restrict__ vgid,
+                                                           const int32_t *__restrict__ gdone, int64_t ntiles,
+                                                           const uint32_t *__restrict__ off, int32_t *list) {
+    constexpr int NW = BIN_TILE / 32;
+    __shared__ uint32_t wc[NW][MAX_SUBS];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < NW * MAX_SUBS; i += BIN_TILE) wc[i / MAX_SUBS][i % MAX_SUBS] = 0;
+    __syncthreads();
+    const int64_t v = blockIdx.x * (int64_t)BIN_TILE + threadIdx.x;
+    int sv = -1;
+    if (v < n) {
+        int32_t d;
+        sv = sub_of(indices, v, sb, vgid, gdone, d);
+    }
+    const unsigned peers = __match_any_sync(FULL, sv);
+    const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+    if (sv >= 0 && rank == 0) wc[wid][sv] = __popc(peers);
+    __syncthreads();
+    if (threadIdx.x < sb.count) {  // exclusive prefix over the warps, per sub-range
+        uint32_t run = 0;
+        for (int w = 0; w < NW; ++w) {
+            const uint32_t x = wc[w][threadIdx.x];
+            wc[w][threadIdx.x] = run;
+            run += x;
+        }
+    }
+    __syncthreads();
+    if (sv >= 0) list[off[sv * ntiles + blockIdx.x] + wc[wid][sv] + rank] = (int32_t)v;
+}
+
+// sub-range starts in the class list (first tile of each), and the total
+__global__ void k_bins_heads(const uint32_t *__restrict__ off, int64_t ntiles, int32_t subs,
+                             const uint32_t *total, int32_t *out) {
+    const int s = threadIdx.x;
+    if (s < subs) out[s] = (int32_t)off[s * ntiles];
+    if (s == subs) out[s] = (int32_t)*total;
+}
+
+struct CntLoad {
+    const uint32_t *cnt;
+    __device__ uint32_t operator()(int64_t i) const { return cnt[i]; }
+};
+struct CntStore {
+    uint32_t *off;
+    __device__ void operator()(int64_t i, uint32_t x, uint32_t) const { off[i] = x; }
+};
 
 // Classes, and inside the warp and block classes sub-ranges at powers of two
 // (warp: 64, 128; block: 512, 1024; large block: 4096), each a stable
-// compaction of the vertices with that degree range.
+// compaction of the vertices with that degree range: one count pass, one
+// scan, one scatter pass and one read-back.  The tie buffer is the count
+// array (no sweep is in flight while the classes are built).
 int launch_bins(pcd_graph *g, cudaStream_t st, bool active_only) {
     int launches = 0;
     const int32_t *vgid = active_only && g->batch ? g->batch->vgid : nullptr;
@@ -629,26 +686,25 @@ int launch_bins(pcd_graph *g, cudaStream_t st, bool active_only) {
         sb.lo[s] = subs[(size_t)s].lo;
         sb.hi[s] = subs[(size_t)s].hi;
     }
-    int32_t *d_max = reinterpret_cast<int32_t *>(g->small);
-    cudaMemsetAsync(d_max, 0, MAX_SUBS * sizeof(int32_t), st);
-    k_sub_maxdeg<<<grid_for(g->n, 256), 256, 0, st>>>(g->indices, g->n, sb, d_max, vgid, gdone);
-    int32_t h_max[MAX_SUBS] = {0};
-    cudaMemcpyAsync(h_max, d_max, MAX_SUBS * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
-    ++launches;
-    int64_t off = 0;
+    const int64_t ntiles = ((int64_t)g->n + BIN_TILE - 1) / BIN_TILE;
+    uint32_t *cnt = reinterpret_cast<uint32_t *>(g->tiebuf);  // sb.count * ntiles <= n / 16 + 16 words
+    int32_t *d_small = reinterpret_cast<int32_t *>(g->small);  // [0, 16): largest degrees; [16, 33): heads
+    cudaMemsetAsync(d_small, 0, MAX_SUBS * sizeof(int32_t), st);
+    k_bins_count<<<(unsigned)ntiles, BIN_TILE, 0, st>>>(g->indices, g->n, sb, vgid, gdone, ntiles, cnt, d_small);
+    launches += 2 + scan_exclusive(CntLoad{cnt}, CntStore{cnt}, sb.count * ntiles, g->scan, st);
+    k_bins_scatter<<<(unsigned)ntiles, BIN_TILE, 0, st>>>(g->indices, g->n, sb, vgid, gdone, ntiles, cnt,
+                                                          g->bin_list);
+    k_bins_heads<<<1, 32, 0, st>>>(cnt, ntiles, sb.count, g->scan_total, d_small + MAX_SUBS);
+    int32_t h[2 * MAX_SUBS + 1] = {0};
+    cudaMemcpyAsync(h, d_small, sizeof(int32_t) * (2 * MAX_SUBS + 1), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
     for (int b = 0; b < NBINS; ++b) g->bin_maxdeg[b] = 0;
-    for (size_t s = 0; s < subs.size(); ++s) {
-        auto &r = subs[s];
-        const SubFlag f{g->indices, g->bins, r.bin, r.lo, r.hi, vgid, gdone};
-        launches += scan_exclusive(f, SubStore{f, g->bin_list + off}, g->n, g->scan, st);
-        uint32_t cnt = 0;
-        cudaMemcpyAsync(&cnt, g->scan_total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
-        cudaStreamSynchronize(st);
-        r.off = off;
-        r.cnt = cnt;
-        r.maxdeg = h_max[s];
+    for (int s = 0; s < sb.count; ++s) {
+        auto &r = subs[(size_t)s];
+        r.off = h[MAX_SUBS + s];
+        r.cnt = h[MAX_SUBS + s + 1] - h[MAX_SUBS + s];
+        r.maxdeg = h[s];
         g->bin_maxdeg[r.bin] = std::max(g->bin_maxdeg[r.bin], r.maxdeg);
-        off += cnt;
     }
     g->bin_off[0] = 0;
     for (int b = 0; b < NBINS; ++b) {
