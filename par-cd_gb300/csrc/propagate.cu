@@ -23,6 +23,7 @@
 // Modularity is analysed with the exact integer key of RuleModInt; vertices
 // whose outcome the key cannot decide are queued and re-analysed in FP64.
 #include <climits>
+#include <type_traits>
 
 #include "pcd_internal.h"
 #include "pcd_scan.cuh"
@@ -932,28 +933,63 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
         K key[RPL];
         int32_t slot[RPL], lab[RPL];
         K wmax = PK::ident();
+        if constexpr (std::is_same<R, RuleModInt>::value && RPL <= 4) {
+            // the integer Modularity key, its loads first: every candidate's
+            // slot, label and count, then all their community volumes, then
+            // the keys (RuleModInt::join with the volume already in hand).
+            // Up to four positions per lane: with more, the extra registers
+            // cost more than the batched loads gain.
+            int32_t kc[RPL], vv[RPL];
 #pragma unroll
-        for (int i = 0; i < RPL; ++i) {
-            const int32_t p = lo + 32 * i + lane;
-            key[i] = PK::ident();
-            slot[i] = -1;
-            lab[i] = -1;
-            if (p < hi) {
-                const int32_t h = singles ? -1 : pos_slot[p];
-                if (singles || (h >= 0 && first[h] == (uint32_t)p)) {
-                    slot[i] = h;
-                    const int32_t l = singles ? a.g.adj[b + p] : keys[h], k = singles ? 1 : cnts[h];
-                    lab[i] = l;
-                    if (l == curr) {
-                        s_curr_freq = k;
-                    } else {
-                        Tag tag{0, 0};
-                        const typename R::Key raw = vr.join(v, d, l, k, a.cm, tag);
-                        if (R::usable(raw)) key[i] = PK::make(raw, k);
+            for (int i = 0; i < RPL; ++i) {
+                const int32_t p = lo + 32 * i + lane;
+                slot[i] = -1;
+                lab[i] = -1;
+                kc[i] = 0;
+                if (p < hi) {
+                    const int32_t h = singles ? -1 : pos_slot[p];
+                    if (singles || (h >= 0 && first[h] == (uint32_t)p)) {
+                        slot[i] = h;
+                        lab[i] = singles ? a.g.adj[b + p] : keys[h];
+                        kc[i] = singles ? 1 : cnts[h];
                     }
                 }
             }
-            wmax = kmax(wmax, key[i]);
+#pragma unroll
+            for (int i = 0; i < RPL; ++i) vv[i] = lab[i] >= 0 && lab[i] != curr ? a.cm.vol[lab[i]] : 0;
+#pragma unroll
+            for (int i = 0; i < RPL; ++i) {
+                key[i] = PK::ident();
+                if (lab[i] == curr)
+                    s_curr_freq = kc[i];
+                else if (lab[i] >= 0)
+                    key[i] = PK::make(vr.two_m * kc[i] - (long long)vv[i] * d, kc[i]);
+                wmax = kmax(wmax, key[i]);
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < RPL; ++i) {
+                const int32_t p = lo + 32 * i + lane;
+                key[i] = PK::ident();
+                slot[i] = -1;
+                lab[i] = -1;
+                if (p < hi) {
+                    const int32_t h = singles ? -1 : pos_slot[p];
+                    if (singles || (h >= 0 && first[h] == (uint32_t)p)) {
+                        slot[i] = h;
+                        const int32_t l = singles ? a.g.adj[b + p] : keys[h], k = singles ? 1 : cnts[h];
+                        lab[i] = l;
+                        if (l == curr) {
+                            s_curr_freq = k;
+                        } else {
+                            Tag tag{0, 0};
+                            const typename R::Key raw = vr.join(v, d, l, k, a.cm, tag);
+                            if (R::usable(raw)) key[i] = PK::make(raw, k);
+                        }
+                    }
+                }
+                wmax = kmax(wmax, key[i]);
+            }
         }
 #pragma unroll
         for (int o = 16; o; o >>= 1) wmax = kmax(wmax, __shfl_xor_sync(FULL, wmax, o));
