@@ -63,6 +63,10 @@ struct SweepArgs {
     GraphView g;
     CommView cm;
     const int32_t *__restrict__ labels;
+    // labels again, with bit 31 set where the vertex's community is a single
+    // vertex (written by k_flag_single before the class kernels; not used
+    // for a partition of single vertices)
+    const int32_t *__restrict__ nlab;
     int32_t *new_labels;
     uint32_t *ndraw;
     int32_t *tiebuf;
@@ -904,12 +908,14 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
                 lab[u] = p < d ? a.g.adj[b + p] : -1;
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) lab[u] = lab[u] >= 0 ? a.labels[lab[u]] : -2;
+            for (int u = 0; u < 4; ++u) lab[u] = lab[u] >= 0 ? a.nlab[lab[u]] : 0;
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int32_t p = p0 + u * BT + tid;
                 const int32_t l = lab[u];
-                if (p < d) {
+                if (p < d && l < 0) {  // a single vertex's label: count 1, first at p, no table entry
+                    pos_slot[p] = l;
+                } else if (p < d) {
                     uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
                     for (;;) {
                         const int32_t kk = keys[h];
@@ -948,10 +954,13 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
                 kc[i] = 0;
                 if (p < hi) {
                     const int32_t h = singles ? -1 : pos_slot[p];
-                    if (singles || (h >= 0 && first[h] == (uint32_t)p)) {
+                    if (singles || h < 0) {  // a single vertex's label (flagged in pos_slot)
+                        lab[i] = singles ? a.g.adj[b + p] : h & 0x7fffffff;
+                        kc[i] = 1;
+                    } else if (first[h] == (uint32_t)p) {
                         slot[i] = h;
-                        lab[i] = singles ? a.g.adj[b + p] : keys[h];
-                        kc[i] = singles ? 1 : cnts[h];
+                        lab[i] = keys[h];
+                        kc[i] = cnts[h];
                     }
                 }
             }
@@ -975,9 +984,11 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
                 lab[i] = -1;
                 if (p < hi) {
                     const int32_t h = singles ? -1 : pos_slot[p];
-                    if (singles || (h >= 0 && first[h] == (uint32_t)p)) {
-                        slot[i] = h;
-                        const int32_t l = singles ? a.g.adj[b + p] : keys[h], k = singles ? 1 : cnts[h];
+                    const bool one = singles || h < 0;  // a single vertex's label (flagged in pos_slot)
+                    if (one || first[h] == (uint32_t)p) {
+                        slot[i] = one ? -1 : h;
+                        const int32_t l = singles ? a.g.adj[b + p] : (one ? h & 0x7fffffff : keys[h]);
+                        const int32_t k = one ? 1 : cnts[h];
                         lab[i] = l;
                         if (l == curr) {
                             s_curr_freq = k;
@@ -1162,9 +1173,9 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                 const int32_t p = p0 + u * BT + tid;
                 l[u] = p < d ? a.g.adj[b + p] : -1;
             }
-            if (!singles) {
+            if (!singles) {  // flagged labels: bit 31 set for a single vertex's community
 #pragma unroll
-                for (int u = 0; u < 4; ++u) l[u] = l[u] >= 0 ? a.labels[l[u]] : -1;  // four gathers in flight
+                for (int u = 0; u < 4; ++u) l[u] = l[u] >= 0 ? a.nlab[l[u]] : 0;  // four gathers in flight
             }
             if (singles) {  // every position is its label's first, count 1: its key at once
                 typename R::Key raw[4];
@@ -1185,17 +1196,30 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                 }
                 continue;
             }
+            // a single vertex's label occurs once in any row and is never the
+            // vertex's own: count 1, first at p, its key now; pos_lab keeps
+            // the flag, and the parts below skip it
+            typename R::Key raw[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                Tag tag{0, 0};
+                const int32_t p = p0 + u * BT + tid;
+                raw[u] = p < d && l[u] < 0 ? vr.join(v, d, l[u] & 0x7fffffff, 1, a.cm, tag) : R::identity();
+            }
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int32_t p = p0 + u * BT + tid;
                 int32_t pt = -1 - lane;
-                if (p < d) {
+                if (p < d && l[u] < 0) {
+                    pos_lab[p] = l[u];
+                    pos_key[p] = R::usable(raw[u]) ? PK::make(raw[u], 1) : PK::ident();
+                } else if (p < d) {
                     pos_lab[p] = l[u];
                     pos_key[p] = PK::ident();
                     pt = (int32_t)hub_part(hash_label(l[u]), parts);
                 }
                 const unsigned peers = __match_any_sync(FULL, pt);
-                if (p < d && lane == __ffs(peers) - 1) atomicAdd(&s_cur[pt], __popc(peers));
+                if (pt >= 0 && lane == __ffs(peers) - 1) atomicAdd(&s_cur[pt], __popc(peers));
             }
         }
         __syncthreads();
@@ -1221,12 +1245,13 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
             __syncthreads();
             for (int32_t p0 = 0; p0 < d; p0 += BT) {  // positions into their part's bucket
                 const int32_t p = p0 + tid;
-                const int32_t pt = p < d ? (int32_t)hub_part(hash_label(pos_lab[p]), parts) : -1 - lane;
+                const int32_t lp = p < d ? pos_lab[p] : -1;  // < 0: a single vertex's label, no bucket
+                const int32_t pt = lp >= 0 ? (int32_t)hub_part(hash_label(lp), parts) : -1 - lane;
                 const unsigned peers = __match_any_sync(FULL, pt);
                 int32_t base = 0;
-                if (p < d && lane == __ffs(peers) - 1) base = atomicAdd(&s_cur[pt], __popc(peers));
+                if (lp >= 0 && lane == __ffs(peers) - 1) base = atomicAdd(&s_cur[pt], __popc(peers));
                 base = __shfl_sync(FULL, base, __ffs(peers) - 1);
-                if (p < d) bucket[base + __popc(peers & lanemask_lt())] = make_int2(p, pos_lab[p]);
+                if (lp >= 0) bucket[base + __popc(peers & lanemask_lt())] = make_int2(p, lp);
             }
             __syncthreads();
             for (int32_t part = 0; part < parts; ++part) {
@@ -1328,7 +1353,7 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
             for (int u = 0; u < UO; ++u) {
                 const int32_t p = base0 + 32 * u + lane;
                 kq[u] = p < hi ? pos_key[p] : PK::ident();
-                lq[u] = p < hi ? pos_lab[p] : -1;
+                lq[u] = p < hi ? pos_lab[p] & 0x7fffffff : -1;  // without the single-vertex flag
             }
             __syncwarp();  // these steps' labels are read before fin_list overwrites read entries
 #pragma unroll
@@ -1415,6 +1440,17 @@ struct DrawStore {
 };
 
 __global__ void k_total_draws(DevCounters *ctr, const uint32_t *total) { ctr->total_draws = *total; }
+
+// nlab[v] = labels[v], bit 31 set when v's community is a single vertex; not
+// needed (nothing written) for a partition of single vertices
+__global__ void k_flag_single(const int32_t *__restrict__ labels, const int32_t *__restrict__ size, int32_t n,
+                              const DevCounters *ctr, int32_t *nlab) {
+    if (ctr->k == n) return;
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t l = labels[v];
+        nlab[v] = size[l] == 1 ? (int32_t)((uint32_t)l | 0x80000000u) : l;
+    }
+}
 
 // frac < 1: whether v draws its ties depends on its frac draw, which depends
 // on every earlier vertex's draw count, so each graph's stream is walked in
@@ -1853,6 +1889,7 @@ int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32
     a.g = GraphView{g->n, g->m, g->indices, g->adj, g->tri, g->tri_deg, g->cc};
     a.cm = CommView{g->sizes, g->intv, g->extv, g->vol};
     a.labels = g->labels;
+    a.nlab = g->first;  // free until the frac < 1 walk, after the class kernels
     a.new_labels = g->labels_alt;
     a.ndraw = g->ndraw;
     a.tiebuf = g->tiebuf;
@@ -1862,7 +1899,10 @@ int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32
     a.amb = g->amb;
     a.ctr = g->ctr;
     k_reset_sweep<<<1, 1, 0, st>>>(g->ctr);
-    ++launches;
+    if (g->n > 0)
+        k_flag_single<<<std::max(1, std::min<int>((g->n + 255) / 256, g->ctx->num_sms * 8)), 256, 0, st>>>(
+            g->labels, g->sizes, g->n, g->ctr, g->first);
+    launches += 2;
     prof_mark(g->ctx, "sweep.reset", st);
     if (kind == PCD_RULE_MODULARITY) {
         RuleModInt r;
