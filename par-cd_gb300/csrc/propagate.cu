@@ -379,10 +379,15 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
         for (int32_t base = b; base < (singles ? b : e); base += 32) {
             const int32_t j = base + lane;
             const bool valid = j < e;
-            const int32_t l = valid ? a.labels[a.g.adj[j]] : -2;
-            const unsigned peers = __match_any_sync(FULL, l);
-            const bool leader = valid && lane == __ffs(peers) - 1;
-            bool isnew = false;
+            // flagged labels: a single vertex's label occurs once in the row, a
+            // new candidate of count 1 without a table slot; such lanes meet
+            // in one dummy group of the match
+            const int32_t raw = valid ? a.nlab[a.g.adj[j]] : -2;
+            const bool one = valid && raw < 0;
+            const int32_t l = one ? raw & 0x7fffffff : raw;
+            const unsigned peers = __match_any_sync(FULL, one ? INT_MIN : l);
+            const bool leader = valid && !one && lane == __ffs(peers) - 1;
+            bool isnew = one;
             uint32_t h = 0;
             if (leader) {
                 h = hash_label(l) & (uint32_t)(ts - 1);
@@ -403,9 +408,9 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
             const unsigned newmask = __ballot_sync(FULL, isnew);
             if (isnew) {
                 int32_t ord = nc + __popc(newmask & lanemask_lt());
-                ords[h] = (uint8_t)ord;
+                if (!one) ords[h] = (uint8_t)ord;
                 clab[ord] = l;
-                ccnt[ord] = (uint16_t)__popc(peers);
+                ccnt[ord] = one ? (uint16_t)1 : (uint16_t)__popc(peers);
             }
             __syncwarp();
             if (leader && !isnew) ccnt[ords[h]] += (uint16_t)__popc(peers);
