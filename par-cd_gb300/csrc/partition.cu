@@ -91,8 +91,8 @@ __global__ void k_set_k(DevCounters *ctr, const uint32_t *total) { ctr->k = (int
 // The leader sums its group's counts from shared memory (a loop as long as
 // the largest group; warp reductions over per-group masks would run once per
 // distinct community of the warp).  `wsh`: this warp's 32 slots.
-__device__ __forceinline__ void add_stats(int32_t l, int32_t di, int32_t de, int32_t *sizes, int32_t *intv,
-                                          int32_t *extv, int32_t *vol, bool valid, int2 *wsh) {
+__device__ __forceinline__ void add_stats(int32_t l, int32_t di, int32_t de, int32_t *intv, int32_t *extv,
+                                          int32_t *vol, bool valid, int2 *wsh) {
     const int lane = threadIdx.x & 31;
     const unsigned peers = __match_any_sync(FULL, valid ? l : -1 - lane);
     wsh[lane] = make_int2(di, de);
@@ -104,12 +104,20 @@ __device__ __forceinline__ void add_stats(int32_t l, int32_t di, int32_t de, int
             a += x.x;
             b += x.y;
         }
-        atomicAdd(sizes + l, __popc(peers));
         atomicAdd(intv + l, a);
         atomicAdd(extv + l, b);
         atomicAdd(vol + l, a + b);
     }
     __syncwarp();
+}
+
+// Community sizes first (one pass over the listed vertices), so that the
+// volume kernels skip the neighbour labels of a vertex alone in its community:
+// it has no internal edge (no loops), all its edges are external.
+__global__ void k_stat_sizes(const int32_t *__restrict__ list, int64_t count, const int32_t *__restrict__ labels,
+                             int32_t *sizes) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(sizes + labels[list[i]], 1);
 }
 
 // `singles`: the partition has one vertex per community (k == n right after a
@@ -133,7 +141,8 @@ __global__ void k_stats_thread(const int32_t *__restrict__ indices, const int32_
             int32_t v = list[idx];
             l = labels[v];
             int32_t b = indices[v], e = indices[v + 1];
-            for (int32_t j = b; j < (singles ? b : e); j += 4) {  // four gathers in flight
+            const bool alone = singles || sizes[l] == 1;
+            for (int32_t j = b; j < (alone ? b : e); j += 4) {  // four gathers in flight
                 int32_t u[4];
 #pragma unroll
                 for (int k = 0; k < 4; ++k) u[k] = j + k < e ? adj[j + k] : -1;
@@ -142,7 +151,7 @@ __global__ void k_stats_thread(const int32_t *__restrict__ indices, const int32_
             }
             de = (e - b) - di;
         }
-        add_stats(l, di, de, sizes, intv, extv, vol, valid, wsh);
+        add_stats(l, di, de, intv, extv, vol, valid, wsh);
     }
 }
 
@@ -161,7 +170,8 @@ __global__ void k_stats_warp(const int32_t *__restrict__ indices, const int32_t 
         int32_t l = labels[v];
         int32_t b = indices[v], e = indices[v + 1];
         int32_t di = 0;
-        for (int32_t j = b + lane; j < (singles ? b : e); j += 4 * 32) {  // four gathers in flight per lane
+        const bool alone = singles || sizes[l] == 1;
+        for (int32_t j = b + lane; j < (alone ? b : e); j += 4 * 32) {  // four gathers in flight per lane
             int32_t u[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) u[k] = j + 32 * k < e ? adj[j + 32 * k] : -1;
@@ -172,7 +182,6 @@ __global__ void k_stats_warp(const int32_t *__restrict__ indices, const int32_t 
         for (int d = 16; d; d >>= 1) di += __shfl_xor_sync(FULL, di, d);
         if (lane == 0) {
             int32_t de = (e - b) - di;
-            atomicAdd(sizes + l, 1);
             atomicAdd(intv + l, di);
             atomicAdd(extv + l, de);
             atomicAdd(vol + l, e - b);
@@ -200,7 +209,8 @@ __global__ void __launch_bounds__(BT) k_stats_block(const int32_t *__restrict__ 
         const int32_t l = labels[v];
         const int32_t b = indices[v], e = indices[v + 1];
         int32_t di = 0;
-        for (int32_t j0 = b + (int32_t)threadIdx.x; j0 < (singles ? b : e); j0 += 4 * BT) {
+        const bool alone = singles || sizes[l] == 1;
+        for (int32_t j0 = b + (int32_t)threadIdx.x; j0 < (alone ? b : e); j0 += 4 * BT) {
             int32_t u[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) u[k] = j0 + k * BT < e ? adj[j0 + k * BT] : -1;
@@ -213,7 +223,6 @@ __global__ void __launch_bounds__(BT) k_stats_block(const int32_t *__restrict__ 
         if (threadIdx.x == 0) {
             int32_t t = 0;
             for (int w = 0; w < NW; ++w) t += part[w];
-            atomicAdd(sizes + l, 1);
             atomicAdd(intv + l, t);
             atomicAdd(extv + l, (e - b) - t);
             atomicAdd(vol + l, e - b);
@@ -233,6 +242,12 @@ int launch_stats(pcd_graph *g, cudaStream_t st, bool after_compress) {
     cudaMemsetAsync(g->intv, 0, bytes, st);
     cudaMemsetAsync(g->extv, 0, bytes, st);
     cudaMemsetAsync(g->vol, 0, bytes, st);
+    const int64_t listed = g->bin_off[NBINS] - g->bin_off[0];
+    if (listed > 0) {
+        k_stat_sizes<<<grid_for(listed, 256), 256, 0, st>>>(g->bin_list + g->bin_off[0], listed, g->labels, g->sizes);
+        prof_mark(g->ctx, "stats.sizes", st);
+        ++launches;
+    }
     int64_t nt = g->bin_off[BIN_WARP] - g->bin_off[0];
     if (nt > 0) {
         k_stats_thread<<<grid_for(nt, 256), 256, 0, st>>>(g->indices, g->adj, g->labels,
