@@ -205,6 +205,15 @@ struct RuleModF64 : RuleF64Base<RuleModF64> {
         double a_j = d / (2.0 * m);
         return e_ij - 2 * a_i * a_j;
     }
+    // join of a community that is one vertex (size 1, no internal edge,
+    // volume V = that vertex's degree) with k = 1: the same operations as
+    // join() with those statistics, which the caller already holds
+    __device__ Key join_one(int32_t, int32_t d, int32_t V, Tag &) const {
+        double e_ij = 1 / (double)m;
+        double a_i = V / (2.0 * m);
+        double a_j = d / (2.0 * m);
+        return e_ij - 2 * a_i * a_j;
+    }
     __device__ double leave(int32_t, int32_t d, int32_t c, int32_t k, const CommView &cm) const {
         double e_ij = k / (double)m;
         double a_i = (cm.vol[c] - d) / (2.0 * m);
@@ -225,6 +234,7 @@ struct RuleCPM : RuleF64Base<RuleCPM> {
     __device__ Key join(int32_t, int32_t, int32_t c, int32_t k, const CommView &cm, Tag &) const {
         return k - lambda * cm.size[c];
     }
+    __device__ Key join_one(int32_t, int32_t, int32_t, Tag &) const { return 1 - lambda * 1; }
     __device__ double leave(int32_t, int32_t, int32_t c, int32_t k, const CommView &cm) const {
         return -(k - lambda * (cm.size[c] - 1));
     }
@@ -239,6 +249,10 @@ struct RuleWCC : RuleF64Base<RuleWCC> {
     __device__ void set_graph(int32_t g) { cc = bv.gcc[g]; }
     __device__ Key join(int32_t, int32_t d, int32_t c, int32_t k, const CommView &cm, Tag &) const {
         return wcc_improvement(1, cm.size[c], 1, k, 0, cm.intv[c] / 2, k, d, cm.extv[c], cc);
+    }
+    // a one-vertex community: size 1, internal volume 0, external volume V
+    __device__ Key join_one(int32_t, int32_t d, int32_t V, Tag &) const {
+        return wcc_improvement(1, 1, 1, 1, 0, 0, 1, d, V, cc);
     }
     __device__ double leave(int32_t, int32_t d, int32_t c, int32_t k, const CommView &cm) const {
         return -wcc_improvement(1, cm.size[c] - 1, 1, k, 0, cm.intv[c] / 2 - k, k, d,
@@ -294,6 +308,11 @@ struct RuleModInt {
         tag.k = k;
         tag.V = V;
         return two_m * k - (long long)V * d;
+    }
+    __device__ Key join_one(int32_t, int32_t d, int32_t V, Tag &tag) const {
+        tag.k = 1;
+        tag.V = V;
+        return two_m - (long long)V * d;
     }
     __device__ int32_t decide(Key best, bool has_best, int32_t, int32_t d, int32_t curr, int32_t curr_freq,
                               const CommView &cm) const {

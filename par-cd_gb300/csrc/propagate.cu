@@ -63,9 +63,9 @@ struct SweepArgs {
     GraphView g;
     CommView cm;
     const int32_t *__restrict__ labels;
-    // labels again, with bit 31 set where the vertex's community is a single
-    // vertex (written by k_flag_single before the class kernels; not used
-    // for a partition of single vertices)
+    // labels again, except that a vertex whose community is itself alone
+    // holds that community's volume with bit 31 set (written by k_flag_single
+    // before the class kernels; not used for a partition of single vertices)
     const int32_t *__restrict__ nlab;
     int32_t *new_labels;
     uint32_t *ndraw;
@@ -277,6 +277,61 @@ __device__ __forceinline__ K kmax(K a, K b) {
     return a > b ? a : b;
 }
 
+// One 32-candidate step of the ordered pass (src/refinement.cpp:150-166 over
+// packed keys: `score > best` takes the candidate, `score == best` is a tie
+// and one rand_r draw).  carry: the packed running maximum before the step
+// (equal levels keep the larger count); t: the ties so far; amb: a tie whose
+// two gains the integer key cannot tell apart; lfin: the level of the final
+// maximum.  A lane whose level is below the carry's can neither tie nor raise
+// it, so only the other ("active") lanes are looked at:
+//   * none: nothing to do;
+//   * the carry already at the final level: no candidate can pass it, so
+//     every active lane ties with it.  The carry is left as it is: once its
+//     level is final, a tie is ambiguous exactly when its count differs from
+//     the carry's (an earlier tie with another count already was);
+//   * up to three: walked one by one in lane order, as the reference loop;
+//   * more: an inclusive max-scan over the warp.
+// Every branch is warp-uniform (carry, lfin and the ballot are).
+template <class PK, class L>
+__device__ __forceinline__ void ordered_step(typename PK::K key, bool cand, L lfin, typename PK::K &carry,
+                                             uint32_t &t, bool &amb, int lane) {
+    using K = typename PK::K;
+    const unsigned act = __ballot_sync(FULL, cand && PK::level(key) >= PK::level(carry));
+    if (!act) return;
+    if (PK::level(carry) == lfin) {
+        t += __popc(act);
+        if (((act >> lane) & 1u) && PK::tie_ambiguous(key, carry)) amb = true;
+        return;
+    }
+    if (__popc(act) <= 3) {
+        unsigned rest = act;
+        while (rest) {
+            const int j = __ffs(rest) - 1;
+            rest &= rest - 1;
+            const K kj = __shfl_sync(FULL, key, j);
+            if (PK::level(kj) == PK::level(carry)) {
+                ++t;
+                if (PK::tie_ambiguous(kj, carry)) amb = true;
+            }
+            carry = kmax(carry, kj);
+        }
+        return;
+    }
+    K inc = key;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const K y = __shfl_up_sync(FULL, inc, o);
+        if (lane >= o) inc = kmax(inc, y);
+    }
+    K ex = __shfl_up_sync(FULL, inc, 1);
+    if (lane == 0) ex = PK::ident();
+    const K pre = kmax(carry, ex);
+    const bool tie = cand && PK::level(key) == PK::level(pre);
+    if (tie && PK::tie_ambiguous(key, pre)) amb = true;
+    t += __popc(__ballot_sync(FULL, tie));
+    carry = kmax(carry, __shfl_sync(FULL, inc, 31));
+}
+
 // Per-warp results of a block, combined by every warp from one shared load
 // per lane and a shuffle scan (rather than every thread reading all NW
 // entries).  carry: the maximum of `init` and the maxima of the warps before
@@ -379,12 +434,13 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
         for (int32_t base = b; base < (singles ? b : e); base += 32) {
             const int32_t j = base + lane;
             const bool valid = j < e;
-            // flagged labels: a single vertex's label occurs once in the row, a
-            // new candidate of count 1 without a table slot; such lanes meet
-            // in one dummy group of the match
-            const int32_t raw = valid ? a.nlab[a.g.adj[j]] : -2;
-            const bool one = valid && raw < 0;
-            const int32_t l = one ? raw & 0x7fffffff : raw;
+            // flagged entries: a single vertex's community occurs once in the
+            // row, a new candidate of count 1 without a table slot; such lanes
+            // meet in one dummy group of the match.  Its candidate entry keeps
+            // the flag word (the volume) and, in place of the count, the row
+            // position, from which the label is read back if it is needed.
+            const int32_t l = valid ? a.nlab[a.g.adj[j]] : -2;
+            const bool one = valid && l < 0;
             const unsigned peers = __match_any_sync(FULL, one ? INT_MIN : l);
             const bool leader = valid && !one && lane == __ffs(peers) - 1;
             bool isnew = one;
@@ -410,7 +466,7 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
                 int32_t ord = nc + __popc(newmask & lanemask_lt());
                 if (!one) ords[h] = (uint8_t)ord;
                 clab[ord] = l;
-                ccnt[ord] = one ? (uint16_t)1 : (uint16_t)__popc(peers);
+                ccnt[ord] = one ? (uint16_t)(j - b) : (uint16_t)__popc(peers);
             }
             __syncwarp();
             if (leader && !isnew) ccnt[ords[h]] += (uint16_t)__popc(peers);
@@ -433,7 +489,11 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
             key[c] = PK::ident();
             if (i < nc) {
                 const int32_t l = clab[i], k = ccnt[i];
-                if (l == curr) {
+                if (l < 0) {  // a single vertex's community: count 1, volume in the flag word
+                    Tag tag{0, 0};
+                    const Key raw = vr.join_one(v, d, l & 0x7fffffff, tag);
+                    if (R::usable(raw)) key[c] = PK::make(raw, 1);
+                } else if (l == curr) {
                     my_curr = k;
                 } else {
                     Tag tag{0, 0};
@@ -458,22 +518,12 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
             const bool cand = key[c] != PK::ident();
             const bool fin = cand && PK::level(key[c]) == lfin;
             const unsigned fm = __ballot_sync(FULL, fin);
-            if (fin) ties[nfin + __popc(fm & lanemask_lt())] = clab[i];
-            nfin += __popc(fm);
-            if (!__any_sync(FULL, cand && PK::level(key[c]) >= PK::level(carry))) continue;
-            K inc = key[c];
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const K y = __shfl_up_sync(FULL, inc, o);
-                if (lane >= o) inc = kmax(inc, y);
+            if (fin) {
+                const int32_t l = clab[i];
+                ties[nfin + __popc(fm & lanemask_lt())] = l >= 0 ? l : a.labels[a.g.adj[b + ccnt[i]]];
             }
-            K ex = __shfl_up_sync(FULL, inc, 1);
-            if (lane == 0) ex = PK::ident();
-            const K pre = kmax(carry, ex);
-            const bool tie = cand && PK::level(key[c]) == PK::level(pre);
-            if (tie && PK::tie_ambiguous(key[c], pre)) amb = true;
-            t += __popc(__ballot_sync(FULL, tie));
-            carry = kmax(carry, __shfl_sync(FULL, inc, 31));
+            nfin += __popc(fm);
+            ordered_step<PK>(key[c], cand, lfin, carry, t, amb, lane);
         }
         __syncwarp();
         amb = __any_sync(FULL, amb);
@@ -834,7 +884,8 @@ __global__ void __launch_bounds__(BT) k_prop_block(SweepArgs a, R rule, const in
 // candidates by gain and let a plain maximum carry what the tie logic needs:
 //   Modularity (exact integer gain N): (N << 14) | k.  |N| <= 2m d <= 2^48
 //     (larger m d goes to the FP64 path first), so the shift cannot overflow,
-//     and k <= d <= 8192 fits the low 14 bits exactly.  Among keys of one
+//     and k <= d <= 8192 fits the low 14 bits exactly (a hub whose count
+//     passes 14 bits is decided in FP64).  Among keys of one
 //     gain level the maximum carries the largest k seen; a tie whose k differs
 //     from it meets a holder with another (k, volume) pair -- equal integer
 //     gain, possibly unequal FP64 gains -- and is re-evaluated in FP64.  The
@@ -918,8 +969,8 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
             for (int u = 0; u < 4; ++u) {
                 const int32_t p = p0 + u * BT + tid;
                 const int32_t l = lab[u];
-                if (p < d && l < 0) {  // a single vertex's label: count 1, first at p, no table entry
-                    pos_slot[p] = l;
+                if (p < d && l < 0) {  // a single vertex's community: count 1, first at p, no table entry
+                    pos_slot[p] = l;   // the flag word (its volume)
                 } else if (p < d) {
                     uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
                     for (;;) {
@@ -949,7 +1000,9 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
             // slot, label and count, then all their community volumes, then
             // the keys (RuleModInt::join with the volume already in hand).
             // Up to four positions per lane: with more, the extra registers
-            // cost more than the batched loads gain.
+            // cost more than the batched loads gain.  A single vertex's
+            // community (flagged in pos_slot) brings its volume along; its
+            // label (lab -2 until then) is read back only at the final level.
             int32_t kc[RPL], vv[RPL];
 #pragma unroll
             for (int i = 0; i < RPL; ++i) {
@@ -957,11 +1010,16 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
                 slot[i] = -1;
                 lab[i] = -1;
                 kc[i] = 0;
+                vv[i] = 0;
                 if (p < hi) {
                     const int32_t h = singles ? -1 : pos_slot[p];
-                    if (singles || h < 0) {  // a single vertex's label (flagged in pos_slot)
-                        lab[i] = singles ? a.g.adj[b + p] : h & 0x7fffffff;
+                    if (singles) {
+                        lab[i] = a.g.adj[b + p];
                         kc[i] = 1;
+                    } else if (h < 0) {
+                        lab[i] = -2;
+                        kc[i] = 1;
+                        vv[i] = h & 0x7fffffff;
                     } else if (first[h] == (uint32_t)p) {
                         slot[i] = h;
                         lab[i] = keys[h];
@@ -970,13 +1028,14 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
                 }
             }
 #pragma unroll
-            for (int i = 0; i < RPL; ++i) vv[i] = lab[i] >= 0 && lab[i] != curr ? a.cm.vol[lab[i]] : 0;
+            for (int i = 0; i < RPL; ++i)
+                if (lab[i] >= 0 && lab[i] != curr) vv[i] = a.cm.vol[lab[i]];
 #pragma unroll
             for (int i = 0; i < RPL; ++i) {
                 key[i] = PK::ident();
                 if (lab[i] == curr)
                     s_curr_freq = kc[i];
-                else if (lab[i] >= 0)
+                else if (lab[i] != -1)
                     key[i] = PK::make(vr.two_m * kc[i] - (long long)vv[i] * d, kc[i]);
                 wmax = kmax(wmax, key[i]);
             }
@@ -989,11 +1048,15 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
                 lab[i] = -1;
                 if (p < hi) {
                     const int32_t h = singles ? -1 : pos_slot[p];
-                    const bool one = singles || h < 0;  // a single vertex's label (flagged in pos_slot)
-                    if (one || first[h] == (uint32_t)p) {
-                        slot[i] = one ? -1 : h;
-                        const int32_t l = singles ? a.g.adj[b + p] : (one ? h & 0x7fffffff : keys[h]);
-                        const int32_t k = one ? 1 : cnts[h];
+                    if (!singles && h < 0) {  // a single vertex's community: its volume in the flag word
+                        lab[i] = -2;
+                        Tag tag{0, 0};
+                        const typename R::Key raw = vr.join_one(v, d, h & 0x7fffffff, tag);
+                        if (R::usable(raw)) key[i] = PK::make(raw, 1);
+                    } else if (singles || first[h] == (uint32_t)p) {
+                        slot[i] = singles ? -1 : h;
+                        const int32_t l = singles ? a.g.adj[b + p] : keys[h];
+                        const int32_t k = singles ? 1 : cnts[h];
                         lab[i] = l;
                         if (l == curr) {
                             s_curr_freq = k;
@@ -1030,22 +1093,11 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
             const bool cand = key[i] != PK::ident();
             const bool fin = cand && PK::level(key[i]) == lfin;
             const unsigned fm = __ballot_sync(FULL, fin);
-            if (fin) fin_list[nfin + __popc(fm & lanemask_lt())] = lab[i];
+            if (fin)  // a single vertex's community (lab -2): its label read back now
+                fin_list[nfin + __popc(fm & lanemask_lt())] =
+                    lab[i] >= 0 ? lab[i] : a.labels[a.g.adj[b + lo + 32 * i + lane]];
             nfin += __popc(fm);
-            if (!__any_sync(FULL, cand && PK::level(key[i]) >= PK::level(carry))) continue;
-            K inc = key[i];
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const K y = __shfl_up_sync(FULL, inc, o);
-                if (lane >= o) inc = kmax(inc, y);
-            }
-            K ex = __shfl_up_sync(FULL, inc, 1);
-            if (lane == 0) ex = PK::ident();
-            const K pre = kmax(carry, ex);
-            const bool tie = cand && PK::level(key[i]) == PK::level(pre);
-            if (tie && PK::tie_ambiguous(key[i], pre)) amb = true;
-            t += __popc(__ballot_sync(FULL, tie));
-            carry = kmax(carry, __shfl_sync(FULL, inc, 31));
+            ordered_step<PK>(key[i], cand, lfin, carry, t, amb, lane);
         }
         amb = __any_sync(FULL, amb);
         if (lane == 0) {
@@ -1201,15 +1253,16 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                 }
                 continue;
             }
-            // a single vertex's label occurs once in any row and is never the
-            // vertex's own: count 1, first at p, its key now; pos_lab keeps
-            // the flag, and the parts below skip it
+            // a single vertex's community occurs once in any row and is never
+            // the vertex's own: count 1, first at p, its key now from the
+            // volume in the flag word; pos_lab keeps the flag word, the parts
+            // below skip it, and its label is read back at the final level
             typename R::Key raw[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 Tag tag{0, 0};
                 const int32_t p = p0 + u * BT + tid;
-                raw[u] = p < d && l[u] < 0 ? vr.join(v, d, l[u] & 0x7fffffff, 1, a.cm, tag) : R::identity();
+                raw[u] = p < d && l[u] < 0 ? vr.join_one(v, d, l[u] & 0x7fffffff, tag) : R::identity();
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
@@ -1329,6 +1382,9 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                             s_curr_freq = kw[u];
                         else if (R::usable(raw[u]))
                             pos_key[pw[u]] = PK::make(raw[u], kw[u]);
+                        // a candidate's count past the packed key's 14 bits:
+                        // the vertex is decided in FP64 (its keys are not used)
+                        if (std::is_same<R, RuleModInt>::value && lw[u] != curr && kw[u] > 0x3FFF) s_amb = 1;
                     }
                 }
                 __syncthreads();
@@ -1358,7 +1414,7 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
             for (int u = 0; u < UO; ++u) {
                 const int32_t p = base0 + 32 * u + lane;
                 kq[u] = p < hi ? pos_key[p] : PK::ident();
-                lq[u] = p < hi ? pos_lab[p] & 0x7fffffff : -1;  // without the single-vertex flag
+                lq[u] = p < hi ? pos_lab[p] : -1;  // < 0: a single vertex's flag word
             }
             __syncwarp();  // these steps' labels are read before fin_list overwrites read entries
 #pragma unroll
@@ -1367,22 +1423,11 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                 const bool cand = key != PK::ident();
                 const bool fin = cand && PK::level(key) == lfin;
                 const unsigned fm = __ballot_sync(FULL, fin);
-                if (fin) fin_list[nfin + __popc(fm & lanemask_lt())] = lq[u];
+                if (fin)  // a single vertex's community: its label read back now
+                    fin_list[nfin + __popc(fm & lanemask_lt())] =
+                        lq[u] >= 0 ? lq[u] : a.labels[a.g.adj[b + base0 + 32 * u + lane]];
                 nfin += __popc(fm);
-                if (!__any_sync(FULL, cand && PK::level(key) >= PK::level(carry))) continue;
-                K inc = key;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const K y = __shfl_up_sync(FULL, inc, o);
-                    if (lane >= o) inc = kmax(inc, y);
-                }
-                K ex = __shfl_up_sync(FULL, inc, 1);
-                if (lane == 0) ex = PK::ident();
-                const K pre = kmax(carry, ex);
-                const bool tie = cand && PK::level(key) == PK::level(pre);
-                if (tie && PK::tie_ambiguous(key, pre)) amb = true;
-                t += __popc(__ballot_sync(FULL, tie));
-                carry = kmax(carry, __shfl_sync(FULL, inc, 31));
+                ordered_step<PK>(key, cand, lfin, carry, t, amb, lane);
             }
         }
         amb = __any_sync(FULL, amb);
@@ -1446,14 +1491,17 @@ struct DrawStore {
 
 __global__ void k_total_draws(DevCounters *ctr, const uint32_t *total) { ctr->total_draws = *total; }
 
-// nlab[v] = labels[v], bit 31 set when v's community is a single vertex; not
-// needed (nothing written) for a partition of single vertices
-__global__ void k_flag_single(const int32_t *__restrict__ labels, const int32_t *__restrict__ size, int32_t n,
-                              const DevCounters *ctr, int32_t *nlab) {
+// nlab[v] = labels[v], or, when v's community is v alone, its volume with bit
+// 31 set (the community's statistics are then size 1, no internal edge and
+// that volume, so a candidate's gain needs nothing else; its label is read
+// back only if it reaches the final level); not needed (nothing written) for
+// a partition of single vertices
+__global__ void k_flag_single(const int32_t *__restrict__ labels, const int32_t *__restrict__ size,
+                              const int32_t *__restrict__ vol, int32_t n, const DevCounters *ctr, int32_t *nlab) {
     if (ctr->k == n) return;
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
         const int32_t l = labels[v];
-        nlab[v] = size[l] == 1 ? (int32_t)((uint32_t)l | 0x80000000u) : l;
+        nlab[v] = size[l] == 1 ? (int32_t)((uint32_t)vol[l] | 0x80000000u) : l;
     }
 }
 
@@ -1906,7 +1954,7 @@ int launch_refine(pcd_graph *g, int32_t kind, double lambda, double frac, uint32
     k_reset_sweep<<<1, 1, 0, st>>>(g->ctr);
     if (g->n > 0)
         k_flag_single<<<std::max(1, std::min<int>((g->n + 255) / 256, g->ctx->num_sms * 8)), 256, 0, st>>>(
-            g->labels, g->sizes, g->n, g->ctr, g->first);
+            g->labels, g->sizes, g->vol, g->n, g->ctr, g->first);
     launches += 2;
     prof_mark(g->ctx, "sweep.reset", st);
     if (kind == PCD_RULE_MODULARITY) {

@@ -401,3 +401,45 @@ def test_block_variants_by_degree_match_oracle(ctx, port, D):
         for a, b in zip(got, want):
             bad = np.nonzero(a.raw != b.raw)[0]
             assert bad.size == 0, f"D={D} {metric} sweep {a.it}: {bad.size} differ"
+
+
+def test_hub_label_count_past_key_width_matches_oracle(ctx, port):
+    """A hub whose row holds one community 20,000 times (more than the 14 bits
+    the packed integer Modularity key keeps for a count) beside 500 single-vertex
+    communities: the hub is decided in FP64, and every label of the sweep equals
+    the oracle's, for Modularity and CPM."""
+    import graphs
+    import oracle
+    import pcd
+
+    A, S = 20000, 500
+    hub_edges = [(0, u) for u in range(1, A + S + 1)]
+    ring = [(u, u + 1) for u in range(1, A)]
+    rng = np.random.default_rng(5)
+    tail = rng.integers(A + 1, A + S + 1, size=(2 * S, 2))
+    g = graphs.convert_edges(np.concatenate([np.array(hub_edges + ring), tail]))
+    assert int(np.diff(g.indices).max()) >= A + S
+    lab = np.arange(g.n, dtype=np.int32)
+    # the converter renumbers vertices: find the hub by its degree, and put
+    # its neighbours of degree 3 (the ring's interior, with a few tail
+    # vertices) in one community
+    deg = np.diff(g.indices)
+    hub = int(np.argmax(deg))
+    nbr = g.adj[g.indices[hub]:g.indices[hub + 1]]
+    three = nbr[deg[nbr] == 3]
+    assert three.size > 0x3FFF
+    lab[three] = lab[three[0]]
+    G = pcd.Graph.from_csr(ctx, g.indices, g.adj)
+    port.load(g.indices, g.adj)
+    comp, _ = port.compress(lab)
+    st = port.stats(comp)
+    assert int(np.bincount(comp)[comp[hub]]) == 1
+    for rule_s in ("mod", "cpm-0.0001"):
+        rk, lam = oracle.parse_rule(rule_s)
+        for seed in (3, 77):
+            G.labels = comp
+            pcd.PropagationRefinement(1.0).refine(G, pcd.parse_metric(rule_s), seed)
+            mine = G.labels
+            theirs = port.refine_prop(rk, lam, comp, 1.0, seed=seed, st=st)
+            assert np.array_equal(mine, theirs), (rule_s, seed, int(np.sum(mine != theirs)))
+    G.free()
