@@ -114,6 +114,17 @@ __device__ __forceinline__ void write_decision(const SweepArgs &a, int32_t v, in
     a.new_labels[v] = dec == DEC_MOVE ? holder : (dec == DEC_NEW ? -1 : curr);
 }
 
+// Final-level candidates are listed as labels, or, for a single vertex's
+// community (whose gain came from the volume in its flag word), as the row
+// position with bit 31 set: the label is read from the row only where a
+// decision or a tie record needs it.  `row` = indices[v].
+__device__ __forceinline__ int32_t fin_entry(int32_t label, int32_t pos) {
+    return label >= 0 ? label : (int32_t)(0x80000000u | (uint32_t)pos);
+}
+__device__ __forceinline__ int32_t fin_label(const SweepArgs &a, int32_t row, int32_t x) {
+    return x >= 0 ? x : a.labels[a.g.adj[row + (x & 0x7fffffff)]];
+}
+
 // Warp-aggregated allocation of tie records: every lane that passes
 // want = r + 1 > 0 gets its own offset in the tie buffer and a record slot.
 // Returns the offset (or -1).  All lanes of the warp must call it.
@@ -518,10 +529,7 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
             const bool cand = key[c] != PK::ident();
             const bool fin = cand && PK::level(key[c]) == lfin;
             const unsigned fm = __ballot_sync(FULL, fin);
-            if (fin) {
-                const int32_t l = clab[i];
-                ties[nfin + __popc(fm & lanemask_lt())] = l >= 0 ? l : a.labels[a.g.adj[b + ccnt[i]]];
-            }
+            if (fin) ties[nfin + __popc(fm & lanemask_lt())] = fin_entry(clab[i], ccnt[i]);
             nfin += __popc(fm);
             ordered_step<PK>(key[c], cand, lfin, carry, t, amb, lane);
         }
@@ -529,7 +537,7 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
         amb = __any_sync(FULL, amb);
         const int32_t curr_freq = __reduce_add_sync(FULL, my_curr);
         const bool has = mreal != PK::ident() && PK::level(mreal) > PK::level(PK::init());
-        const int32_t holder = has ? ties[0] : -1;
+        const int32_t holder = has ? ties[0] : -1;  // a fin_entry: resolved where it is used
         const int32_t r = has ? nfin - 1 : 0;
         int32_t dec = DEC_AMBIGUOUS;
         if constexpr (R::kExactInt) {  // integer decision: cheaper in every lane than a broadcast
@@ -546,12 +554,13 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
         const bool rec = dec == DEC_MOVE && r > 0;
         const long long off = rec ? (long long)b + v : -1;
         if (lane == 0) {
+            const int32_t hl = dec == DEC_MOVE ? fin_label(a, b, holder) : holder;
             a.ndraw[v] = t;
-            write_decision(a, v, dec, holder, curr);
-            record_ties(a, v, b, rec, r, holder);
+            write_decision(a, v, dec, hl, curr);
+            record_ties(a, v, b, rec, r, hl);
         }
         if (off >= 0)
-            for (int32_t j = lane; j < r; j += 32) a.tiebuf[off + 1 + j] = ties[1 + j];
+            for (int32_t j = lane; j < r; j += 32) a.tiebuf[off + 1 + j] = fin_label(a, b, ties[1 + j]);
         __syncwarp();
     }
 }
@@ -1093,9 +1102,8 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
             const bool cand = key[i] != PK::ident();
             const bool fin = cand && PK::level(key[i]) == lfin;
             const unsigned fm = __ballot_sync(FULL, fin);
-            if (fin)  // a single vertex's community (lab -2): its label read back now
-                fin_list[nfin + __popc(fm & lanemask_lt())] =
-                    lab[i] >= 0 ? lab[i] : a.labels[a.g.adj[b + lo + 32 * i + lane]];
+            if (fin)  // a single vertex's community (lab -2) is listed by its position
+                fin_list[nfin + __popc(fm & lanemask_lt())] = fin_entry(lab[i], lo + 32 * i + lane);
             nfin += __popc(fm);
             ordered_step<PK>(key[i], cand, lfin, carry, t, amb, lane);
         }
@@ -1114,7 +1122,7 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
         // the holder is the first final-level candidate: entry 0 of the first
         // range that has one (that range's warp has not overwritten it: only
         // its own entries >= 0 are written, and entry 0 is the holder itself)
-        const int32_t holder = has_best ? pos_slot[hw * span] : -1;
+        const int32_t holder = has_best ? pos_slot[hw * span] : -1;  // a fin_entry
         const int32_t r = has_best ? nf - 1 : 0;
         int32_t dec = DEC_AMBIGUOUS;
         if constexpr (R::kExactInt) {  // integer decision: cheaper in every lane than a broadcast
@@ -1134,16 +1142,17 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
             if (dec == DEC_AMBIGUOUS) {
                 push_ambiguous(a, v, d);
             } else {
+                const int32_t hl = dec == DEC_MOVE ? fin_label(a, b, holder) : holder;
                 a.ndraw[v] = tt;
-                write_decision(a, v, dec, holder, curr);
-                record_ties(a, v, b, rec, r, holder);
+                write_decision(a, v, dec, hl, curr);
+                record_ties(a, v, b, rec, r, hl);
             }
         }
         if (rec) {  // the same number of iterations in every lane
             const long long off = (long long)b + v;  // record_ties' slots: holder, then the ties
             for (int32_t j0 = 0; j0 < nfin; j0 += 32) {
                 const int32_t j = j0 + lane, gi = before + j;  // 0 is the holder
-                if (j < nfin && gi > 0) a.tiebuf[off + gi] = fin_list[j];
+                if (j < nfin && gi > 0) a.tiebuf[off + gi] = fin_label(a, b, fin_list[j]);
             }
         }
         __syncthreads();
@@ -1153,9 +1162,13 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
 // ---------------------------------------------------------------------------
 // Hubs: 1024-thread blocks (one per SM) that take hubs from a queue in list
 // order (largest first), so one very large hub does not leave the others to a
-// fixed share of the blocks.  A hub's labels are split by hash into P parts of
-// at most part_labels distinct labels; each part is histogrammed in the shared
-// table (label, count, first position: every bucket entry inserts itself,
+// fixed share of the blocks.  The gather pass keys every single vertex's
+// community at once (count 1, volume in its flag word) and counts the other
+// entries; those are split by hash into P parts of at most part_labels of
+// them (one part, the usual case once most neighbours are single vertices,
+// reads the positions straight from pos_lab; more parts are bucketed first);
+// each part is histogrammed in the shared
+// table (label, count, first position: every entry inserts itself,
 // with shared-memory atomics for the count and the minimum position, since
 // bucket order is not position order), then the table is walked once in slot
 // order: each label's packed key is written at its first position and the
@@ -1184,7 +1197,7 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
     __shared__ K s_agg[NW];
     __shared__ uint32_t s_t[NW];
     __shared__ int32_t s_nfin[NW];
-    __shared__ int32_t s_amb, s_curr_freq;
+    __shared__ int32_t s_amb, s_curr_freq, s_nrest;
     __shared__ int32_t s_vi[2];  // by iteration parity: a slot is rewritten only after every thread read it
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const bool singles = singleton_partition(a);
@@ -1215,14 +1228,15 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
             if (tid == 0) atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);
             continue;
         }
-        const int32_t parts = min(HUB_MAX_PARTS, max(1, (d + part_labels - 1) / part_labels));
-        for (int32_t i = tid; i < parts; i += BT) s_cur[i] = 0;
         if (tid == 0) {
             s_amb = 0;
             s_curr_freq = 0;
+            s_nrest = 0;
         }
         __syncthreads();
-        // the row's labels by position (gathered once) and the part sizes
+        // the row's labels by position (gathered once), and how many are not
+        // a single vertex's community (those go through the parts)
+        int32_t nrest = 0;
         for (int32_t p0 = 0; p0 < d; p0 += BT * 4) {
             int32_t l[4];
 #pragma unroll
@@ -1267,22 +1281,40 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int32_t p = p0 + u * BT + tid;
-                int32_t pt = -1 - lane;
-                if (p < d && l[u] < 0) {
+                if (p < d) {
                     pos_lab[p] = l[u];
-                    pos_key[p] = R::usable(raw[u]) ? PK::make(raw[u], 1) : PK::ident();
-                } else if (p < d) {
-                    pos_lab[p] = l[u];
-                    pos_key[p] = PK::ident();
-                    pt = (int32_t)hub_part(hash_label(l[u]), parts);
+                    pos_key[p] = l[u] < 0 && R::usable(raw[u]) ? PK::make(raw[u], 1) : PK::ident();
+                    nrest += l[u] >= 0;
                 }
+            }
+        }
+        if (!singles) {
+            nrest = __reduce_add_sync(FULL, nrest);
+            if (lane == 0 && nrest) atomicAdd(&s_nrest, nrest);
+        }
+        __syncthreads();
+        // parts of at most part_labels labels, by hash; one part needs no buckets
+        const int32_t nr = s_nrest;
+        const int32_t parts = min(HUB_MAX_PARTS, max(1, (nr + part_labels - 1) / part_labels));
+        if (!singles && nr > 0 && parts > 1) {  // part sizes
+            for (int32_t i = tid; i < parts; i += BT) s_cur[i] = 0;
+            __syncthreads();
+            for (int32_t p0 = 0; p0 < d; p0 += BT) {
+                const int32_t p = p0 + tid;
+                const int32_t lp = p < d ? pos_lab[p] : -1;
+                const int32_t pt = lp >= 0 ? (int32_t)hub_part(hash_label(lp), parts) : -1 - lane;
                 const unsigned peers = __match_any_sync(FULL, pt);
                 if (pt >= 0 && lane == __ffs(peers) - 1) atomicAdd(&s_cur[pt], __popc(peers));
             }
+            __syncthreads();
         }
-        __syncthreads();
-        if (!singles) {  // parts: sizes, buckets, histograms and the slot walk
-            if (wid == 0) {  // exclusive scan of the part sizes
+        if (!singles && nr > 0) {  // parts: buckets, histograms and the slot walk
+            if (parts == 1) {
+                if (tid == 0) {
+                    s_start[0] = 0;
+                    s_start[1] = d;  // the positions themselves, read straight from pos_lab
+                }
+            } else if (wid == 0) {  // exclusive scan of the part sizes
                 int32_t carry = 0;
                 for (int32_t i0 = 0; i0 < parts; i0 += 32) {
                     const int32_t i = i0 + lane;
@@ -1299,30 +1331,38 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                 if (lane == 0) s_start[parts] = carry;
             }
             __syncthreads();
-            for (int32_t i = tid; i < parts; i += BT) s_cur[i] = s_start[i];
-            __syncthreads();
-            for (int32_t p0 = 0; p0 < d; p0 += BT) {  // positions into their part's bucket
-                const int32_t p = p0 + tid;
-                const int32_t lp = p < d ? pos_lab[p] : -1;  // < 0: a single vertex's label, no bucket
-                const int32_t pt = lp >= 0 ? (int32_t)hub_part(hash_label(lp), parts) : -1 - lane;
-                const unsigned peers = __match_any_sync(FULL, pt);
-                int32_t base = 0;
-                if (lp >= 0 && lane == __ffs(peers) - 1) base = atomicAdd(&s_cur[pt], __popc(peers));
-                base = __shfl_sync(FULL, base, __ffs(peers) - 1);
-                if (lp >= 0) bucket[base + __popc(peers & lanemask_lt())] = make_int2(p, lp);
+            if (parts > 1) {
+                for (int32_t i = tid; i < parts; i += BT) s_cur[i] = s_start[i];
+                __syncthreads();
+                for (int32_t p0 = 0; p0 < d; p0 += BT) {  // positions into their part's bucket
+                    const int32_t p = p0 + tid;
+                    const int32_t lp = p < d ? pos_lab[p] : -1;  // < 0: a single vertex's label, no bucket
+                    const int32_t pt = lp >= 0 ? (int32_t)hub_part(hash_label(lp), parts) : -1 - lane;
+                    const unsigned peers = __match_any_sync(FULL, pt);
+                    int32_t base = 0;
+                    if (lp >= 0 && lane == __ffs(peers) - 1) base = atomicAdd(&s_cur[pt], __popc(peers));
+                    base = __shfl_sync(FULL, base, __ffs(peers) - 1);
+                    if (lp >= 0) bucket[base + __popc(peers & lanemask_lt())] = make_int2(p, lp);
+                }
+                __syncthreads();
             }
-            __syncthreads();
             for (int32_t part = 0; part < parts; ++part) {
+                // one part: the row's positions [0, d), its single vertices skipped
                 const int32_t i0 = s_start[part], i1 = s_start[part + 1];
                 int32_t ts = 64;
-                while (ts < 2 * (i1 - i0) && ts < table_cap) ts <<= 1;
-                // histogram of this part's labels, four bucket entries in flight per thread
+                while (ts < 2 * (parts == 1 ? nr : i1 - i0) && ts < table_cap) ts <<= 1;
+                // histogram of this part's labels, four entries in flight per thread
                 for (int32_t j0 = i0; j0 < i1; j0 += 4 * BT) {
                   int2 eq[4];
 #pragma unroll
                   for (int u = 0; u < 4; ++u) {
                       const int32_t j = j0 + u * BT + tid;
-                      eq[u] = j < i1 ? bucket[j] : make_int2(-1, -2);
+                      if (parts == 1) {
+                          const int32_t lp = j < i1 ? pos_lab[j] : -1;
+                          eq[u] = make_int2(lp >= 0 ? j : -1, lp);
+                      } else {
+                          eq[u] = j < i1 ? bucket[j] : make_int2(-1, -2);
+                      }
                   }
 #pragma unroll
                   for (int u = 0; u < 4; ++u) {
@@ -1423,9 +1463,8 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                 const bool cand = key != PK::ident();
                 const bool fin = cand && PK::level(key) == lfin;
                 const unsigned fm = __ballot_sync(FULL, fin);
-                if (fin)  // a single vertex's community: its label read back now
-                    fin_list[nfin + __popc(fm & lanemask_lt())] =
-                        lq[u] >= 0 ? lq[u] : a.labels[a.g.adj[b + base0 + 32 * u + lane]];
+                if (fin)  // a single vertex's community is listed by its position
+                    fin_list[nfin + __popc(fm & lanemask_lt())] = fin_entry(lq[u], base0 + 32 * u + lane);
                 nfin += __popc(fm);
                 ordered_step<PK>(key, cand, lfin, carry, t, amb, lane);
             }
@@ -1441,7 +1480,7 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
         int32_t nf, before, hw;
         warp_totals<NW>(s_t, s_nfin, wid, lane, tt, nf, before, hw);
         const bool has_best = mreal != PK::ident() && PK::level(mreal) > PK::level(PK::init());
-        const int32_t holder = has_best && hw >= 0 ? pos_lab[hw * span] : -1;
+        const int32_t holder = has_best && hw >= 0 ? pos_lab[hw * span] : -1;  // a fin_entry
         const int32_t r = has_best ? nf - 1 : 0;
         int32_t dec = DEC_AMBIGUOUS;
         if constexpr (R::kExactInt) {  // integer decision: cheaper in every lane than a broadcast
@@ -1461,16 +1500,17 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
             if (dec == DEC_AMBIGUOUS) {
                 push_ambiguous(a, v, d);
             } else {
+                const int32_t hl = dec == DEC_MOVE ? fin_label(a, b, holder) : holder;
                 a.ndraw[v] = tt;
-                write_decision(a, v, dec, holder, curr);
-                record_ties(a, v, b, rec, r, holder);
+                write_decision(a, v, dec, hl, curr);
+                record_ties(a, v, b, rec, r, hl);
             }
         }
         if (rec) {  // the same number of iterations in every lane
             const long long off = (long long)b + v;
             for (int32_t j0 = 0; j0 < nfin; j0 += 32) {
                 const int32_t j = j0 + lane, gi = before + j;  // 0 is the holder
-                if (j < nfin && gi > 0) a.tiebuf[off + gi] = fin_list[j];
+                if (j < nfin && gi > 0) a.tiebuf[off + gi] = fin_label(a, b, fin_list[j]);
             }
         }
         __syncthreads();

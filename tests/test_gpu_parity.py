@@ -443,3 +443,26 @@ def test_hub_label_count_past_key_width_matches_oracle(ctx, port):
             theirs = port.refine_prop(rk, lam, comp, 1.0, seed=seed, st=st)
             assert np.array_equal(mine, theirs), (rule_s, seed, int(np.sum(mine != theirs)))
     G.free()
+
+
+@pytest.mark.parametrize("part", [1024, 8192])
+def test_hub_parts_match_oracle(ctx, port, part):
+    """Every row above 32 neighbours in the hub class, its other-than-single
+    entries split into parts of at most `part` (several parts on the planted
+    9,000-neighbour rows at 1,024, one part at 8,192): Modularity and CPM
+    sweeps against the oracle."""
+    import oracle
+    import pcd
+
+    g = _planted_degree_graph(9000)
+    for metric in ("mod", "cpm-0.05"):
+        G = pcd.Graph.from_csr(ctx, g.indices, g.adj)
+        G.set_bins([4, 8, 16, 32, 32, 32, 32])
+        G.set_hub_part(part)
+        got = []
+        pcd.run(G, pcd.parse_metric(metric), 0, 1.0, 1, 4, keep_raw=True, callback=got.append)
+        G.free()
+        _, _, want = oracle.run_schedule(port, g.indices, g.adj, metric, 0, 1.0, 1, 4)
+        for a, b in zip(got, want):
+            bad = np.nonzero(a.raw != b.raw)[0]
+            assert bad.size == 0, f"part {part} {metric} sweep {a.it}: {bad.size} differ"
