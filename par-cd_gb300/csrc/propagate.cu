@@ -902,24 +902,30 @@ __global__ void __launch_bounds__(BT) k_prop_block(SweepArgs a, R rule, const in
 //   FP64 rules: the gain itself (NaN gains are not candidates).
 // ---------------------------------------------------------------------------
 // ---------------------------------------------------------------------------
-// block per vertex, one keyed pass (degrees up to NW * 32 * RPL).
-//   H  histogram: every position inserts its label into the shared table
-//      (positions with one label meet in one slot, one CAS wins; count and
-//      first position by shared-memory atomics); pos_slot[p] = the slot of p's
-//      label.  (Pre-aggregating equal labels across the warp with match_any
-//      cost more than the atomics it saved: R-MAT scale 24, large-block class
-//      4.99 -> 4.54 ms without it.)
-//   K  every warp owns a contiguous position range, RPL positions per lane in
-//      registers; a position is a candidate iff first[slot] == p.  Packed keys
-//      and the range maximum; one barrier, then every warp knows its carry-in
-//      (the initial 0.0 and the maxima of the ranges before it) and the final
-//      maximum.
+// block per vertex, one keyed pass (degrees up to NW * 32 * RPL).  Every warp
+// owns a contiguous range of the row, RPL positions per lane in registers
+// (p = lo + 32 i + lane: each step of a warp reads 32 consecutive neighbours).
+//   H  the range's neighbour labels, all RPL gathers in flight; a single
+//      vertex's community (flag word) is a candidate of count 1 at once, its
+//      key from the volume in the flag word; every other label is inserted
+//      into the shared table (positions with one label meet in one slot, one
+//      CAS wins; count and first position by shared-memory atomics).
+//      (Pre-aggregating equal labels across the warp with match_any cost more
+//      than the atomics it saved: R-MAT scale 24, large-block class 4.99 ->
+//      4.54 ms without it.)
+//   K  one barrier, then a table position is a candidate iff first[slot] ==
+//      p; packed keys and the range maximum; one barrier, then every warp
+//      knows its carry-in (the initial 0.0 and the maxima of the ranges
+//      before it) and the final maximum.
 //   S  ordered pass over the range from the carry-in: ties with the running
 //      maximum (one rand_r draw each), FP64 ambiguity, and the final level's
-//      candidates (holder first, then its ties) compacted into the range's own
-//      consumed pos_slot entries.  The table slots are cleared here.
+//      candidates (holder first, then its ties) listed in the range's own
+//      part of fin_all.  The table slots are cleared here.
 //   Every warp then derives the same decision from the per-warp totals; warp
-//   0 writes it and each warp writes its share of the final-level ties.
+//   0 writes it and each warp writes its share of the final-level ties.  No
+//   barrier closes a vertex: the next vertex's H only touches the table
+//   (cleared before the S barrier) and registers, so warps that finish early
+//   start loading the next row; the per-vertex flags alternate by parity.
 // ---------------------------------------------------------------------------
 template <class R, int BT, int RPL>
 __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const int32_t *__restrict__ list,
@@ -931,11 +937,11 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
     int32_t *keys = smem;
     int32_t *cnts = smem + table_cap;
     uint32_t *first = reinterpret_cast<uint32_t *>(smem + 2 * table_cap);
-    int32_t *pos_slot = smem + 3 * table_cap;  // NW * 32 * RPL entries
+    int32_t *fin_all = smem + 3 * table_cap;  // NW * 32 * RPL entries: each range's final-level list
     __shared__ K s_agg[NW];
     __shared__ uint32_t s_t[NW];
     __shared__ int32_t s_nfin[NW];
-    __shared__ int32_t s_amb, s_curr_freq;
+    __shared__ int32_t s_amb[2], s_curr_freq[2];  // by the parity of the analysed vertex
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const bool singles = singleton_partition(a);
     for (int32_t i = tid; i < table_cap; i += BT) {
@@ -943,7 +949,12 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
         cnts[i] = 0;
         first[i] = 0xffffffffu;
     }
+    if (tid == 0) {
+        s_amb[0] = 0;
+        s_curr_freq[0] = 0;
+    }
     __syncthreads();
+    int par = 0;
     for (int64_t vi = blockIdx.x; vi < count; vi += gridDim.x) {
         const int32_t v = list[vi];
         const int32_t b = a.g.indices[v], d = a.g.indices[v + 1] - b;
@@ -959,28 +970,36 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
             if (tid == 0) atomicOr(&a.ctr->error, ERR_SCRATCH_OVERFLOW);
             continue;
         }
-        if (tid == 0) {
-            s_amb = 0;
-            s_curr_freq = 0;
+        const int32_t span = ((d + NW - 1) / NW + 31) & ~31;
+        const int32_t lo = min(d, wid * span), hi = min(d, lo + span);
+        // H: labels of the range (a partition of single vertices: the row as
+        // it stands, every position a candidate of count 1)
+        int32_t lab[RPL], slot[RPL];
+        K key[RPL];
+#pragma unroll
+        for (int i = 0; i < RPL; ++i) {
+            const int32_t p = lo + 32 * i + lane;
+            lab[i] = p < hi ? a.g.adj[b + p] : -1;
         }
-        // H: histogram, four gathers in flight per thread (none for a
-        // partition of single vertices: K reads the row as it stands)
-        for (int32_t p0 = 0; p0 < (singles ? 0 : d); p0 += BT * 4) {
-            int32_t lab[4];
+        if (!singles) {
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int32_t p = p0 + u * BT + tid;
-                lab[u] = p < d ? a.g.adj[b + p] : -1;
-            }
+            for (int i = 0; i < RPL; ++i) lab[i] = lab[i] >= 0 ? a.nlab[lab[i]] : -1;
+        }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) lab[u] = lab[u] >= 0 ? a.nlab[lab[u]] : 0;
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int32_t p = p0 + u * BT + tid;
-                const int32_t l = lab[u];
-                if (p < d && l < 0) {  // a single vertex's community: count 1, first at p, no table entry
-                    pos_slot[p] = l;   // the flag word (its volume)
-                } else if (p < d) {
+        for (int i = 0; i < RPL; ++i) {
+            const int32_t p = lo + 32 * i + lane;
+            key[i] = PK::ident();
+            slot[i] = -1;
+            if (p >= hi) {
+                lab[i] = -1;
+            } else if (!singles) {
+                const int32_t l = lab[i];
+                if (l < 0) {  // a single vertex's community: count 1, first here
+                    Tag tag{0, 0};
+                    const typename R::Key raw = vr.join_one(v, d, l & 0x7fffffff, tag);
+                    if (R::usable(raw)) key[i] = PK::make(raw, 1);
+                    lab[i] = -2;  // listed by its position if it reaches the final level
+                } else {
                     uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
                     for (;;) {
                         const int32_t kk = keys[h];
@@ -993,87 +1012,57 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
                     }
                     atomicAdd(&cnts[h], 1);
                     atomicMin(&first[h], (uint32_t)p);
-                    pos_slot[p] = (int32_t)h;
+                    slot[i] = (int32_t)h;
                 }
             }
         }
         __syncthreads();
-        // K: candidates of this warp's range
-        const int32_t span = ((d + NW - 1) / NW + 31) & ~31;
-        const int32_t lo = min(d, wid * span), hi = min(d, lo + span);
-        K key[RPL];
-        int32_t slot[RPL], lab[RPL];
+        if (tid == 0) {  // the next vertex's flags (the last reads of this parity were before the barrier)
+            s_amb[par ^ 1] = 0;
+            s_curr_freq[par ^ 1] = 0;
+        }
+        // K: the table's candidates (a label's first position), their keys
+        // and the range maximum
         K wmax = PK::ident();
-        if constexpr (std::is_same<R, RuleModInt>::value && RPL <= 4) {
-            // the integer Modularity key, its loads first: every candidate's
-            // slot, label and count, then all their community volumes, then
-            // the keys (RuleModInt::join with the volume already in hand).
-            // Up to four positions per lane: with more, the extra registers
-            // cost more than the batched loads gain.  A single vertex's
-            // community (flagged in pos_slot) brings its volume along; its
-            // label (lab -2 until then) is read back only at the final level.
-            int32_t kc[RPL], vv[RPL];
+        int32_t kc[RPL];
 #pragma unroll
-            for (int i = 0; i < RPL; ++i) {
-                const int32_t p = lo + 32 * i + lane;
-                slot[i] = -1;
-                lab[i] = -1;
-                kc[i] = 0;
-                vv[i] = 0;
-                if (p < hi) {
-                    const int32_t h = singles ? -1 : pos_slot[p];
-                    if (singles) {
-                        lab[i] = a.g.adj[b + p];
-                        kc[i] = 1;
-                    } else if (h < 0) {
-                        lab[i] = -2;
-                        kc[i] = 1;
-                        vv[i] = h & 0x7fffffff;
-                    } else if (first[h] == (uint32_t)p) {
-                        slot[i] = h;
-                        lab[i] = keys[h];
-                        kc[i] = cnts[h];
-                    }
-                }
+        for (int i = 0; i < RPL; ++i) {
+            const int32_t p = lo + 32 * i + lane;
+            kc[i] = 0;
+            if (singles) {
+                if (p < hi) kc[i] = 1;
+            } else if (slot[i] >= 0) {
+                if (first[slot[i]] == (uint32_t)p)
+                    kc[i] = cnts[slot[i]];
+                else
+                    slot[i] = -1;  // cleared by the label's first position
             }
+        }
+        if constexpr (std::is_same<R, RuleModInt>::value && RPL <= 4) {
+            // the integer Modularity key, the community volumes loaded together
+            int32_t vv[RPL];
 #pragma unroll
-            for (int i = 0; i < RPL; ++i)
-                if (lab[i] >= 0 && lab[i] != curr) vv[i] = a.cm.vol[lab[i]];
+            for (int i = 0; i < RPL; ++i) vv[i] = kc[i] > 0 && lab[i] != curr ? a.cm.vol[lab[i]] : 0;
 #pragma unroll
             for (int i = 0; i < RPL; ++i) {
-                key[i] = PK::ident();
-                if (lab[i] == curr)
-                    s_curr_freq = kc[i];
-                else if (lab[i] != -1)
-                    key[i] = PK::make(vr.two_m * kc[i] - (long long)vv[i] * d, kc[i]);
+                if (kc[i] > 0) {
+                    if (lab[i] == curr)
+                        s_curr_freq[par] = kc[i];
+                    else
+                        key[i] = PK::make(vr.two_m * kc[i] - (long long)vv[i] * d, kc[i]);
+                }
                 wmax = kmax(wmax, key[i]);
             }
         } else {
 #pragma unroll
             for (int i = 0; i < RPL; ++i) {
-                const int32_t p = lo + 32 * i + lane;
-                key[i] = PK::ident();
-                slot[i] = -1;
-                lab[i] = -1;
-                if (p < hi) {
-                    const int32_t h = singles ? -1 : pos_slot[p];
-                    if (!singles && h < 0) {  // a single vertex's community: its volume in the flag word
-                        lab[i] = -2;
+                if (kc[i] > 0) {
+                    if (lab[i] == curr) {
+                        s_curr_freq[par] = kc[i];
+                    } else {
                         Tag tag{0, 0};
-                        const typename R::Key raw = vr.join_one(v, d, h & 0x7fffffff, tag);
-                        if (R::usable(raw)) key[i] = PK::make(raw, 1);
-                    } else if (singles || first[h] == (uint32_t)p) {
-                        slot[i] = singles ? -1 : h;
-                        const int32_t l = singles ? a.g.adj[b + p] : keys[h];
-                        const int32_t k = singles ? 1 : cnts[h];
-                        lab[i] = l;
-                        if (l == curr) {
-                            s_curr_freq = k;
-                        } else {
-                            Tag tag{0, 0};
-                            const typename R::Key raw = vr.join(v, d, l, k, a.cm, tag);
-                            if (R::usable(raw)) key[i] = PK::make(raw, k);
-                        }
+                        const typename R::Key raw = vr.join(v, d, lab[i], kc[i], a.cm, tag);
+                        if (R::usable(raw)) key[i] = PK::make(raw, kc[i]);
                     }
                 }
                 wmax = kmax(wmax, key[i]);
@@ -1090,7 +1079,7 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
         uint32_t t = 0;
         int32_t nfin = 0;
         bool amb = false;
-        int32_t *fin_list = pos_slot + lo;  // this range's entries were all read in K
+        int32_t *fin_list = fin_all + lo;
 #pragma unroll
         for (int i = 0; i < RPL; ++i) {
             if (lo + 32 * i >= hi) break;
@@ -1102,16 +1091,22 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
             const bool cand = key[i] != PK::ident();
             const bool fin = cand && PK::level(key[i]) == lfin;
             const unsigned fm = __ballot_sync(FULL, fin);
-            if (fin)  // a single vertex's community (lab -2) is listed by its position
-                fin_list[nfin + __popc(fm & lanemask_lt())] = fin_entry(lab[i], lo + 32 * i + lane);
-            nfin += __popc(fm);
-            ordered_step<PK>(key[i], cand, lfin, carry, t, amb, lane);
+            if (fm) {  // a single vertex's community (lab -2) is listed by its position
+                if (fin) fin_list[nfin + __popc(fm & lanemask_lt())] = fin_entry(lab[i], lo + 32 * i + lane);
+                nfin += __popc(fm);
+            }
+            if (PK::level(carry) == lfin) {  // nothing passes the carry: the final level ties with it
+                t += __popc(fm);
+                if (fin && PK::tie_ambiguous(key[i], carry)) amb = true;
+            } else {
+                ordered_step<PK>(key[i], cand, lfin, carry, t, amb, lane);
+            }
         }
         amb = __any_sync(FULL, amb);
         if (lane == 0) {
             s_t[wid] = t;
             s_nfin[wid] = nfin;
-            if (amb) s_amb = 1;
+            if (amb) s_amb[par] = 1;
         }
         __syncthreads();
         // every warp: the same totals and decision
@@ -1120,20 +1115,21 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
         warp_totals<NW>(s_t, s_nfin, wid, lane, tt, nf, before, hw);
         const bool has_best = mreal != PK::ident() && PK::level(mreal) > PK::level(PK::init());
         // the holder is the first final-level candidate: entry 0 of the first
-        // range that has one (that range's warp has not overwritten it: only
-        // its own entries >= 0 are written, and entry 0 is the holder itself)
-        const int32_t holder = has_best ? pos_slot[hw * span] : -1;  // a fin_entry
+        // range that has one (a fin_entry)
+        const int32_t holder = has_best ? fin_all[hw * span] : -1;
         const int32_t r = has_best ? nf - 1 : 0;
+        const int32_t curr_freq = s_curr_freq[par];
+        const bool any_amb = s_amb[par] != 0;
         int32_t dec = DEC_AMBIGUOUS;
         if constexpr (R::kExactInt) {  // integer decision: cheaper in every lane than a broadcast
-            if (!s_amb) {
+            if (!any_amb) {
                 const typename R::Key best = has_best ? PK::raw_level(mreal) : R::initial();
-                dec = vr.decide(best, has_best, v, d, curr, s_curr_freq, a.cm);
+                dec = vr.decide(best, has_best, v, d, curr, curr_freq, a.cm);
             }
         } else {  // FP64 leave gain: one lane per warp evaluates it
-            if (!s_amb && lane == 0) {
+            if (!any_amb && lane == 0) {
                 const typename R::Key best = has_best ? PK::raw_level(mreal) : R::initial();
-                dec = vr.decide(best, has_best, v, d, curr, s_curr_freq, a.cm);
+                dec = vr.decide(best, has_best, v, d, curr, curr_freq, a.cm);
             }
             dec = __shfl_sync(FULL, dec, 0);
         }
@@ -1155,7 +1151,7 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
                 if (j < nfin && gi > 0) a.tiebuf[off + gi] = fin_label(a, b, fin_list[j]);
             }
         }
-        __syncthreads();
+        par ^= 1;
     }
 }
 
