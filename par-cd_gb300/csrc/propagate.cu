@@ -343,6 +343,25 @@ __device__ __forceinline__ void ordered_step(typename PK::K key, bool cand, L lf
     carry = kmax(carry, __shfl_sync(FULL, inc, 31));
 }
 
+// The same step with per-lane tallies: when no candidate of the step passes
+// the running maximum (the usual case once a few have been seen), every
+// candidate at the carry's level ties with it; the lane counts its own in
+// t_lane / a_lane, and the caller reduces them once after the pass.  A step
+// in which one passes runs in order (ordered_step).
+template <class PK, class L>
+__device__ __forceinline__ void tally_step(typename PK::K key, bool cand, L lfin, typename PK::K &carry,
+                                           uint32_t &t, bool &amb, uint32_t &t_lane, bool &a_lane, int lane) {
+    const auto cl = PK::level(carry);
+    const auto lv = PK::level(key);
+    if (__any_sync(FULL, cand && lv > cl)) {
+        ordered_step<PK>(key, cand, lfin, carry, t, amb, lane);
+    } else {
+        const bool eq = cand && lv == cl;
+        t_lane += eq;
+        a_lane |= eq && PK::tie_ambiguous(key, carry);
+    }
+}
+
 // Per-warp results of a block, combined by every warp from one shared load
 // per lane and a shuffle scan (rather than every thread reading all NW
 // entries).  carry: the maximum of `init` and the maxima of the warps before
@@ -918,17 +937,33 @@ __global__ void __launch_bounds__(BT) k_prop_block(SweepArgs a, R rule, const in
 //      knows its carry-in (the initial 0.0 and the maxima of the ranges
 //      before it) and the final maximum.
 //   S  ordered pass over the range from the carry-in: ties with the running
-//      maximum (one rand_r draw each), FP64 ambiguity, and the final level's
-//      candidates (holder first, then its ties) listed in the range's own
-//      part of fin_all.  The table slots are cleared here.
-//   Every warp then derives the same decision from the per-warp totals; warp
-//   0 writes it and each warp writes its share of the final-level ties.  No
-//   barrier closes a vertex: the next vertex's H only touches the table
-//   (cleared before the S barrier) and registers, so warps that finish early
-//   start loading the next row; the per-vertex flags alternate by parity.
+//      maximum (one rand_r draw each), FP64 ambiguity and the number of the
+//      final level's candidates.  A range whose maximum is below its
+//      carry-in has none; once the carry holds the final level, every
+//      final-level candidate ties with it (in larger blocks tallied per lane
+//      and reduced once).  The table slots are cleared here.
+//   Every warp then derives the same decision from the per-warp totals.  For
+//   a move, each range lists its final-level candidates from its registers:
+//   the first of all (the holder) is the new label, and with ties every one
+//   goes to the tie buffer at its rank.  No barrier closes a vertex: the
+//   next vertex's H only touches the table (cleared before the S barrier)
+//   and registers, so warps that finish early start loading the next row;
+//   the per-vertex flags alternate by parity.
 // ---------------------------------------------------------------------------
+// Blocks per SM the register budget is set for: 512-thread variants two (64
+// registers a thread), 256-thread ones with three or four positions per lane
+// five (48); the others, and WCC's FP64 gain, leave it to the compiler
+template <class R>
+constexpr int block1_min_blocks(int bt, int rpl) {
+    return std::is_same<R, RuleWCC>::value ? 0 : bt == 512 ? 2 : bt == 256 && (rpl == 3 || rpl == 4) ? 5 : 0;
+}
+template <class R>
+constexpr bool block1_lists_in_pass(int bt) {
+    return bt == 256 || std::is_same<R, RuleWCC>::value;
+}
+
 template <class R, int BT, int RPL>
-__global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const int32_t *__restrict__ list,
+__global__ void __launch_bounds__(BT, block1_min_blocks<R>(BT, RPL)) k_prop_block1(SweepArgs a, R rule, const int32_t *__restrict__ list,
                                                     int64_t count, int32_t table_cap) {
     using PK = PackedKey<R>;
     using K = typename PK::K;
@@ -937,7 +972,13 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
     int32_t *keys = smem;
     int32_t *cnts = smem + table_cap;
     uint32_t *first = reinterpret_cast<uint32_t *>(smem + 2 * table_cap);
-    int32_t *fin_all = smem + 3 * table_cap;  // NW * 32 * RPL entries: each range's final-level list
+    // 256-thread blocks (and WCC, whose FP64 gain needs the registers) list
+    // the final level's candidates in the ordered pass (fin_all: each range's
+    // list at its own positions), so their keys and labels need not stay in
+    // registers until the decision; larger blocks, whose ordered pass holds
+    // most of their time, list them only for a move
+    constexpr bool kListInS = block1_lists_in_pass<R>(BT);
+    int32_t *fin_all = smem + 3 * table_cap;  // NW * 32 * RPL entries when kListInS
     __shared__ K s_agg[NW];
     __shared__ uint32_t s_t[NW];
     __shared__ int32_t s_nfin[NW];
@@ -1075,31 +1116,54 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
         K carry, mreal;
         warp_carry_in<PK, NW>(s_agg, wid, lane, carry, mreal);
         const auto lfin = PK::level(kmax(PK::init(), mreal));
-        // S: ordered ties, final-level candidates, table clearing
-        uint32_t t = 0;
-        int32_t nfin = 0;
-        bool amb = false;
-        int32_t *fin_list = fin_all + lo;
+        // S: table clearing; ties with the running maximum and the final
+        // level's candidates of this range (listed in the tail, and only when
+        // the vertex moves).  A range whose maximum is below the carry-in has
+        // neither; once the carry holds the final level, the final level's
+        // candidates all tie with it, tallied per lane and reduced once.
 #pragma unroll
-        for (int i = 0; i < RPL; ++i) {
-            if (lo + 32 * i >= hi) break;
+        for (int i = 0; i < RPL; ++i)
             if (slot[i] >= 0) {
                 keys[slot[i]] = -1;
                 cnts[slot[i]] = 0;
                 first[slot[i]] = 0xffffffffu;
             }
-            const bool cand = key[i] != PK::ident();
-            const bool fin = cand && PK::level(key[i]) == lfin;
-            const unsigned fm = __ballot_sync(FULL, fin);
-            if (fm) {  // a single vertex's community (lab -2) is listed by its position
-                if (fin) fin_list[nfin + __popc(fm & lanemask_lt())] = fin_entry(lab[i], lo + 32 * i + lane);
-                nfin += __popc(fm);
+        uint32_t t = 0;
+        int32_t nfin = 0;
+        bool amb = false;
+        if (wmax != PK::ident() && PK::level(wmax) >= PK::level(carry)) {
+            int32_t c_fin = 0;
+            bool a_fin = false;
+#pragma unroll
+            for (int i = 0; i < RPL; ++i) {
+                if (lo + 32 * i >= hi) break;
+                const bool cand = key[i] != PK::ident();
+                const bool fin = cand && PK::level(key[i]) == lfin;
+                if constexpr (kListInS) {  // a single vertex's community (lab -2) is listed by its position
+                    const unsigned fm = __ballot_sync(FULL, fin);
+                    if (fm) {
+                        if (fin) fin_all[lo + nfin + __popc(fm & lanemask_lt())] = fin_entry(lab[i], lo + 32 * i + lane);
+                        nfin += __popc(fm);
+                    }
+                    if (PK::level(carry) == lfin) {  // nothing passes the carry: the final level ties with it
+                        t += __popc(fm);
+                        if (fin && PK::tie_ambiguous(key[i], carry)) amb = true;
+                    } else {
+                        ordered_step<PK>(key[i], cand, lfin, carry, t, amb, lane);
+                    }
+                } else if (PK::level(carry) == lfin) {  // the same, tallied per lane and reduced once
+                    c_fin += fin;
+                    a_fin |= fin && PK::tie_ambiguous(key[i], carry);
+                } else {
+                    nfin += __popc(__ballot_sync(FULL, fin));
+                    ordered_step<PK>(key[i], cand, lfin, carry, t, amb, lane);
+                }
             }
-            if (PK::level(carry) == lfin) {  // nothing passes the carry: the final level ties with it
-                t += __popc(fm);
-                if (fin && PK::tie_ambiguous(key[i], carry)) amb = true;
-            } else {
-                ordered_step<PK>(key[i], cand, lfin, carry, t, amb, lane);
+            if (!kListInS) {
+                c_fin = __reduce_add_sync(FULL, c_fin);
+                nfin += c_fin;
+                t += (uint32_t)c_fin;
+                amb |= a_fin;
             }
         }
         amb = __any_sync(FULL, amb);
@@ -1114,9 +1178,6 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
         int32_t nf, before, hw;
         warp_totals<NW>(s_t, s_nfin, wid, lane, tt, nf, before, hw);
         const bool has_best = mreal != PK::ident() && PK::level(mreal) > PK::level(PK::init());
-        // the holder is the first final-level candidate: entry 0 of the first
-        // range that has one (a fin_entry)
-        const int32_t holder = has_best ? fin_all[hw * span] : -1;
         const int32_t r = has_best ? nf - 1 : 0;
         const int32_t curr_freq = s_curr_freq[par];
         const bool any_amb = s_amb[par] != 0;
@@ -1134,21 +1195,66 @@ __global__ void __launch_bounds__(BT) k_prop_block1(SweepArgs a, R rule, const i
             dec = __shfl_sync(FULL, dec, 0);
         }
         const bool rec = dec == DEC_MOVE && r > 0;
+        if constexpr (kListInS) {
+            // the holder is the first final-level candidate: entry 0 of the
+            // first range that has one (a fin_entry)
+            const int32_t holder = has_best ? fin_all[hw * span] : -1;
+            if (tid == 0) {
+                if (dec == DEC_AMBIGUOUS) {
+                    push_ambiguous(a, v, d);
+                } else {
+                    const int32_t hl = dec == DEC_MOVE ? fin_label(a, b, holder) : holder;
+                    a.ndraw[v] = tt;
+                    write_decision(a, v, dec, hl, curr);
+                    record_ties(a, v, b, rec, r, hl);
+                }
+            }
+            if (rec) {  // the same number of iterations in every lane
+                const long long off = (long long)b + v;  // record_ties' slots: holder, then the ties
+                for (int32_t j0 = 0; j0 < nfin; j0 += 32) {
+                    const int32_t j = j0 + lane, gi = before + j;  // 0 is the holder
+                    if (j < nfin && gi > 0) a.tiebuf[off + gi] = fin_label(a, b, fin_all[lo + j]);
+                }
+            }
+            par ^= 1;
+            continue;
+        }
         if (tid == 0) {
             if (dec == DEC_AMBIGUOUS) {
                 push_ambiguous(a, v, d);
             } else {
-                const int32_t hl = dec == DEC_MOVE ? fin_label(a, b, holder) : holder;
                 a.ndraw[v] = tt;
-                write_decision(a, v, dec, hl, curr);
-                record_ties(a, v, b, rec, r, hl);
+                a.nties[v] = rec ? r : 0;
+                if (dec != DEC_MOVE) write_decision(a, v, dec, -1, curr);
             }
         }
-        if (rec) {  // the same number of iterations in every lane
-            const long long off = (long long)b + v;  // record_ties' slots: holder, then the ties
-            for (int32_t j0 = 0; j0 < nfin; j0 += 32) {
-                const int32_t j = j0 + lane, gi = before + j;  // 0 is the holder
-                if (j < nfin && gi > 0) a.tiebuf[off + gi] = fin_label(a, b, fin_list[j]);
+        // a move: the final level's candidates in row order, the first (the
+        // holder, in the first range that has one) is the new label, and with
+        // ties every one goes to the vertex's slots of the tie buffer
+        // ([indices[v] + v, ...): the holder, then the ties)
+        if (dec == DEC_MOVE && nfin > 0 && (rec || wid == hw)) {
+            // ranks first, then every needed label read at once (a neighbour's
+            // current label), then the writes
+            const long long off = (long long)b + v;
+            int32_t gi[RPL];
+            int32_t j = before;
+#pragma unroll
+            for (int i = 0; i < RPL; ++i) {
+                const bool fin = key[i] != PK::ident() && PK::level(key[i]) == lfin;
+                const unsigned fm = __ballot_sync(FULL, fin);
+                const int32_t g = j + __popc(fm & lanemask_lt());
+                gi[i] = fin && (rec || g == 0) ? g : -1;
+                j += __popc(fm);
+            }
+            int32_t L[RPL];
+#pragma unroll
+            for (int i = 0; i < RPL; ++i) L[i] = gi[i] >= 0 ? a.g.adj[b + lo + 32 * i + lane] : -1;
+#pragma unroll
+            for (int i = 0; i < RPL; ++i) L[i] = L[i] >= 0 ? a.labels[L[i]] : -1;
+#pragma unroll
+            for (int i = 0; i < RPL; ++i) {
+                if (gi[i] == 0) a.new_labels[v] = L[i];
+                if (gi[i] >= 0 && rec) a.tiebuf[off + gi[i]] = L[i];
             }
         }
         par ^= 1;
@@ -1438,9 +1544,9 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
         K carry, mreal;
         warp_carry_in<PK, NW>(s_agg, wid, lane, carry, mreal);
         const auto lfin = PK::level(kmax(PK::init(), mreal));
-        uint32_t t = 0;
+        uint32_t t = 0, t_lane = 0;
         int32_t nfin = 0;
-        bool amb = false;
+        bool amb = false, a_lane = false;
         int32_t *fin_list = pos_lab + lo;  // entries already read are overwritten
         constexpr int UO = 4;  // 32-position steps whose loads are issued together
         for (int32_t base0 = lo; base0 < hi; base0 += 32 * UO) {
@@ -1462,10 +1568,11 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                 if (fin)  // a single vertex's community is listed by its position
                     fin_list[nfin + __popc(fm & lanemask_lt())] = fin_entry(lq[u], base0 + 32 * u + lane);
                 nfin += __popc(fm);
-                ordered_step<PK>(key, cand, lfin, carry, t, amb, lane);
+                tally_step<PK>(key, cand, lfin, carry, t, amb, t_lane, a_lane, lane);
             }
         }
-        amb = __any_sync(FULL, amb);
+        t += __reduce_add_sync(FULL, t_lane);
+        amb = __any_sync(FULL, amb || a_lane);
         if (lane == 0) {
             s_t[wid] = t;
             s_nfin[wid] = nfin;
@@ -1876,7 +1983,7 @@ static void launch_block1(pcd_graph *g, const SweepArgs &a, const R &rule, const
                           int32_t dmax, cudaStream_t st) {
     int32_t cap = 64;
     while (cap < 2 * dmax) cap <<= 1;
-    const size_t smem = (3ull * cap + (size_t)BT * RPL) * sizeof(int32_t);
+    const size_t smem = (3ull * cap + (block1_lists_in_pass<R>(BT) ? (size_t)BT * RPL : 0)) * sizeof(int32_t);
     cudaFuncSetAttribute(k_prop_block1<R, BT, RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_prop_block1<R, BT, RPL>, BT, smem);
