@@ -1305,6 +1305,7 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
     const bool singles = singleton_partition(a);
     K *pos_key = reinterpret_cast<K *>(gscratch + (int64_t)blockIdx.x * gstride);
     int32_t *pos_lab = reinterpret_cast<int32_t *>(pos_key + pos_cap);
+    constexpr bool kHubKeyOnRead = !std::is_same<R, RuleWCC>::value;
     // (position, label) grouped by part; starts on an 8-byte boundary whatever pos_cap is
     int2 *bucket = reinterpret_cast<int2 *>(pos_lab + ((pos_cap + 1) & ~1));
     for (int32_t i = tid; i < table_cap; i += BT) {
@@ -1322,6 +1323,20 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
         const int32_t b = a.g.indices[v], d = a.g.indices[v + 1] - b;
         const int32_t curr = a.labels[v];
         const R vr = rule.at(v);
+        // the packed key of a single vertex's community from its flag word,
+        // and a position's key (formed from pos_lab, or stored in pos_key)
+        auto flag_key = [&](int32_t lw) -> K {
+            Tag tag{0, 0};
+            const typename R::Key raw = vr.join_one(v, d, lw & 0x7fffffff, tag);
+            return R::usable(raw) ? PK::make(raw, 1) : PK::ident();
+        };
+        auto pos_key_at = [&](int32_t p) -> K {
+            if (kHubKeyOnRead) {
+                const int32_t lp = pos_lab[p];
+                if (lp < 0) return flag_key(lp);
+            }
+            return pos_key[p];
+        };
         if (vr.vertex_ambiguous(d)) {
             if (tid == 0) push_ambiguous(a, v, d);
             continue;
@@ -1370,22 +1385,17 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
                 continue;
             }
             // a single vertex's community occurs once in any row and is never
-            // the vertex's own: count 1, first at p, its key now from the
-            // volume in the flag word; pos_lab keeps the flag word, the parts
-            // below skip it, and its label is read back at the final level
-            typename R::Key raw[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                Tag tag{0, 0};
-                const int32_t p = p0 + u * BT + tid;
-                raw[u] = p < d && l[u] < 0 ? vr.join_one(v, d, l[u] & 0x7fffffff, tag) : R::identity();
-            }
+            // the vertex's own: count 1, first at p, its key from the volume
+            // in the flag word; pos_lab keeps the flag word, the parts below
+            // skip it, and its label is read back at the final level.  Its key
+            // is formed again where it is read (kHubKeyOnRead) rather than
+            // stored, except for WCC, whose gain is too costly to form twice.
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int32_t p = p0 + u * BT + tid;
                 if (p < d) {
                     pos_lab[p] = l[u];
-                    pos_key[p] = l[u] < 0 && R::usable(raw[u]) ? PK::make(raw[u], 1) : PK::ident();
+                    if (!kHubKeyOnRead || l[u] >= 0) pos_key[p] = l[u] < 0 ? flag_key(l[u]) : PK::ident();
                     nrest += l[u] >= 0;
                 }
             }
@@ -1536,7 +1546,7 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
         const int32_t span = ((d + NW - 1) / NW + 31) & ~31;
         const int32_t lo = min(d, wid * span), hi = min(d, lo + span);
         K wmax = PK::ident();
-        for (int32_t p = lo + lane; p < hi; p += 32) wmax = kmax(wmax, pos_key[p]);
+        for (int32_t p = lo + lane; p < hi; p += 32) wmax = kmax(wmax, pos_key_at(p));
 #pragma unroll
         for (int o = 16; o; o >>= 1) wmax = kmax(wmax, __shfl_xor_sync(FULL, wmax, o));
         if (lane == 0) s_agg[wid] = wmax;
@@ -1555,8 +1565,12 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
 #pragma unroll
             for (int u = 0; u < UO; ++u) {
                 const int32_t p = base0 + 32 * u + lane;
-                kq[u] = p < hi ? pos_key[p] : PK::ident();
                 lq[u] = p < hi ? pos_lab[p] : -1;  // < 0: a single vertex's flag word
+            }
+#pragma unroll
+            for (int u = 0; u < UO; ++u) {
+                const int32_t p = base0 + 32 * u + lane;
+                kq[u] = p >= hi ? PK::ident() : (kHubKeyOnRead && lq[u] < 0 ? flag_key(lq[u]) : pos_key[p]);
             }
             __syncwarp();  // these steps' labels are read before fin_list overwrites read entries
 #pragma unroll
