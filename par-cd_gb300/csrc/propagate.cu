@@ -978,6 +978,9 @@ __global__ void __launch_bounds__(BT, block1_min_blocks<R>(BT, RPL)) k_prop_bloc
     // registers until the decision; larger blocks, whose ordered pass holds
     // most of their time, list them only for a move
     constexpr bool kListInS = block1_lists_in_pass<R>(BT);
+    // WCC keys every candidate in K: its gain is an out-of-line FP64
+    // function, and calls from both passes would each save the live registers
+    constexpr bool kOneKeyInK = std::is_same<R, RuleWCC>::value;
     int32_t *fin_all = smem + 3 * table_cap;  // NW * 32 * RPL entries when kListInS
     __shared__ K s_agg[NW];
     __shared__ uint32_t s_t[NW];
@@ -1017,6 +1020,7 @@ __global__ void __launch_bounds__(BT, block1_min_blocks<R>(BT, RPL)) k_prop_bloc
         // it stands, every position a candidate of count 1)
         int32_t lab[RPL], slot[RPL];
         K key[RPL];
+        uint32_t one_mask = 0;  // kOneKeyInK: positions holding a flag word
 #pragma unroll
         for (int i = 0; i < RPL; ++i) {
             const int32_t p = lo + 32 * i + lane;
@@ -1036,10 +1040,14 @@ __global__ void __launch_bounds__(BT, block1_min_blocks<R>(BT, RPL)) k_prop_bloc
             } else if (!singles) {
                 const int32_t l = lab[i];
                 if (l < 0) {  // a single vertex's community: count 1, first here
-                    Tag tag{0, 0};
-                    const typename R::Key raw = vr.join_one(v, d, l & 0x7fffffff, tag);
-                    if (R::usable(raw)) key[i] = PK::make(raw, 1);
-                    lab[i] = -2;  // listed by its position if it reaches the final level
+                    if constexpr (kOneKeyInK) {
+                        one_mask |= 1u << i;  // keyed in K, beside the table's candidates
+                    } else {
+                        Tag tag{0, 0};
+                        const typename R::Key raw = vr.join_one(v, d, l & 0x7fffffff, tag);
+                        if (R::usable(raw)) key[i] = PK::make(raw, 1);
+                        lab[i] = -2;  // listed by its position if it reaches the final level
+                    }
                 } else {
                     uint32_t h = hash_label(l) & (uint32_t)(ts - 1);
                     for (;;) {
@@ -1097,6 +1105,12 @@ __global__ void __launch_bounds__(BT, block1_min_blocks<R>(BT, RPL)) k_prop_bloc
         } else {
 #pragma unroll
             for (int i = 0; i < RPL; ++i) {
+                if (kOneKeyInK && ((one_mask >> i) & 1u)) {
+                    Tag tag{0, 0};
+                    const typename R::Key raw = vr.join_one(v, d, lab[i] & 0x7fffffff, tag);
+                    if (R::usable(raw)) key[i] = PK::make(raw, 1);
+                    lab[i] = -2;
+                }
                 if (kc[i] > 0) {
                     if (lab[i] == curr) {
                         s_curr_freq[par] = kc[i];
