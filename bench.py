@@ -780,6 +780,19 @@ def powerlaw_leg(args, dev):
         ms = timed_sweeps(G, rule, start, seed, args.pl_reps + 1, stream)[1:]
         rec["sweep1_ms"] = statistics.median(ms)
         rec["sweep1_edges_per_s"] = m / (rec["sweep1_ms"] / 1e3)
+        # the same sweep once more with CUDA events between the class launches
+        try:
+            ctx.profile(True)
+            timed_sweeps(G, rule, start, seed, 1, stream)
+            phases = {}
+            for nm, t_ms in ctx.profile_read():  # a class may run as several launches
+                if nm.startswith("sweep."):
+                    phases[nm] = round(phases.get(nm, 0.0) + t_ms, 4)
+            rec["sweep1_phases_ms"] = phases
+        except Exception as e:  # the spans are a diagnostic: the leg goes on without them
+            rec["sweep1_phases_ms"] = {"unavailable": str(e)[:200]}
+        finally:
+            ctx.profile(False)
         torch.cuda.synchronize()
         t = time.perf_counter()
         res = pcd.run(G, rule, 2, 1.0, 1, iters, 0.0, init, keep_raw=True, initial_on_device=True)
