@@ -290,3 +290,44 @@ def test_threaded_triangles_and_wcc_score_equal_the_sequential_ones():
     lab, _ = p.compress(p.clustering())
     st = p.stats(lab)
     assert p.score(2, 0.0, lab, st) == p.score(2, 0.0, lab, st, threads=4)
+
+
+def test_single_vertex_community_facts_behind_the_flag_word():
+    """The sweep kernels replace the label of a neighbour that is alone in its
+    community by that community's volume (bit 31 set) and form its gain from
+    size 1, no internal edge and that volume, without reading the community's
+    statistics.  Pinned here on the oracle's statistics (the reference's
+    collect_statistics restated) for golden graphs under random partitions:
+    such a community has internal volume 0 and external volume = volume = its
+    vertex's degree, its label occurs at most once in any row, and never in
+    its own vertex's row."""
+    import oracle
+
+    port = oracle.Port()
+    rng = np.random.default_rng(17)
+    for name in ("rmat12", "pl20k", "sbm10k"):
+        g = golden_graph(name)
+        port.load(g.indices, g.adj)
+        deg = np.diff(g.indices)
+        for k in (g.n // 2, g.n // 8, g.n // 64):
+            # k random communities, and about a third of the vertices alone
+            # (labels kept in [0, n), the range the reference's relabelling takes)
+            lab0, k0 = port.compress(rng.integers(0, max(k, 1), size=g.n).astype(np.int32))
+            alone = rng.random(g.n) < 0.33
+            lab0[alone] = k0 + np.arange(int(alone.sum()), dtype=np.int32)
+            comp, _ = port.compress(lab0)
+            st = port.stats(comp)
+            one = st.sizes == 1
+            assert one.any()
+            assert np.all(st.int_volume[one] == 0)
+            owner = np.empty(st.k, np.int64)
+            owner[comp] = np.arange(g.n)  # a single-vertex community's only vertex
+            assert np.array_equal(st.ext_volume[one], deg[owner[one]])
+            row_of = np.repeat(np.arange(g.n), deg)
+            lab = comp[g.adj]
+            flagged = one[lab]
+            # at most once per row: (row, label) pairs of flagged entries are distinct
+            pairs = row_of[flagged].astype(np.int64) * st.k + lab[flagged]
+            assert np.unique(pairs).size == pairs.size
+            # never the row's own label
+            assert not np.any(lab[flagged] == comp[row_of[flagged]])
