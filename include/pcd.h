@@ -113,10 +113,12 @@ pcd_status pcd_graph_free(pcd_graph *g);
  * (par-cd_gb300/tune.py) and the tests move them. */
 pcd_status pcd_graph_set_bins(pcd_graph *g, const int32_t max_deg[7]);
 pcd_status pcd_graph_get_bins(pcd_graph *g, int32_t max_deg[7], int64_t counts[8]);
-/* No counterpart in the reference.  Distinct labels per hash part of the hub
- * kernel (default 6144, range [1024, 8192]: a part must fit half of the
- * 16384-slot shared table).  Results do not depend on it; the autotuner moves
- * it. */
+/* No counterpart in the reference.  Size of a hash part of the hub kernel:
+ * a hub row's entries whose neighbour is not alone in its community are split
+ * into ceil(entries / labels) parts by label hash, each histogrammed in the
+ * 16384-slot shared table (default 6144, range [1024, 8192]: a part's labels
+ * must fit half of the table).  Results do not depend on it; the autotuner
+ * moves it. */
 pcd_status pcd_graph_set_hub_part(pcd_graph *g, int32_t labels);
 
 /* Device memory a graph or batch holds right now (every buffer libpcd
