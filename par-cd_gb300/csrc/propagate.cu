@@ -366,20 +366,43 @@ __device__ __forceinline__ void tally_step(typename PK::K key, bool cand, L lfin
 // per lane and a shuffle scan (rather than every thread reading all NW
 // entries).  carry: the maximum of `init` and the maxima of the warps before
 // `wid`; mreal: the maximum over all warps.
+// Maximum over the warp.  Integer keys: two 32-bit warp reductions, the high
+// words (signed) and then the low words (unsigned) of the lanes that hold the
+// top high word, which orders like the signed 64-bit value; FP64 keys: a
+// butterfly of shuffles.
+__device__ __forceinline__ long long warp_max(long long x) {
+    const int hi = (int)(x >> 32);
+    const int top = __reduce_max_sync(FULL, hi);
+    const unsigned lo = __reduce_max_sync(FULL, hi == top ? (unsigned)x : 0u);
+    return (long long)(((unsigned long long)(unsigned)top << 32) | lo);
+}
+__device__ __forceinline__ double warp_max(double x) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) x = kmax(x, __shfl_xor_sync(FULL, x, o));
+    return x;
+}
+
 template <class PK, int NW>
 __device__ __forceinline__ void warp_carry_in(const typename PK::K *s_agg, int wid, int lane, typename PK::K &carry,
                                               typename PK::K &mreal) {
     static_assert(NW <= 32, "one lane per warp");
     using K = typename PK::K;
-    K inc = lane < NW ? s_agg[lane] : PK::ident();
+    const K mine = lane < NW ? s_agg[lane] : PK::ident();
+    if constexpr (std::is_same<K, long long>::value) {  // two reductions instead of a scan
+        mreal = warp_max(mine);
+        const K before = warp_max(lane < wid ? mine : PK::ident());
+        carry = wid > 0 ? kmax(PK::init(), before) : PK::init();
+    } else {
+        K inc = mine;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const K y = __shfl_up_sync(FULL, inc, o);
-        if (lane >= o) inc = kmax(inc, y);
+        for (int o = 1; o < 32; o <<= 1) {
+            const K y = __shfl_up_sync(FULL, inc, o);
+            if (lane >= o) inc = kmax(inc, y);
+        }
+        mreal = __shfl_sync(FULL, inc, 31);
+        const K before = __shfl_sync(FULL, inc, wid > 0 ? wid - 1 : 0);
+        carry = wid > 0 ? kmax(PK::init(), before) : PK::init();
     }
-    mreal = __shfl_sync(FULL, inc, 31);
-    const K before = __shfl_sync(FULL, inc, wid > 0 ? wid - 1 : 0);
-    carry = wid > 0 ? kmax(PK::init(), before) : PK::init();
 }
 
 // tt: the sum of the warps' tie counts (mod 2^32); nf: the final-level
@@ -533,8 +556,7 @@ __global__ void __launch_bounds__(256) k_prop_warp(SweepArgs a, R rule, const in
             }
             wmax = kmax(wmax, key[c]);
         }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) wmax = kmax(wmax, __shfl_xor_sync(FULL, wmax, o));
+        wmax = warp_max(wmax);
         const K mreal = wmax;
         const auto lfin = PK::level(kmax(PK::init(), mreal));
         K carry = PK::init();
@@ -1123,8 +1145,7 @@ __global__ void __launch_bounds__(BT, block1_min_blocks<R>(BT, RPL)) k_prop_bloc
                 wmax = kmax(wmax, key[i]);
             }
         }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) wmax = kmax(wmax, __shfl_xor_sync(FULL, wmax, o));
+        wmax = warp_max(wmax);
         if (lane == 0) s_agg[wid] = wmax;
         __syncthreads();
         K carry, mreal;
@@ -1561,8 +1582,7 @@ __global__ void __launch_bounds__(1024) k_prop_hub_parts(SweepArgs a, R rule, co
         const int32_t lo = min(d, wid * span), hi = min(d, lo + span);
         K wmax = PK::ident();
         for (int32_t p = lo + lane; p < hi; p += 32) wmax = kmax(wmax, pos_key_at(p));
-#pragma unroll
-        for (int o = 16; o; o >>= 1) wmax = kmax(wmax, __shfl_xor_sync(FULL, wmax, o));
+        wmax = warp_max(wmax);
         if (lane == 0) s_agg[wid] = wmax;
         __syncthreads();
         K carry, mreal;
